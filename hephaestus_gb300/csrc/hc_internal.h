@@ -1,0 +1,174 @@
+// hc_internal.h -- shared declarations of the GB300 H(curl) operator library.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "hcurl_op.h"
+
+namespace hc {
+
+constexpr int kMaxP = 3;             // hex orders 1..3
+constexpr int kRedBlocks = 304;      // 2 x 152 SMs: blocks of every grid-stride vector kernel
+constexpr int kRedThreads = 512;
+constexpr int kMaxLanczos = 64;
+
+// 1-D operators of the hex element on [0,1]: closed (Gauss-Lobatto nodal, p+1
+// functions) and open (Gauss-Legendre nodal, p functions) bases.
+//   Mcc[i][j] = int phi^c_i phi^c_j,  Mco[i][j] = int phi^c_i phi^o_j,
+//   Moo[i][j] = int phi^o_i phi^o_j,  D[a][j] = (phi^c_j)'(x^o_a)
+// D expands the derivative of a closed function in the open basis exactly.
+template <typename T>
+struct Tab1D {
+  T Mcc[kMaxP + 1][kMaxP + 1];
+  T Mco[kMaxP + 1][kMaxP];
+  T Moo[kMaxP][kMaxP];
+  T D[kMaxP][kMaxP + 1];
+};
+void build_tab1d(int p, Tab1D<double>* t);  // host, FP64
+
+// Device-resident scalars of one Krylov solve: the host reads them once per
+// batch of iterations, never per iteration.
+struct KrylovScalars {
+  double rz;       // r.z of the current iterate
+  double pq;       // p.Jp (starts as the essential-dof part, then the apply adds)
+  double rr;       // r.r
+  double bb;       // b.b
+  double tol2;     // squared absolute stopping threshold
+  double rtol2, atol2;
+  double alpha, beta;
+  double lz[2 * kMaxLanczos + 2];  // Lanczos alphas, betas
+  int it;          // completed iterations
+  int done;        // 1 = stop (converged or failed)
+  int status;      // hc_status when done
+  int maxit;
+  unsigned int counter[8];  // tickets of the grid reductions
+};
+
+// Structured hex problem as the kernels see it.  Factors are SoA:
+// fac[k*ne + e], k = 0..5 the mass tensor sigma |det J| J^-1 J^-T, k = 6..11 the
+// curl tensor dt nu / |det J| J^T J, each packed symmetric (00,01,02,11,12,22).
+struct HexDev {
+  int p, nx, ny, nz;
+  int64_t ne, ndof;
+  int64_t off[3];
+  int full;           // 1 = general parallelepipeds (9 tensor blocks), 0 = axis aligned
+  int ess_bits;       // face attribute bits (implicit mask)
+  const uint8_t* ess; // explicit device mask or nullptr
+  const double* fac;  // FP64 factors (diagonal, FP64 apply)
+};
+
+}  // namespace hc
+
+struct hcop {
+  int type = HC_HEX;
+  int p = 1;
+  int nx = 0, ny = 0, nz = 0;
+  int64_t ndof = 0, ne = 0;
+  int64_t off[3] = {0, 0, 0};
+  double dt = 1.0;
+  bool has_mass = false;
+  bool full = false;
+  int ess_bits = 0;
+  bool explicit_mask = false;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  std::vector<uint8_t> ess_host;
+
+  // device memory owned by the handle
+  double* fac = nullptr;      // 12*ne FP64 factors
+  float* facf = nullptr;      // 12*ne FP32 copy (FP32 apply)
+  uint8_t* ess = nullptr;     // ndof essential flags
+  double* diag = nullptr;     // ndof diagonal of J
+  double* dinv = nullptr;     // ndof 1/diag
+  float* dinvf = nullptr;     // FP32 copy
+  double* sdinv = nullptr;    // 1/sqrt(diag)
+  float* sdinvf = nullptr;
+  hc::KrylovScalars* scal = nullptr;   // device scalars
+  hc::KrylovScalars* hscal = nullptr;  // pinned host mirror
+  double* partials = nullptr;          // device, reduction partials
+  void* work = nullptr;                // Krylov vectors
+  size_t work_bytes = 0;
+  double* xbuf = nullptr;              // device staging for host-pointer calls
+  double* ybuf = nullptr;
+  double lmax64 = 0.0, lmax32 = 0.0;   // cached Chebyshev bounds
+
+  hc::HexDev hexdev() const {
+    hc::HexDev d;
+    d.p = p;
+    d.nx = nx;
+    d.ny = ny;
+    d.nz = nz;
+    d.ne = ne;
+    d.ndof = ndof;
+    d.off[0] = off[0];
+    d.off[1] = off[1];
+    d.off[2] = off[2];
+    d.full = full ? 1 : 0;
+    d.ess_bits = ess_bits;
+    d.ess = explicit_mask ? ess : nullptr;
+    d.fac = fac;
+    return d;
+  }
+};
+
+namespace hc {
+// ---- hc_hex.cu ----
+cudaError_t upload_tables();
+int hex_apply_blocks(const HexDev& d);
+// y += op(x).  masked: skip essential rows and zero essential entries of x
+// (y must already hold (I-P)x for J).  mscale/cscale multiply the mass/curl
+// factors.  S != nullptr: PCG mode (energy p.Jp accumulated onto S->pq,
+// alpha formed, skipped when S->done).
+template <typename T>
+cudaError_t hex_apply(const HexDev& d, const T* fac, const T* x, T* y, double mscale, double cscale,
+                      bool masked, KrylovScalars* S, double* partials, cudaStream_t s);
+cudaError_t hex_diag(const HexDev& d, double* diag, cudaStream_t s);
+
+// ---- hc_krylov.cu ----
+cudaError_t diag_finish(int64_t n, const uint8_t* ess, double* d, double* dinv, float* dinvf, double* sd,
+                        float* sdf, cudaStream_t s);
+template <typename T>
+cudaError_t init_masked(int64_t n, const uint8_t* ess, const T* x, T* y, cudaStream_t s);
+// operator callback used by the solvers: y = J x with y pre-initialised by the
+// callee; S/partials as in hex_apply
+template <typename T>
+struct OpJ {
+  hcop* h;
+  const T* fac;
+  cudaError_t apply(const T* x, T* y, KrylovScalars* S, double* partials, cudaStream_t s) const;
+};
+struct SolveCfg {
+  int precond;
+  int cheb_degree;
+  double cheb_ratio;
+  double lmax;
+  double rtol, atol;
+  int maxit;
+};
+// Preconditioned CG on J x = b, device vectors of type T, x = initial guess.
+template <typename T>
+hc_status pcg_device(hcop* h, const SolveCfg& cfg, const T* b, T* x, int* iters, int* applies,
+                     double* relres_dev_norm);
+// Lanczos estimate of lambda_max(D^-1 J) with operator precision T.
+template <typename T>
+hc_status lanczos_device(hcop* h, int steps, double* lmax);
+// Mixed precision: FP32 inner PCG in FP64 iterative refinement.
+hc_status mixed_device(hcop* h, const hc_solve_params* prm, const double* b, double* x,
+                       hc_solve_info* info);
+hc_status ensure_work(hcop* h, size_t bytes);
+cudaError_t ensure_scalars(hcop* h);
+double vec_norm2_host(hcop* h, const double* x, int64_t n);  // synchronous helper
+
+}  // namespace hc
+
+#define HC_CUDA_TRY(h, expr)                                                              \
+  do {                                                                                    \
+    cudaError_t _e = (expr);                                                              \
+    if (_e != cudaSuccess) {                                                              \
+      (h)->err = std::string(#expr) + ": " + cudaGetErrorString(_e);                      \
+      return HC_ECUDA;                                                                    \
+    }                                                                                     \
+  } while (0)

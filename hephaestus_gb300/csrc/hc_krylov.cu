@@ -1,0 +1,688 @@
+// hc_krylov.cu -- device PCG, Chebyshev-Jacobi preconditioner, Lanczos bound,
+// and FP32-inner / FP64-outer iterative refinement.
+//
+// Replaces, for this operator, the HyprePCG solve of the reference
+// (src/formulations/HCurl/hcurl_formulation.cpp:81-85,
+// src/problem_builders/problem_builder_base.cpp:221-253,
+// src/solvers/hephaestus_solvers.hpp:34-57).  All scalars (alpha, beta, dots,
+// the stopping test) live in device memory; the host reads them once per batch
+// of iterations.  Vector kernels are grid-stride streams over 2 x 152 blocks;
+// every dot is a deterministic two-level FP64 reduction (FP32 products are
+// summed in FP32 over runs of 8 before entering FP64).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "hc_internal.h"
+#include "hc_reduce.cuh"
+
+namespace hc {
+
+#define GS_LOOP(i, n) \
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
+
+static inline unsigned vgrid(int64_t n) {
+  int64_t b = (n + kRedThreads - 1) / kRedThreads;
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, kRedBlocks));
+}
+
+// ---------------------------------------------------------------------------
+// setup kernels
+// ---------------------------------------------------------------------------
+__global__ void k_diag_finish(int64_t n, const uint8_t* __restrict__ ess, double* d, double* dinv, float* dinvf,
+                              double* sd, float* sdf, int* bad) {
+  GS_LOOP(i, n) {
+    double v = ess[i] ? 1.0 : d[i];
+    if (!(v > 0.0) || !isfinite(v)) {
+      atomicExch(bad, 1);
+      v = 1.0;
+    }
+    d[i] = v;
+    const double iv = 1.0 / v;
+    dinv[i] = iv;
+    dinvf[i] = (float)iv;
+    const double s = sqrt(iv);
+    sd[i] = s;
+    sdf[i] = (float)s;
+  }
+}
+
+cudaError_t diag_finish(int64_t n, const uint8_t* ess, double* d, double* dinv, float* dinvf, double* sd,
+                        float* sdf, cudaStream_t s) {
+  int* bad = nullptr;
+  cudaError_t e = cudaMallocAsync(&bad, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  cudaMemsetAsync(bad, 0, sizeof(int), s);
+  k_diag_finish<<<vgrid(n), kRedThreads, 0, s>>>(n, ess, d, dinv, dinvf, sd, sdf, bad);
+  int hb = 0;
+  cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, s);
+  e = cudaStreamSynchronize(s);
+  cudaFreeAsync(bad, s);
+  if (e != cudaSuccess) return e;
+  return hb ? cudaErrorInvalidValue : cudaGetLastError();
+}
+
+template <typename T>
+__global__ void k_init_masked(int64_t n, const uint8_t* __restrict__ ess, const T* __restrict__ x,
+                              T* __restrict__ y) {
+  GS_LOOP(i, n) y[i] = ess[i] ? x[i] : T(0);
+}
+template <typename T>
+cudaError_t init_masked(int64_t n, const uint8_t* ess, const T* x, T* y, cudaStream_t s) {
+  k_init_masked<T><<<vgrid(n), kRedThreads, 0, s>>>(n, ess, x, y);
+  return cudaGetLastError();
+}
+template cudaError_t init_masked<double>(int64_t, const uint8_t*, const double*, double*, cudaStream_t);
+template cudaError_t init_masked<float>(int64_t, const uint8_t*, const float*, float*, cudaStream_t);
+
+template <typename T>
+cudaError_t OpJ<T>::apply(const T* x, T* y, KrylovScalars* S, double* partials, cudaStream_t s) const {
+  const HexDev d = h->hexdev();
+  return hex_apply<T>(d, fac, x, y, h->has_mass ? 1.0 : 0.0, 1.0, true, S, partials, s);
+}
+template struct OpJ<double>;
+template struct OpJ<float>;
+
+// ---------------------------------------------------------------------------
+// PCG kernels
+// ---------------------------------------------------------------------------
+// r = b - q (q = J x0); bb, rr and (Jacobi) rz; initial stopping test
+template <typename T, bool JAC>
+__global__ void __launch_bounds__(kRedThreads)
+    k_pcg_setup(int64_t n, const T* __restrict__ b, const T* __restrict__ q, T* __restrict__ r,
+                const T* __restrict__ dinv, KrylovScalars* S, double* partials) {
+  double v[3] = {0.0, 0.0, 0.0}, tot[3];
+  GS_LOOP(i, n) {
+    const double bi = (double)b[i];
+    const double ri = bi - (double)q[i];
+    r[i] = (T)ri;
+    v[0] += bi * bi;
+    v[1] += ri * ri;
+    if (JAC) v[2] += ri * ri * (dinv ? (double)dinv[i] : 1.0);
+  }
+  block_sum_n<3>(v);
+  if (grid_sum_n<3>(v, partials, &S->counter[4], tot)) {
+    S->bb = tot[0];
+    S->rr = tot[1];
+    S->tol2 = fmax(S->rtol2 * tot[0], S->atol2);
+    if (JAC) S->rz = tot[2];
+    S->it = 0;
+    S->beta = 0.0;
+    S->done = 0;
+    S->status = HC_NOT_CONVERGED;
+    if (!isfinite(tot[0]) || !isfinite(tot[1])) {
+      S->done = 1;
+      S->status = HC_BREAKDOWN;
+    } else if (tot[1] <= S->tol2) {
+      S->done = 1;
+      S->status = HC_OK;
+    }
+  }
+}
+
+// x += alpha p; r -= alpha q; rr (and Jacobi rz = r.D^-1 r); stopping test; beta
+template <typename T, bool JAC>
+__global__ void __launch_bounds__(kRedThreads)
+    k_pcg_update(int64_t n, T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
+                 const T* __restrict__ q, const T* __restrict__ dinv, KrylovScalars* S, double* partials) {
+  if (S->done) return;
+  const T a = (T)S->alpha;
+  double v[2] = {0.0, 0.0}, tot[2];
+  T rrt = T(0), rzt = T(0);
+  int c = 0;
+  GS_LOOP(i, n) {
+    x[i] += a * p[i];
+    const T ri = r[i] - a * q[i];
+    r[i] = ri;
+    rrt += ri * ri;
+    if (JAC) rzt += ri * ri * (dinv ? dinv[i] : T(1));
+    if (++c == 8) {
+      v[0] += (double)rrt;
+      v[1] += (double)rzt;
+      rrt = rzt = T(0);
+      c = 0;
+    }
+  }
+  v[0] += (double)rrt;
+  v[1] += (double)rzt;
+  block_sum_n<2>(v);
+  if (grid_sum_n<2>(v, partials, &S->counter[2], tot)) {
+    S->rr = tot[0];
+    S->it += 1;
+    if (!isfinite(tot[0])) {
+      S->done = 1;
+      S->status = HC_BREAKDOWN;
+    } else if (tot[0] <= S->tol2) {
+      S->done = 1;
+      S->status = HC_OK;
+    } else if (S->it >= S->maxit) {
+      S->done = 1;
+      S->status = HC_NOT_CONVERGED;
+    }
+    if (JAC) {
+      S->beta = tot[1] / S->rz;
+      S->rz = tot[1];
+    }
+  }
+}
+
+// p = z + beta p (z = D^-1 r for Jacobi); q = (I-P) p; S->pq = sum_ess p_i^2
+template <typename T, bool JAC>
+__global__ void __launch_bounds__(kRedThreads)
+    k_pcg_dir(int64_t n, const T* __restrict__ zr, const T* __restrict__ dinv, T* __restrict__ p,
+              T* __restrict__ q, const uint8_t* __restrict__ ess, KrylovScalars* S, double* partials) {
+  if (S->done) return;
+  const T b = (T)S->beta;
+  double v[1] = {0.0}, tot[1];
+  GS_LOOP(i, n) {
+    const T z = JAC ? (dinv ? dinv[i] * zr[i] : zr[i]) : zr[i];
+    const T pi = z + b * p[i];
+    p[i] = pi;
+    const bool e = ess[i] != 0;
+    q[i] = e ? pi : T(0);
+    if (e) v[0] += (double)pi * (double)pi;
+  }
+  block_sum_n<1>(v);
+  if (grid_sum_n<1>(v, partials, &S->counter[3], tot)) S->pq = tot[0];
+}
+
+// rz = r.z ; first: beta = 0, else beta = rz_new / rz
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+    k_rz_beta(int64_t n, const T* __restrict__ r, const T* __restrict__ z, int first, KrylovScalars* S,
+              double* partials) {
+  if (S->done) return;
+  double v[1] = {0.0}, tot[1];
+  T acc = T(0);
+  int c = 0;
+  GS_LOOP(i, n) {
+    acc += r[i] * z[i];
+    if (++c == 8) {
+      v[0] += (double)acc;
+      acc = T(0);
+      c = 0;
+    }
+  }
+  v[0] += (double)acc;
+  block_sum_n<1>(v);
+  if (grid_sum_n<1>(v, partials, &S->counter[5], tot)) {
+    if (first) {
+      S->beta = 0.0;
+    } else {
+      S->beta = tot[0] / S->rz;
+    }
+    S->rz = tot[0];
+  }
+}
+
+// Chebyshev iteration (Saad, Iterative Methods for Sparse Linear Systems,
+// Alg. 12.1) on D^-1 J z = D^-1 r, zero start, fixed degree: a fixed SPD
+// polynomial preconditioner when lmax bounds the spectrum of D^-1 J.
+template <typename T>
+__global__ void k_cheb0(int64_t n, const T* __restrict__ r, const T* __restrict__ dinv, T* __restrict__ z,
+                        T* __restrict__ dk, T* __restrict__ w, const uint8_t* __restrict__ ess, T inv_theta,
+                        const KrylovScalars* S) {
+  if (S->done) return;
+  GS_LOOP(i, n) {
+    const T zi = r[i] * dinv[i] * inv_theta;
+    z[i] = zi;
+    dk[i] = zi;
+    w[i] = ess[i] ? zi : T(0);
+  }
+}
+template <typename T>
+__global__ void k_chebk(int64_t n, const T* __restrict__ r, const T* __restrict__ dinv, T* __restrict__ z,
+                        T* __restrict__ dk, T* __restrict__ w, const uint8_t* __restrict__ ess, T c1, T c2,
+                        int init_next, const KrylovScalars* S) {
+  if (S->done) return;
+  GS_LOOP(i, n) {
+    const T d = c1 * dk[i] + c2 * dinv[i] * (r[i] - w[i]);
+    dk[i] = d;
+    const T zi = z[i] + d;
+    z[i] = zi;
+    if (init_next) w[i] = ess[i] ? zi : T(0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Lanczos kernels on D^-1/2 J D^-1/2
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_lz_start(int64_t n, T* __restrict__ v, KrylovScalars* S, double* partials) {
+  double a[1] = {0.0}, tot[1];
+  GS_LOOP(i, n) {
+    const double t = (double)i * 0.6180339887498949;
+    const T vi = (T)(t - floor(t) - 0.5);
+    v[i] = vi;
+    a[0] += (double)vi * (double)vi;
+  }
+  block_sum_n<1>(a);
+  if (grid_sum_n<1>(a, partials, &S->counter[6], tot)) S->rr = tot[0];
+}
+template <typename T>
+__global__ void k_lz_scale0(int64_t n, T* __restrict__ v, T* __restrict__ vp, const KrylovScalars* S) {
+  const T s = (T)(1.0 / sqrt(S->rr));
+  GS_LOOP(i, n) {
+    v[i] *= s;
+    vp[i] = T(0);
+  }
+}
+template <typename T>
+__global__ void k_lz_pre(int64_t n, const T* __restrict__ v, const T* __restrict__ sd, T* __restrict__ tmp,
+                         T* __restrict__ w, const uint8_t* __restrict__ ess) {
+  GS_LOOP(i, n) {
+    const T t = sd[i] * v[i];
+    tmp[i] = t;
+    w[i] = ess[i] ? t : T(0);
+  }
+}
+template <typename T>
+__global__ void k_lz_alpha(int64_t n, T* __restrict__ w, const T* __restrict__ sd, const T* __restrict__ v,
+                           KrylovScalars* S, double* partials, int j) {
+  double a[1] = {0.0}, tot[1];
+  GS_LOOP(i, n) {
+    const T wi = sd[i] * w[i];
+    w[i] = wi;
+    a[0] += (double)wi * (double)v[i];
+  }
+  block_sum_n<1>(a);
+  if (grid_sum_n<1>(a, partials, &S->counter[6], tot)) S->lz[j] = tot[0];
+}
+template <typename T>
+__global__ void k_lz_update(int64_t n, T* __restrict__ w, const T* __restrict__ v, const T* __restrict__ vp,
+                            KrylovScalars* S, double* partials, int j) {
+  const T a = (T)S->lz[j], b = (T)S->lz[kMaxLanczos + j];
+  double s[1] = {0.0}, tot[1];
+  GS_LOOP(i, n) {
+    const T wi = w[i] - a * v[i] - b * vp[i];
+    w[i] = wi;
+    s[0] += (double)wi * (double)wi;
+  }
+  block_sum_n<1>(s);
+  if (grid_sum_n<1>(s, partials, &S->counter[6], tot)) S->lz[kMaxLanczos + j + 1] = sqrt(tot[0]);
+}
+template <typename T>
+__global__ void k_lz_shift(int64_t n, const T* __restrict__ w, T* __restrict__ v, T* __restrict__ vp,
+                           const KrylovScalars* S, int j) {
+  const double bn = S->lz[kMaxLanczos + j + 1];
+  const T ib = bn > 0.0 ? (T)(1.0 / bn) : T(0);
+  GS_LOOP(i, n) {
+    vp[i] = v[i];
+    v[i] = w[i] * ib;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// refinement kernels (FP64 outer)
+// ---------------------------------------------------------------------------
+// r = b - r (r holds J x); returns ||r||^2 and ||b||^2 into S->rr, S->bb
+__global__ void __launch_bounds__(kRedThreads)
+    k_resid64(int64_t n, const double* __restrict__ b, double* __restrict__ r, KrylovScalars* S, double* partials) {
+  double v[2] = {0.0, 0.0}, tot[2];
+  GS_LOOP(i, n) {
+    const double bi = b[i];
+    const double ri = bi - r[i];
+    r[i] = ri;
+    v[0] += ri * ri;
+    v[1] += bi * bi;
+  }
+  block_sum_n<2>(v);
+  if (grid_sum_n<2>(v, partials, &S->counter[7], tot)) {
+    S->rr = tot[0];
+    S->bb = tot[1];
+  }
+}
+__global__ void k_d2f_scaled(int64_t n, const double* __restrict__ r, float* __restrict__ rf, double s) {
+  GS_LOOP(i, n) rf[i] = (float)(r[i] * s);
+}
+__global__ void k_axpy_f2d(int64_t n, const float* __restrict__ c, double* __restrict__ x, double s) {
+  GS_LOOP(i, n) x[i] += s * (double)c[i];
+}
+
+// ---------------------------------------------------------------------------
+// host drivers
+// ---------------------------------------------------------------------------
+cudaError_t ensure_scalars(hcop* h) {
+  if (h->scal) return cudaSuccess;
+  cudaError_t e = cudaMalloc(&h->scal, sizeof(KrylovScalars));
+  if (e != cudaSuccess) return e;
+  e = cudaMemset(h->scal, 0, sizeof(KrylovScalars));
+  if (e != cudaSuccess) return e;
+  e = cudaMallocHost(&h->hscal, sizeof(KrylovScalars));
+  if (e != cudaSuccess) return e;
+  const HexDev d = h->hexdev();
+  const size_t np = (size_t)std::max(kRedBlocks, hex_apply_blocks(d)) * 4;
+  return cudaMalloc(&h->partials, np * sizeof(double));
+}
+
+hc_status ensure_work(hcop* h, size_t bytes) {
+  if (h->work_bytes >= bytes) return HC_OK;
+  if (h->work) cudaFree(h->work);
+  h->work = nullptr;
+  h->work_bytes = 0;
+  cudaError_t e = cudaMalloc(&h->work, bytes);
+  if (e != cudaSuccess) {
+    h->err = std::string("work space allocation failed: ") + cudaGetErrorString(e);
+    return HC_ENOMEM;
+  }
+  h->work_bytes = bytes;
+  return HC_OK;
+}
+
+// largest eigenvalue of the symmetric tridiagonal (a, b) by Sturm bisection
+static double tridiag_lmax(const std::vector<double>& a, const std::vector<double>& b) {
+  const int m = (int)a.size();
+  double lo = 1e300, hi = -1e300;
+  for (int i = 0; i < m; ++i) {
+    const double rad = (i > 0 ? std::fabs(b[i - 1]) : 0.0) + (i + 1 < m ? std::fabs(b[i]) : 0.0);
+    lo = std::min(lo, a[i] - rad);
+    hi = std::max(hi, a[i] + rad);
+  }
+  for (int it = 0; it < 200; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    int below = 0;
+    double q = 1.0;
+    for (int i = 0; i < m; ++i) {
+      q = a[i] - mid - (i > 0 ? b[i - 1] * b[i - 1] / q : 0.0);
+      if (q == 0.0) q = 1e-300;
+      if (q < 0.0) ++below;
+    }
+    if (below >= m) hi = mid;
+    else lo = mid;
+  }
+  return hi;
+}
+
+template <typename T>
+static const T* sd_of(hcop* h);
+template <>
+const double* sd_of<double>(hcop* h) {
+  return h->sdinv;
+}
+template <>
+const float* sd_of<float>(hcop* h) {
+  return h->sdinvf;
+}
+template <typename T>
+static const T* dinv_of(hcop* h);
+template <>
+const double* dinv_of<double>(hcop* h) {
+  return h->dinv;
+}
+template <>
+const float* dinv_of<float>(hcop* h) {
+  return h->dinvf;
+}
+template <typename T>
+static const T* fac_of(hcop* h);
+template <>
+const double* fac_of<double>(hcop* h) {
+  return h->fac;
+}
+template <>
+const float* fac_of<float>(hcop* h) {
+  return h->facf;
+}
+
+template <typename T>
+hc_status lanczos_device(hcop* h, int steps, double* lmax, T* wk) {
+  if (steps < 2 || steps > kMaxLanczos) {
+    h->err = "Lanczos steps must be in [2, 64]";
+    return HC_EINVAL;
+  }
+  HC_CUDA_TRY(h, ensure_scalars(h));
+  const int64_t n = h->ndof;
+  cudaStream_t s = h->stream;
+  T *v = wk, *vp = wk + n, *w = wk + 2 * n, *tmp = wk + 3 * n;
+  KrylovScalars* S = h->scal;
+  const unsigned g = vgrid(n);
+  const OpJ<T> op{h, fac_of<T>(h)};
+  HC_CUDA_TRY(h, cudaMemsetAsync(S->lz, 0, sizeof(S->lz), s));
+  k_lz_start<T><<<g, kRedThreads, 0, s>>>(n, v, S, h->partials);
+  k_lz_scale0<T><<<g, kRedThreads, 0, s>>>(n, v, vp, S);
+  for (int j = 0; j < steps; ++j) {
+    k_lz_pre<T><<<g, kRedThreads, 0, s>>>(n, v, sd_of<T>(h), tmp, w, h->ess);
+    HC_CUDA_TRY(h, op.apply(tmp, w, nullptr, nullptr, s));
+    k_lz_alpha<T><<<g, kRedThreads, 0, s>>>(n, w, sd_of<T>(h), v, S, h->partials, j);
+    k_lz_update<T><<<g, kRedThreads, 0, s>>>(n, w, v, vp, S, h->partials, j);
+    k_lz_shift<T><<<g, kRedThreads, 0, s>>>(n, w, v, vp, S, j);
+  }
+  HC_CUDA_TRY(h, cudaGetLastError());
+  HC_CUDA_TRY(h, cudaMemcpyAsync(h->hscal, S, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, s));
+  HC_CUDA_TRY(h, cudaStreamSynchronize(s));
+  std::vector<double> a, b;
+  for (int j = 0; j < steps; ++j) {
+    a.push_back(h->hscal->lz[j]);
+    const double bj = h->hscal->lz[kMaxLanczos + j + 1];
+    if (j + 1 < steps) b.push_back(bj);
+    if (!(bj > 0.0)) break;  // invariant subspace found
+  }
+  b.resize(a.size() - 1);
+  *lmax = tridiag_lmax(a, b);
+  if (!std::isfinite(*lmax) || *lmax <= 0.0) {
+    h->err = "Lanczos bound is not positive";
+    return HC_BREAKDOWN;
+  }
+  return HC_OK;
+}
+
+template <typename T>
+hc_status lanczos_device(hcop* h, int steps, double* lmax) {
+  hc_status st = ensure_work(h, (size_t)4 * h->ndof * sizeof(T));
+  if (st != HC_OK) return st;
+  return lanczos_device<T>(h, steps, lmax, (T*)h->work);
+}
+template hc_status lanczos_device<double>(hcop*, int, double*);
+template hc_status lanczos_device<float>(hcop*, int, double*);
+
+// Preconditioned CG; wk holds 6 n-vectors of T.
+template <typename T>
+static hc_status pcg_run(hcop* h, const SolveCfg& cfg, const T* b, T* x, T* wk, int* iters, int* applies) {
+  HC_CUDA_TRY(h, ensure_scalars(h));
+  const int64_t n = h->ndof;
+  cudaStream_t s = h->stream;
+  KrylovScalars* S = h->scal;
+  T *r = wk, *p = wk + n, *q = wk + 2 * n, *z = wk + 3 * n, *dk = wk + 4 * n, *w = wk + 5 * n;
+  const unsigned g = vgrid(n);
+  const OpJ<T> op{h, fac_of<T>(h)};
+  const T* dinv = dinv_of<T>(h);
+  double* part = h->partials;
+  int napply = 0;
+
+  // scalars
+  KrylovScalars* hs = h->hscal;
+  std::memset(hs, 0, sizeof(KrylovScalars));
+  hs->rtol2 = cfg.rtol * cfg.rtol;
+  hs->atol2 = cfg.atol * cfg.atol;
+  hs->maxit = cfg.maxit;
+  HC_CUDA_TRY(h, cudaMemcpyAsync(S, hs, sizeof(KrylovScalars), cudaMemcpyHostToDevice, s));
+  HC_CUDA_TRY(h, cudaMemsetAsync(p, 0, n * sizeof(T), s));
+
+  const bool jac = cfg.precond != HC_PRECOND_CHEBYSHEV;
+  const bool none = cfg.precond == HC_PRECOND_NONE;
+  // z = C(r) for the Chebyshev preconditioner
+  double theta = 0, delta = 0, sigma1 = 0;
+  std::vector<double> c1s, c2s;
+  if (!jac) {
+    const double lmin = cfg.lmax / cfg.cheb_ratio;
+    theta = 0.5 * (cfg.lmax + lmin);
+    delta = 0.5 * (cfg.lmax - lmin);
+    sigma1 = theta / delta;
+    double rho = 1.0 / sigma1;
+    for (int k = 1; k < cfg.cheb_degree; ++k) {
+      const double rn = 1.0 / (2.0 * sigma1 - rho);
+      c1s.push_back(rn * rho);
+      c2s.push_back(2.0 * rn / delta);
+      rho = rn;
+    }
+  }
+  auto cheb = [&]() -> cudaError_t {
+    k_cheb0<T><<<g, kRedThreads, 0, s>>>(n, r, dinv, z, dk, w, h->ess, (T)(1.0 / theta), S);
+    for (int k = 1; k < cfg.cheb_degree; ++k) {
+      cudaError_t e = op.apply(z, w, nullptr, nullptr, s);
+      if (e != cudaSuccess) return e;
+      ++napply;
+      const int init_next = (k + 1 < cfg.cheb_degree) ? 1 : 0;
+      k_chebk<T><<<g, kRedThreads, 0, s>>>(n, r, dinv, z, dk, w, h->ess, (T)c1s[k - 1], (T)c2s[k - 1],
+                                           init_next, S);
+    }
+    return cudaGetLastError();
+  };
+
+  // r = b - J x
+  HC_CUDA_TRY(h, init_masked<T>(n, h->ess, x, q, s));
+  HC_CUDA_TRY(h, op.apply(x, q, nullptr, nullptr, s));
+  ++napply;
+  // no preconditioner: the Jacobi kernels with a null diagonal (z = r)
+  const T* dj = none ? nullptr : dinv;
+  if (jac) {
+    k_pcg_setup<T, true><<<g, kRedThreads, 0, s>>>(n, b, q, r, dj, S, part);
+    k_pcg_dir<T, true><<<g, kRedThreads, 0, s>>>(n, r, dj, p, q, h->ess, S, part);
+  } else {
+    k_pcg_setup<T, false><<<g, kRedThreads, 0, s>>>(n, b, q, r, dinv, S, part);
+    HC_CUDA_TRY(h, cheb());
+    k_rz_beta<T><<<g, kRedThreads, 0, s>>>(n, r, z, 1, S, part);
+    k_pcg_dir<T, false><<<g, kRedThreads, 0, s>>>(n, z, dinv, p, q, h->ess, S, part);
+  }
+  HC_CUDA_TRY(h, cudaGetLastError());
+
+  const int chunk = 25;
+  int launched = 0;
+  for (;;) {
+    for (int k = 0; k < chunk && launched < cfg.maxit; ++k, ++launched) {
+      HC_CUDA_TRY(h, op.apply(p, q, S, part, s));
+      ++napply;
+      if (jac) {
+        k_pcg_update<T, true><<<g, kRedThreads, 0, s>>>(n, x, r, p, q, dj, S, part);
+        k_pcg_dir<T, true><<<g, kRedThreads, 0, s>>>(n, r, dj, p, q, h->ess, S, part);
+      } else {
+        k_pcg_update<T, false><<<g, kRedThreads, 0, s>>>(n, x, r, p, q, dinv, S, part);
+        HC_CUDA_TRY(h, cheb());
+        k_rz_beta<T><<<g, kRedThreads, 0, s>>>(n, r, z, 0, S, part);
+        k_pcg_dir<T, false><<<g, kRedThreads, 0, s>>>(n, z, dinv, p, q, h->ess, S, part);
+      }
+    }
+    HC_CUDA_TRY(h, cudaGetLastError());
+    HC_CUDA_TRY(h, cudaMemcpyAsync(hs, S, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, s));
+    HC_CUDA_TRY(h, cudaStreamSynchronize(s));
+    if (hs->done || launched >= cfg.maxit) break;
+  }
+  *iters = hs->it;
+  if (applies) *applies = napply;
+  if (!hs->done) return HC_NOT_CONVERGED;
+  return (hc_status)hs->status;
+}
+
+template <typename T>
+hc_status pcg_device(hcop* h, const SolveCfg& cfg, const T* b, T* x, int* iters, int* applies,
+                     double* unused) {
+  (void)unused;
+  hc_status st = ensure_work(h, (size_t)6 * h->ndof * sizeof(T));
+  if (st != HC_OK) return st;
+  return pcg_run<T>(h, cfg, b, x, (T*)h->work, iters, applies);
+}
+template hc_status pcg_device<double>(hcop*, const SolveCfg&, const double*, double*, int*, int*, double*);
+template hc_status pcg_device<float>(hcop*, const SolveCfg&, const float*, float*, int*, int*, double*);
+
+// FP32 inner PCG inside FP64 iterative refinement.
+hc_status mixed_device(hcop* h, const hc_solve_params* prm, const double* b, double* x, hc_solve_info* info) {
+  const int64_t n = h->ndof;
+  // layout: r64 (n doubles) | rf, cf (2n floats) | 6n floats of PCG work
+  const size_t bytes = (size_t)n * sizeof(double) + (size_t)8 * n * sizeof(float);
+  hc_status st = ensure_work(h, bytes);
+  if (st != HC_OK) return st;
+  HC_CUDA_TRY(h, ensure_scalars(h));
+  double* r64 = (double*)h->work;
+  float* rf = (float*)(r64 + n);
+  float* cf = rf + n;
+  float* wk = cf + n;
+  cudaStream_t s = h->stream;
+  const unsigned g = vgrid(n);
+  const OpJ<double> op64{h, h->fac};
+  KrylovScalars* S = h->scal;
+  int applies = 0, iters = 0, outer = 0;
+
+  SolveCfg in;
+  in.precond = prm->precond;
+  in.cheb_degree = prm->cheb_degree > 0 ? prm->cheb_degree : 2;
+  in.cheb_ratio = prm->cheb_ratio > 0 ? prm->cheb_ratio : 30.0;
+  in.rtol = prm->inner_rtol > 0 ? prm->inner_rtol : 1e-4;
+  in.atol = 0.0;
+  in.lmax = prm->cheb_lmax;
+  if (in.precond == HC_PRECOND_CHEBYSHEV && in.lmax <= 0) {
+    if (h->lmax32 <= 0) {
+      double lm = 0;
+      st = lanczos_device<float>(h, 20, &lm, wk);
+      if (st != HC_OK) return st;
+      h->lmax32 = 1.1 * lm;
+    }
+    in.lmax = h->lmax32;
+  }
+  const int max_outer = prm->max_outer > 0 ? prm->max_outer : 50;
+
+  auto residual = [&](double* rn2, double* bn2) -> hc_status {
+    HC_CUDA_TRY(h, init_masked<double>(n, h->ess, x, r64, s));
+    HC_CUDA_TRY(h, op64.apply(x, r64, nullptr, nullptr, s));
+    ++applies;
+    k_resid64<<<g, kRedThreads, 0, s>>>(n, b, r64, S, h->partials);
+    HC_CUDA_TRY(h, cudaGetLastError());
+    HC_CUDA_TRY(h, cudaMemcpyAsync(h->hscal, S, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, s));
+    HC_CUDA_TRY(h, cudaStreamSynchronize(s));
+    *rn2 = h->hscal->rr;
+    *bn2 = h->hscal->bb;
+    return HC_OK;
+  };
+  double rn2 = 0, bn2 = 0;
+  st = residual(&rn2, &bn2);
+  if (st != HC_OK) return st;
+  const double bn = std::sqrt(bn2);
+  const double tol = std::max(prm->rtol * bn, prm->atol);
+  hc_status result = HC_NOT_CONVERGED;
+  while (true) {
+    const double rn = std::sqrt(rn2);
+    if (!std::isfinite(rn)) {
+      result = HC_BREAKDOWN;
+      break;
+    }
+    if (rn <= tol) {
+      result = HC_OK;
+      break;
+    }
+    if (outer >= max_outer || iters >= prm->maxit) break;
+    ++outer;
+    k_d2f_scaled<<<g, kRedThreads, 0, s>>>(n, r64, rf, 1.0 / rn);
+    HC_CUDA_TRY(h, cudaMemsetAsync(cf, 0, n * sizeof(float), s));
+    in.maxit = prm->maxit - iters;
+    int it = 0, ap = 0;
+    hc_status ist = pcg_run<float>(h, in, rf, cf, wk, &it, &ap);
+    iters += it;
+    applies += ap;
+    if (ist == HC_BREAKDOWN || ist == HC_ECUDA || ist == HC_ENOMEM) {
+      result = ist;
+      break;
+    }
+    k_axpy_f2d<<<g, kRedThreads, 0, s>>>(n, cf, x, rn);
+    HC_CUDA_TRY(h, cudaGetLastError());
+    st = residual(&rn2, &bn2);
+    if (st != HC_OK) return st;
+  }
+  if (info) {
+    info->status = result;
+    info->iterations = iters;
+    info->outer_iterations = outer;
+    info->applies = applies;
+    info->rel_residual = bn > 0 ? std::sqrt(rn2) / bn : std::sqrt(rn2);
+    info->lmax = in.lmax;
+  }
+  return result;
+}
+
+double vec_norm2_host(hcop* h, const double* x, int64_t n) {
+  (void)h;
+  (void)x;
+  (void)n;
+  return 0.0;
+}
+
+}  // namespace hc

@@ -1,0 +1,288 @@
+"""Host-side mirror of the reference's operator/solver interface for this path.
+
+Reference shape (C++, MFEM-based):
+  - kernels add integrators to a ParBilinearForm:
+      CurlCurlKernel::Apply     -> CurlCurlIntegrator(dt*alpha)
+                                   (src/kernels/curl_curl_kernel.cpp:21-24)
+      VectorFEMassKernel::Apply -> VectorFEMassIntegrator(beta)
+                                   (src/kernels/vector_fe_mass_kernel.cpp:21-24)
+      WeakCurlCurlKernel::Apply -> lf += -C_alpha u_n
+                                   (src/kernels/weak_curl_curl_kernel.cpp:14-31)
+  - EquationSystem (an mfem::Operator) exposes Mult / GetGradient of the
+    eliminated system (src/equation_systems/equation_system.cpp:133-210);
+  - solvers are configured from InputParameters "Tolerance", "AbsTolerance",
+    "MaxIter", "PrintLevel" (src/solvers/hephaestus_solvers.hpp:34-86).
+
+Here the same roles sit on the C ABI: HCurlForm collects the kernels'
+coefficients like a ParBilinearForm, HCurlOperator is the assembled
+(matrix-free, device-resident) Jacobian with Mult/GetGradient/
+FormLinearSystem, and GpuHCurlPCGSolver takes the reference's solver option
+names.  Errors raise, mirroring MFEM_ABORT at this layer.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data_as(C.c_void_p)
+    return C.c_void_p(int(a.data_ptr()))  # torch tensor
+
+
+def _dev_ptr(t, dtype_name):
+    import torch
+
+    if not isinstance(t, torch.Tensor) or not t.is_cuda or not t.is_contiguous():
+        raise TypeError("expected a contiguous CUDA tensor")
+    if str(t.dtype) != "torch." + dtype_name:
+        raise TypeError("expected dtype %s, got %s" % (dtype_name, t.dtype))
+    return C.c_void_p(t.data_ptr())
+
+
+# ----------------------------------------------------------------------------
+# kernels (coefficient registration, like hephaestus::Kernel<ParBilinearForm>)
+# ----------------------------------------------------------------------------
+class CurlCurlKernel:
+    """Adds (coef curl u, curl u') to a form; coef is per element."""
+
+    def __init__(self, coef):
+        self.coef = np.ascontiguousarray(coef, dtype=np.float64)
+
+    def Apply(self, form):
+        form.curl_coefs.append(self.coef)
+
+
+class VectorFEMassKernel:
+    """Adds (coef u, u') to a form; coef is per element."""
+
+    def __init__(self, coef):
+        self.coef = np.ascontiguousarray(coef, dtype=np.float64)
+
+    def Apply(self, form):
+        form.mass_coefs.append(self.coef)
+
+
+class HCurlForm:
+    """Structured-hex Nedelec bilinear form, filled by kernels, assembled on the device.
+
+    Geometry: nx*ny*nz parallelepiped hexes with vertices (x fastest) or the
+    unit cube.  The assembled operator is K = sum curl terms + sum mass terms.
+    """
+
+    def __init__(self, nx, ny, nz, order, vertices=None):
+        self.nx, self.ny, self.nz, self.order = nx, ny, nz, order
+        self.vertices = None if vertices is None else np.ascontiguousarray(vertices, dtype=np.float64)
+        self.curl_coefs = []
+        self.mass_coefs = []
+
+    def Assemble(self, ess_attr_bits=0, ess_mask=None):
+        if not self.curl_coefs:
+            raise ValueError("a curl-curl kernel is required")
+        nu = np.sum(self.curl_coefs, axis=0)
+        sigma = np.sum(self.mass_coefs, axis=0) if self.mass_coefs else None
+        return HCurlOperator(self.nx, self.ny, self.nz, self.order, nu, sigma, dt=1.0,
+                             vertices=self.vertices, ess_attr_bits=ess_attr_bits, ess_mask=ess_mask)
+
+
+class HCurlOperator:
+    """Device-resident eliminated operator J = P K P + (I - P),  K = dt C_nu + M_sigma.
+
+    Mult(x, y) is EquationSystem::Mult; GetGradient() returns self (the
+    operator is linear); FormLinearSystem applies MFEM's elimination to a
+    right-hand side.
+    """
+
+    def __init__(self, nx, ny, nz, order, nu, sigma=None, dt=1.0, vertices=None, ess_attr_bits=0x3F,
+                 ess_mask=None, stream=None):
+        L = N.lib()
+        ne = nx * ny * nz
+        self._nu = np.ascontiguousarray(nu, dtype=np.float64)
+        self._sigma = None if sigma is None else np.ascontiguousarray(sigma, dtype=np.float64)
+        if self._nu.shape != (ne,) or (self._sigma is not None and self._sigma.shape != (ne,)):
+            raise ValueError("nu/sigma must have one value per element (%d)" % ne)
+        self._verts = None if vertices is None else np.ascontiguousarray(vertices, dtype=np.float64)
+        self._mask = None if ess_mask is None else np.ascontiguousarray(ess_mask, dtype=np.uint8)
+        d = N.ProblemDesc()
+        d.elem_type = N.HC_HEX
+        d.order = order
+        d.nx, d.ny, d.nz = nx, ny, nz
+        d.vertices = _ptr(self._verts)
+        d.nu = _ptr(self._nu)
+        d.sigma = _ptr(self._sigma)
+        d.dt = dt
+        d.ess_mask = _ptr(self._mask)
+        d.ess_attr_bits = ess_attr_bits
+        h = C.c_void_p()
+        st = L.hc_create(C.byref(d), C.byref(h))
+        if st != N.HC_OK:
+            raise N.HcError(st, N.last_error(None))
+        self.h = h
+        self.nx, self.ny, self.nz, self.order, self.dt = nx, ny, nz, order, dt
+        self.ndof = L.hc_num_dofs(h)
+        self.ne = L.hc_num_elems(h)
+        self.height = self.width = self.ndof
+        if stream is not None:
+            self.set_stream(stream)
+
+    # -- lifecycle --
+    def close(self):
+        if getattr(self, "h", None):
+            N.lib().hc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream):
+        """stream: a torch.cuda.Stream or a raw cudaStream_t integer."""
+        s = getattr(stream, "cuda_stream", stream)
+        N.check(N.lib().hc_set_stream(self.h, C.c_void_p(int(s) if s else 0)), self.h)
+
+    # -- layout --
+    def dof_index(self, c, i, j, k):
+        return N.lib().hc_hex_dof_index(self.h, c, i, j, k)
+
+    def ess_mask(self):
+        m = np.zeros(self.ndof, dtype=np.uint8)
+        N.check(N.lib().hc_get_ess_mask(self.h, _ptr(m)), self.h)
+        return m
+
+    # -- host-vector actions (mfem::Vector host data) --
+    def _h(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if x.shape != (self.ndof,):
+            raise ValueError("vector length %s != %d" % (x.shape, self.ndof))
+        return x
+
+    def Mult(self, x, y=None):
+        x = self._h(x)
+        y = np.empty_like(x) if y is None else y
+        N.check(N.lib().hc_mult(self.h, _ptr(x), _ptr(y)), self.h)
+        return y
+
+    def GetGradient(self, x=None):
+        return self
+
+    def ApplyForm(self, x):
+        """K x without elimination."""
+        x = self._h(x)
+        y = np.empty_like(x)
+        N.check(N.lib().hc_apply_form(self.h, _ptr(x), _ptr(y)), self.h)
+        return y
+
+    def AddWeakCurlCurl(self, u, lf, scale=-1.0):
+        """lf += scale * C_nu u   (WeakCurlCurlKernel::Apply with scale -1)."""
+        u = self._h(u)
+        if not (isinstance(lf, np.ndarray) and lf.dtype == np.float64 and lf.flags.c_contiguous):
+            raise TypeError("lf must be a contiguous float64 array (updated in place)")
+        N.check(N.lib().hc_add_weak_curlcurl(self.h, _ptr(u), _ptr(lf), scale), self.h)
+        return lf
+
+    def Diagonal(self):
+        d = np.empty(self.ndof)
+        N.check(N.lib().hc_diag(self.h, _ptr(d)), self.h)
+        return d
+
+    def FormLinearSystem(self, x_bc, b):
+        """MFEM FormLinearSystem for J: B = P (b - K (I-P) x_bc) + (I-P) x_bc, X = x_bc."""
+        m = self.ess_mask().astype(bool)
+        xb = np.where(m, self._h(x_bc), 0.0)
+        B = np.array(self._h(b), copy=True)
+        if np.any(xb):
+            B -= self.ApplyForm(xb)
+        B[m] = xb[m]
+        return np.array(x_bc, dtype=np.float64, copy=True), B
+
+    # -- device actions (torch CUDA tensors) --
+    def MultDevice(self, x, y):
+        if str(x.dtype) == "torch.float32":
+            N.check(N.lib().hc_mult_device_f32(self.h, _dev_ptr(x, "float32"), _dev_ptr(y, "float32")), self.h)
+        else:
+            N.check(N.lib().hc_mult_device(self.h, _dev_ptr(x, "float64"), _dev_ptr(y, "float64")), self.h)
+        return y
+
+    def ApplyFormDevice(self, x, y):
+        N.check(N.lib().hc_apply_form_device(self.h, _dev_ptr(x, "float64"), _dev_ptr(y, "float64")), self.h)
+        return y
+
+    def LanczosLmax(self, steps=20):
+        v = C.c_double(0)
+        N.check(N.lib().hc_lanczos_lmax(self.h, steps, C.byref(v)), self.h)
+        return v.value
+
+
+_PRECOND = {"none": N.HC_PRECOND_NONE, "jacobi": N.HC_PRECOND_JACOBI, "chebyshev": N.HC_PRECOND_CHEBYSHEV}
+_PREC = {"fp64": N.HC_FP64, "mixed": N.HC_MIXED}
+
+
+class GpuHCurlPCGSolver:
+    """PCG on the device, configured with the reference's option names.
+
+    Options (defaults as DefaultJacobiPCGSolver, hephaestus_solvers.hpp:34-57):
+      Tolerance (1e-9), AbsTolerance (1e-16), MaxIter (1000), PrintLevel (ignored),
+    plus: Precision ('fp64' | 'mixed'), Preconditioner ('jacobi' |
+    'chebyshev' | 'none'), ChebyshevDegree (2), ChebyshevRatio (30),
+    ChebyshevLmax (0 = estimate), InnerTolerance (1e-4), MaxOuter (50).
+    """
+
+    def __init__(self, params=None, op=None):
+        params = dict(params or {})
+        self.p = N.SolveParams()
+        self.p.precision = _PREC[params.get("Precision", "fp64")]
+        self.p.precond = _PRECOND[params.get("Preconditioner", "jacobi")]
+        self.p.cheb_degree = int(params.get("ChebyshevDegree", 2))
+        self.p.cheb_ratio = float(params.get("ChebyshevRatio", 30.0))
+        self.p.cheb_lmax = float(params.get("ChebyshevLmax", 0.0))
+        self.p.rtol = float(params.get("Tolerance", 1e-9))
+        self.p.atol = float(params.get("AbsTolerance", 1e-16))
+        self.p.maxit = int(params.get("MaxIter", 1000))
+        self.p.inner_rtol = float(params.get("InnerTolerance", 1e-4))
+        self.p.max_outer = int(params.get("MaxOuter", 50))
+        self.op = op
+        self.info = N.SolveInfo()
+        self.raise_on_nonconvergence = bool(params.get("RaiseOnNonConvergence", False))
+
+    def SetOperator(self, op):
+        self.op = op
+
+    def Mult(self, b, x):
+        """Solve J x = b (host float64 arrays; x is the initial guess, updated in place)."""
+        op = self.op
+        b = op._h(b)
+        if not (isinstance(x, np.ndarray) and x.dtype == np.float64 and x.flags.c_contiguous):
+            raise TypeError("x must be a contiguous float64 array (updated in place)")
+        st = N.lib().hc_solve(op.h, C.byref(self.p), _ptr(b), _ptr(x), C.byref(self.info))
+        self._check(st)
+        return x
+
+    def MultDevice(self, b, x):
+        """Solve with device float64 tensors (x updated in place)."""
+        op = self.op
+        st = N.lib().hc_solve_device(op.h, C.byref(self.p), _dev_ptr(b, "float64"), _dev_ptr(x, "float64"),
+                                     C.byref(self.info))
+        self._check(st)
+        return x
+
+    def _check(self, st):
+        if st in (N.HC_OK,):
+            return
+        if st in (N.HC_NOT_CONVERGED, N.HC_BREAKDOWN) and not self.raise_on_nonconvergence:
+            return
+        raise N.HcError(st, N.last_error(self.op.h))
+
+    @property
+    def result(self):
+        i = self.info
+        return {"status": N.STATUS_NAMES[i.status], "iterations": i.iterations,
+                "outer_iterations": i.outer_iterations, "applies": i.applies,
+                "rel_residual": i.rel_residual, "lmax": i.lmax}

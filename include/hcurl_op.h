@@ -1,0 +1,171 @@
+/*
+ * hcurl_op.h -- C ABI of the GB300 H(curl) curl-curl + mass operator and solver.
+ *
+ * One handle owns one discretised problem on the device: the Nedelec space on
+ * a structured hex grid (sum-factorised partial assembly) or on a tet mesh
+ * (element matrices), the per-element coefficient factors, the essential
+ * (tangential Dirichlet) dof set and all Krylov work space.  The operator is
+ * the reference's A/E-formulation bilinear form
+ *
+ *     a1(u, u') = (sigma u, u') + (dt nu curl u, curl u')
+ *
+ * (src/formulations/HCurl/hcurl_formulation.cpp:1-38), i.e. the sum of the
+ * contributions that CurlCurlKernel (src/kernels/curl_curl_kernel.cpp:21-24,
+ * coefficient dt*alpha registered at hcurl_formulation.cpp:117-128) and
+ * VectorFEMassKernel (src/kernels/vector_fe_mass_kernel.cpp:21-24) add to the
+ * ParBilinearForm.  "Mult" entry points apply the operator after essential-dof
+ * elimination, exactly what EquationSystem::Mult / GetGradient expose
+ * (src/equation_systems/equation_system.cpp:133-210):
+ *
+ *     J x = P K P x + (I - P) x,     P = projector onto non-essential dofs.
+ *
+ * Conventions
+ *  - No call aborts or throws.  Every call returns hc_status; on failure
+ *    hc_last_error() gives a one-line reason (thread-local for hc_create).
+ *  - Host-pointer calls (hc_mult, hc_solve, ...) copy in, run on the
+ *    handle's stream and synchronise; they are what an mfem::Operator /
+ *    mfem::Solver shim calls with Vector::HostRead()/HostWrite() data.
+ *  - *_device calls take device pointers, enqueue on the handle's stream and
+ *    return without synchronising.
+ *  - A handle is not re-entrant; different handles may be used from
+ *    different host threads on different streams.
+ *  - Dof numbering of the structured hex space (documented in the design doc and
+ *    in hc_hex_dof_index below) is tensor-product: component c's dofs are
+ *    open (Gauss-Legendre nodal) in direction c and closed (Gauss-Lobatto
+ *    nodal) in the other two, x fastest, components concatenated.
+ */
+#ifndef HCURL_OP_H
+#define HCURL_OP_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct hcop hcop_t;
+
+typedef enum {
+  HC_OK = 0,
+  HC_EINVAL = 1,         /* bad argument (null pointer, size, NaN, ...)   */
+  HC_ENOMEM = 2,         /* device allocation failed / over HBM budget    */
+  HC_ECUDA = 3,          /* CUDA runtime error                            */
+  HC_NOT_CONVERGED = 4,  /* maxit reached                                 */
+  HC_BREAKDOWN = 5,      /* p^T K p <= 0, NaN or Inf in the iteration     */
+  HC_TIMEOUT = 6,        /* a bounded device wait expired                 */
+  HC_ENOTSUP = 7         /* valid request this build does not support     */
+} hc_status;
+
+enum { HC_HEX = 0, HC_TET = 1 };
+
+/* Precision of a solve or of a device apply. */
+enum {
+  HC_FP64 = 0,   /* plain FP64 operator and PCG (the drop-in path)        */
+  HC_FP32 = 1,   /* FP32 operator and vectors, FP64 dots and alpha/beta   */
+  HC_MIXED = 2   /* FP32 inner PCG inside FP64 iterative refinement       */
+};
+
+enum { HC_PRECOND_NONE = 0, HC_PRECOND_JACOBI = 1, HC_PRECOND_CHEBYSHEV = 2 };
+
+typedef struct {
+  int32_t elem_type;        /* HC_HEX (structured grid) or HC_TET                 */
+  int32_t order;            /* Nedelec order: hex 1..3, tet 1..2                  */
+  /* HC_HEX */
+  int32_t nx, ny, nz;       /* elements per direction                             */
+  /* HC_TET */
+  int64_t n_vert;           /* vertex count                                       */
+  int64_t n_elem;           /* tet count                                          */
+  const int64_t* elem_verts;/* n_elem * 4 vertex ids                              */
+  /* both */
+  const double* vertices;   /* HC_HEX: (nx+1)(ny+1)(nz+1)*3, x fastest, NULL =
+                               unit cube; every hex must be a parallelepiped.
+                               HC_TET: n_vert*3                                    */
+  const double* nu;         /* per-element curl-curl coefficient (required, >= 0)  */
+  const double* sigma;      /* per-element mass coefficient (>= 0), NULL = none    */
+  double dt;                /* curl-curl scale: K = dt*C_nu + M_sigma (> 0)        */
+  /* essential (tangential Dirichlet) dofs: explicit mask wins over attributes */
+  const uint8_t* ess_mask;  /* n_dof flags or NULL                                 */
+  int32_t ess_attr_bits;    /* bit a-1 marks boundary attribute a.  HC_HEX faces:
+                               1..6 = x-, x+, y-, y+, z-, z+.                      */
+  int64_t n_bdr;            /* HC_TET boundary triangles                           */
+  const int64_t* bdr_tris;  /* n_bdr * 3 vertex ids                                */
+  const int32_t* bdr_attr;  /* n_bdr attributes                                    */
+} hc_problem_desc;
+
+typedef struct {
+  int32_t precision;        /* HC_FP64 | HC_FP32 | HC_MIXED                        */
+  int32_t precond;          /* HC_PRECOND_*                                        */
+  int32_t cheb_degree;      /* polynomial degree (>= 1) for HC_PRECOND_CHEBYSHEV   */
+  double cheb_ratio;        /* interval [lmax/ratio, lmax]; <= 0 -> 30              */
+  double cheb_lmax;         /* upper eigenvalue bound of D^-1 J; <= 0 -> estimate  */
+  double rtol, atol;        /* stop when ||b - J x|| <= max(rtol ||b||, atol)      */
+  int32_t maxit;            /* max PCG iterations (inner iterations in total)      */
+  double inner_rtol;        /* HC_MIXED: inner FP32 solve tolerance (<= 0 -> 1e-4)  */
+  int32_t max_outer;        /* HC_MIXED: max refinement steps (<= 0 -> 50)          */
+} hc_solve_params;
+
+typedef struct {
+  int32_t status;           /* hc_status of the solve                              */
+  int32_t iterations;       /* total PCG iterations                                */
+  int32_t outer_iterations; /* refinement steps (HC_MIXED), else 1                 */
+  int32_t applies;          /* operator applications                               */
+  double rel_residual;      /* ||b - J x||_2 / ||b||_2 in FP64 at exit             */
+  double lmax;              /* Chebyshev upper bound used                          */
+} hc_solve_info;
+
+/* ---- lifecycle ---------------------------------------------------------- */
+/* Replaces the construction of CurlCurlEquationSystem's bilinear form +
+ * FormLinearSystem (equation_system.cpp:133-198, 325-347): all inputs are
+ * copied to the device, coefficient factors are computed in FP64.           */
+hc_status hc_create(const hc_problem_desc* desc, hcop_t** out);
+void hc_destroy(hcop_t* h);
+/* Stream for all later work of this handle (cudaStream_t; NULL = default). */
+hc_status hc_set_stream(hcop_t* h, void* stream);
+/* Last error of this handle, or of the calling thread's last hc_create when
+ * h is NULL.                                                               */
+hc_status hc_last_error(const hcop_t* h, char* buf, size_t n);
+
+/* ---- sizes / layout ----------------------------------------------------- */
+int64_t hc_num_dofs(const hcop_t* h);
+int64_t hc_num_elems(const hcop_t* h);
+/* Structured hex: global index of dof (component c, i, j, k).             */
+int64_t hc_hex_dof_index(const hcop_t* h, int c, int64_t i, int64_t j, int64_t k);
+/* Essential-dof mask as the library resolved it (n_dof bytes, host).      */
+hc_status hc_get_ess_mask(const hcop_t* h, uint8_t* mask);
+
+/* ---- operator actions ---------------------------------------------------- */
+/* y = J x (eliminated operator), host FP64 vectors.
+ * Replaces EquationSystem::Mult (equation_system.cpp:201-204).              */
+hc_status hc_mult(hcop_t* h, const double* x, double* y);
+/* y = K x (full form, no elimination), host FP64.                          */
+hc_status hc_apply_form(hcop_t* h, const double* x, double* y);
+/* y += scale * C_nu x (curl-curl with nu alone, no dt, no elimination):
+ * WeakCurlCurlKernel::Apply's _curl_curl->AddMultTranspose(u, lf, -1)
+ * (src/kernels/weak_curl_curl_kernel.cpp:27-31) with scale = -1.            */
+hc_status hc_add_weak_curlcurl(hcop_t* h, const double* x, double* y, double scale);
+/* Diagonal of J (HypreDiagScale's diagonal, hephaestus_solvers.hpp:34-57).  */
+hc_status hc_diag(hcop_t* h, double* d);
+
+/* Device-pointer forms, enqueued on the handle's stream.                   */
+hc_status hc_mult_device(hcop_t* h, const double* x, double* y);
+hc_status hc_mult_device_f32(hcop_t* h, const float* x, float* y);
+hc_status hc_apply_form_device(hcop_t* h, const double* x, double* y);
+
+/* ---- linear solve --------------------------------------------------------- */
+/* Solve J x = b for x (x holds the initial guess on entry).  Replaces the
+ * HyprePCG solve of HCurlFormulation::ConstructJacobianSolver
+ * (hcurl_formulation.cpp:81-85, problem_builder_base.cpp:221-253) for this
+ * operator; preconditioner is Jacobi or Chebyshev-Jacobi instead of AMS.
+ * Essential rows of b carry the boundary values (MFEM FormLinearSystem).   */
+hc_status hc_solve(hcop_t* h, const hc_solve_params* prm, const double* b, double* x,
+                   hc_solve_info* info);
+hc_status hc_solve_device(hcop_t* h, const hc_solve_params* prm, const double* b, double* x,
+                          hc_solve_info* info);
+/* Largest eigenvalue estimate of D^-1 J by `steps` Lanczos steps started from
+ * v_i = frac(i * 0.6180339887498949) - 1/2.                                */
+hc_status hc_lanczos_lmax(hcop_t* h, int steps, double* lmax);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HCURL_OP_H */

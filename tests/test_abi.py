@@ -1,0 +1,79 @@
+"""CPU tests of the C ABI boundary: the library loads, exports exactly what
+include/hcurl_op.h declares, and rejects bad input before touching a GPU."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from hephaestus_gb300 import _native as N
+
+
+def test_library_exports_every_declared_symbol():
+    L = N.lib()
+    names = N.declared_symbols()
+    assert len(names) >= 18
+    for n in names:
+        assert hasattr(L, n), n
+
+
+def _desc(**kw):
+    d = N.ProblemDesc()
+    d.elem_type = N.HC_HEX
+    d.order = 2
+    d.nx = d.ny = d.nz = 2
+    d.dt = 1.0
+    for k, v in kw.items():
+        setattr(d, k, v)
+    return d
+
+
+@pytest.mark.parametrize("field,value,needle", [
+    ("order", 0, "order"),
+    ("order", 4, "order"),
+    ("nx", 0, "nx"),
+    ("dt", 0.0, "dt"),
+    ("elem_type", 7, "elem_type"),
+])
+def test_create_rejects_bad_descriptor(field, value, needle):
+    nu = np.ones(8)
+    d = _desc(nu=nu.ctypes.data_as(C.c_void_p))
+    setattr(d, field, value)
+    h = C.c_void_p()
+    st = N.lib().hc_create(C.byref(d), C.byref(h))
+    assert st == N.HC_EINVAL
+    assert needle in N.last_error(None)
+    assert not h.value
+
+
+def test_create_rejects_missing_or_bad_coefficients():
+    h = C.c_void_p()
+    d = _desc()
+    assert N.lib().hc_create(C.byref(d), C.byref(h)) == N.HC_EINVAL
+    assert "nu" in N.last_error(None)
+    nu = np.ones(8)
+    nu[3] = np.nan
+    d = _desc(nu=nu.ctypes.data_as(C.c_void_p))
+    assert N.lib().hc_create(C.byref(d), C.byref(h)) == N.HC_EINVAL
+    sig = -np.ones(8)
+    nu = np.ones(8)
+    d = _desc(nu=nu.ctypes.data_as(C.c_void_p), sigma=sig.ctypes.data_as(C.c_void_p))
+    assert N.lib().hc_create(C.byref(d), C.byref(h)) == N.HC_EINVAL
+    assert "sigma" in N.last_error(None)
+
+
+def test_null_arguments_return_einval():
+    L = N.lib()
+    assert L.hc_create(None, None) == N.HC_EINVAL
+    assert L.hc_mult(None, None, None) == N.HC_EINVAL
+    assert L.hc_solve(None, None, None, None, None) == N.HC_EINVAL
+    assert L.hc_diag(None, None) == N.HC_EINVAL
+    assert L.hc_num_dofs(None) == -1
+    assert L.hc_last_error(None, None, 0) == N.HC_EINVAL
+    L.hc_destroy(None)  # no-op
+
+
+def test_tets_not_yet_supported_is_reported():
+    nu = np.ones(8)
+    d = _desc(elem_type=N.HC_TET, nu=nu.ctypes.data_as(C.c_void_p))
+    h = C.c_void_p()
+    assert N.lib().hc_create(C.byref(d), C.byref(h)) == N.HC_ENOTSUP

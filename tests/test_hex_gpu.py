@@ -1,0 +1,184 @@
+"""GPU parity of the structured-hex Nedelec operator and solvers against the
+FP64 oracle (CSR assembly + SpMV + textbook PCG), through the C ABI."""
+import numpy as np
+import pytest
+
+import oracle
+from hephaestus_gb300 import GpuHCurlPCGSolver, HCurlOperator, meshes
+from tests import hexref
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12   # FP64 apply, relative 2-norm
+TOL32 = 2e-6    # FP32 apply, relative 2-norm
+
+
+def _sheared(n):
+    v = meshes.box_vertices(n, n, n)
+    A = np.array([[1.0, 0.2, 0.1], [0.0, 0.9, -0.15], [0.05, 0.0, 1.1]])
+    return v @ A.T
+
+
+def _pair(n, p, shear=False, mass=True, bits=0x3F, seed=0, dt=0.01):
+    rng = np.random.default_rng(seed)
+    ne = n ** 3
+    nu = meshes.loguniform(ne, 1.0, 1e3, rng)
+    sigma = meshes.loguniform(ne, 1e-2, 1e6, rng) if mass else None
+    verts = _sheared(n) if shear else None
+    op = HCurlOperator(n, n, n, p, nu, sigma, dt=dt, vertices=verts, ess_attr_bits=bits)
+    ref = oracle.Problem.hex(n, n, n, p, verts)
+    ref.set_coef(dt * nu, sigma)
+    ref.assemble()
+    ref.set_ess(op.ess_mask())
+    return op, ref, rng
+
+
+@pytest.mark.parametrize("p", [1, 2, 3])
+@pytest.mark.parametrize("shear", [False, True])
+def test_apply_parity_fp64(p, shear):
+    op, ref, rng = _pair(3, p, shear)
+    x = rng.standard_normal(op.ndof)
+    y = op.ApplyForm(x)
+    yr = ref.apply(x)
+    assert np.linalg.norm(y - yr) / np.linalg.norm(yr) < TOL64
+    ym = op.Mult(x)
+    ymr = ref.apply_masked(x)
+    assert np.linalg.norm(ym - ymr) / np.linalg.norm(ymr) < TOL64
+
+
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_apply_parity_fp32(p):
+    import torch
+
+    op, ref, rng = _pair(4, p)
+    x = rng.standard_normal(op.ndof)
+    xd = torch.tensor(x, dtype=torch.float32, device="cuda")
+    yd = torch.empty_like(xd)
+    op.MultDevice(xd, yd)
+    torch.cuda.synchronize()
+    y = yd.double().cpu().numpy()
+    yr = ref.apply_masked(x.astype(np.float32).astype(np.float64))
+    assert np.linalg.norm(y - yr) / np.linalg.norm(yr) < TOL32
+
+
+@pytest.mark.parametrize("p", [1, 2])
+def test_diag_parity(p):
+    op, ref, _ = _pair(3, p, shear=True)
+    d = op.Diagonal()
+    dr = ref.diag_masked()
+    assert np.abs(d - dr).max() / np.abs(dr).max() < TOL64
+
+
+def test_ess_mask_matches_oracle_faces():
+    for bits in (0x3F, 0b000101, 0b110000):
+        op, ref, _ = _pair(3, 2, bits=bits)
+        assert np.array_equal(op.ess_mask(), ref.hex_ess_mask(bits))
+
+
+def test_weak_curlcurl_parity():
+    op, ref, rng = _pair(3, 2, mass=True, dt=0.05)
+    u = rng.standard_normal(op.ndof)
+    lf = rng.standard_normal(op.ndof)
+    lf0 = lf.copy()
+    op.AddWeakCurlCurl(u, lf, -1.0)
+    # C_nu u with the oracle: alpha = nu (no dt), no mass
+    ref.set_coef(op._nu, None)
+    ref.assemble()
+    want = lf0 - ref.apply(u)
+    assert np.linalg.norm(lf - want) / np.linalg.norm(want) < TOL64
+
+
+@pytest.mark.parametrize("p", [1, 2])
+def test_curl_of_gradient_vanishes_on_device(p):
+    n = 4
+    rng = np.random.default_rng(5)
+    op = HCurlOperator(n, n, n, p, rng.uniform(0.5, 2, n ** 3), None, dt=1.0, vertices=_sheared(n),
+                       ess_attr_bits=0)
+    phi = rng.standard_normal((n * p + 1,) * 3)
+    g = hexref.discrete_gradient(n, n, n, p, phi)
+    y = op.ApplyForm(g)
+    assert np.linalg.norm(y) < 1e-11 * np.linalg.norm(g) * np.abs(op._nu).max() * 10
+
+
+def test_symmetry_and_linearity_fp64():
+    op, _, rng = _pair(6, 2)
+    x, z = rng.standard_normal(op.ndof), rng.standard_normal(op.ndof)
+    Jx, Jz = op.Mult(x), op.Mult(z)
+    assert abs(z @ Jx - x @ Jz) < 1e-12 * np.linalg.norm(Jx) * np.linalg.norm(z)
+    J2 = op.Mult(2.5 * x - z)
+    assert np.linalg.norm(J2 - (2.5 * Jx - Jz)) < 1e-12 * np.linalg.norm(J2)
+
+
+def _rhs(op, ref, p):
+    b = ref.load_coil(q=p + 2)
+    b[op.ess_mask() == 1] = 0.0
+    return b
+
+
+@pytest.mark.parametrize("precond", ["jacobi", "chebyshev"])
+def test_pcg_fp64_matches_oracle(precond):
+    op, ref, _ = _pair(5, 2)
+    b = _rhs(op, ref, 2)
+    s = GpuHCurlPCGSolver({"Tolerance": 1e-12, "MaxIter": 20000, "Preconditioner": precond,
+                           "ChebyshevDegree": 3}, op)
+    x = np.zeros(op.ndof)
+    s.Mult(b, x)
+    assert s.result["status"] == "OK", s.result
+    xr, st, it, rr = ref.pcg(b, precond=1, rtol=1e-13, maxit=100000)
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-9
+    r = b - ref.apply_masked(x)
+    assert np.linalg.norm(r) / np.linalg.norm(b) < 2e-12
+
+
+def test_pcg_iterates_match_oracle_iteration_counts():
+    op, ref, _ = _pair(4, 1)
+    b = _rhs(op, ref, 1)
+    s = GpuHCurlPCGSolver({"Tolerance": 1e-10, "MaxIter": 20000}, op)
+    x = np.zeros(op.ndof)
+    s.Mult(b, x)
+    xr, st, it, rr = ref.pcg(b, precond=1, rtol=1e-10, maxit=20000)
+    assert abs(s.result["iterations"] - it) <= max(2, it // 50)
+
+
+def test_mixed_precision_reaches_fp64_accuracy():
+    op, ref, _ = _pair(6, 2)
+    b = _rhs(op, ref, 2)
+    xr, st, it, rr = ref.pcg(b, precond=1, rtol=1e-14, maxit=200000)
+    s = GpuHCurlPCGSolver({"Precision": "mixed", "Tolerance": 1e-12, "MaxIter": 200000,
+                           "InnerTolerance": 1e-4}, op)
+    x = np.zeros(op.ndof)
+    s.Mult(b, x)
+    assert s.result["status"] == "OK", s.result
+    assert s.result["outer_iterations"] >= 2
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-10
+
+
+def test_lanczos_bound_matches_oracle():
+    op, ref, _ = _pair(4, 2)
+    lg = op.LanczosLmax(20)
+    lo = ref.lanczos_lmax(20)
+    assert abs(lg - lo) / lo < 1e-6
+
+
+def test_breakdown_and_nonconvergence_statuses():
+    op, ref, _ = _pair(4, 2)
+    b = _rhs(op, ref, 2)
+    s = GpuHCurlPCGSolver({"Tolerance": 1e-14, "MaxIter": 3}, op)
+    x = np.zeros(op.ndof)
+    s.Mult(b, x)
+    assert s.result["status"] == "NOT_CONVERGED" and s.result["iterations"] == 3
+    bad = b.copy()
+    bad[5] = np.nan
+    s2 = GpuHCurlPCGSolver({"Tolerance": 1e-10, "MaxIter": 50}, op)
+    x = np.zeros(op.ndof)
+    s2.Mult(bad, x)
+    assert s2.result["status"] == "BREAKDOWN"
+
+
+def test_non_affine_hex_rejected():
+    n = 2
+    v = meshes.box_vertices(n, n, n).copy()
+    v[13] += 0.05  # move the centre vertex: trilinear, not affine
+    with pytest.raises(Exception) as e:
+        HCurlOperator(n, n, n, 1, np.ones(8), None, vertices=v)
+    assert "parallelepiped" in str(e.value)
