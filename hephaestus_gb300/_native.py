@@ -96,6 +96,8 @@ _SIGS = {
     "hc_mult_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "hc_mult_device_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "hc_apply_form_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hc_add_mult_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hc_add_mult_device_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "hc_solve": (C.c_int, [C.c_void_p, C.POINTER(SolveParams), C.c_void_p, C.c_void_p, C.POINTER(SolveInfo)]),
     "hc_solve_device": (C.c_int, [C.c_void_p, C.POINTER(SolveParams), C.c_void_p, C.c_void_p,
                                   C.POINTER(SolveInfo)]),

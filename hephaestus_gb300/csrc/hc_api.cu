@@ -376,6 +376,20 @@ hc_status hc_mult_device_f32(hcop_t* h, const float* x, float* y) {
   return HC_OK;
 }
 
+hc_status hc_add_mult_device(hcop_t* h, const double* x, double* y) {
+  if (!h || !x || !y) return HC_EINVAL;
+  const OpJ<double> op{h, h->fac};
+  HC_CUDA_TRY(h, op.apply(x, y, nullptr, nullptr, h->stream));
+  return HC_OK;
+}
+
+hc_status hc_add_mult_device_f32(hcop_t* h, const float* x, float* y) {
+  if (!h || !x || !y) return HC_EINVAL;
+  const OpJ<float> op{h, h->facf};
+  HC_CUDA_TRY(h, op.apply(x, y, nullptr, nullptr, h->stream));
+  return HC_OK;
+}
+
 hc_status hc_apply_form_device(hcop_t* h, const double* x, double* y) {
   if (!h || !x || !y) return HC_EINVAL;
   HC_CUDA_TRY(h, cudaMemsetAsync(y, 0, h->ndof * sizeof(double), h->stream));

@@ -211,6 +211,14 @@ class HCurlOperator:
             N.check(N.lib().hc_mult_device(self.h, _dev_ptr(x, "float64"), _dev_ptr(y, "float64")), self.h)
         return y
 
+    def AddMultDevice(self, x, y):
+        """y += P K P x on device tensors (float32 or float64)."""
+        if str(x.dtype) == "torch.float32":
+            N.check(N.lib().hc_add_mult_device_f32(self.h, _dev_ptr(x, "float32"), _dev_ptr(y, "float32")), self.h)
+        else:
+            N.check(N.lib().hc_add_mult_device(self.h, _dev_ptr(x, "float64"), _dev_ptr(y, "float64")), self.h)
+        return y
+
     def ApplyFormDevice(self, x, y):
         N.check(N.lib().hc_apply_form_device(self.h, _dev_ptr(x, "float64"), _dev_ptr(y, "float64")), self.h)
         return y

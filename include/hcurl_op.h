@@ -29,10 +29,10 @@
  *    return without synchronising.
  *  - A handle is not re-entrant; different handles may be used from
  *    different host threads on different streams.
- *  - Dof numbering of the structured hex space (documented in the design doc and
- *    in hc_hex_dof_index below) is tensor-product: component c's dofs are
- *    open (Gauss-Legendre nodal) in direction c and closed (Gauss-Lobatto
- *    nodal) in the other two, x fastest, components concatenated.
+ *  - Dof numbering of the structured hex space (see hc_hex_dof_index) is
+ *    tensor-product: component c's dofs are open (Gauss-Legendre nodal) in
+ *    direction c and closed (Gauss-Lobatto nodal) in the other two, x
+ *    fastest, components concatenated.
  */
 #ifndef HCURL_OP_H
 #define HCURL_OP_H
@@ -150,6 +150,10 @@ hc_status hc_diag(hcop_t* h, double* d);
 hc_status hc_mult_device(hcop_t* h, const double* x, double* y);
 hc_status hc_mult_device_f32(hcop_t* h, const float* x, float* y);
 hc_status hc_apply_form_device(hcop_t* h, const double* x, double* y);
+/* y += P K P x (no initialisation of y; MFEM Operator::AddMult of the
+ * eliminated form without its identity block).  One kernel launch.        */
+hc_status hc_add_mult_device(hcop_t* h, const double* x, double* y);
+hc_status hc_add_mult_device_f32(hcop_t* h, const float* x, float* y);
 
 /* ---- linear solve --------------------------------------------------------- */
 /* Solve J x = b for x (x holds the initial guess on entry).  Replaces the

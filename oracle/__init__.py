@@ -44,6 +44,8 @@ def lib():
             "orc_apply_masked": (None, [vp, vp, vp, i32]),
             "orc_diag_masked": (None, [vp, vp]),
             "orc_apply_curlcurl": (None, [vp, vp, vp]),
+            "orc_build_eliminated": (i64, [vp]),
+            "orc_spmv_eliminated": (None, [vp, vp, vp, i32]),
             "orc_pcg": (i32, [vp, vp, vp, i32, i32, dbl, dbl, dbl, dbl, i32, i32, P(i32), P(dbl)]),
             "orc_lanczos_lmax": (dbl, [vp, i32, i32]),
             "orc_cheb_apply": (None, [vp, i32, dbl, dbl, vp, vp, i32]),

@@ -176,6 +176,11 @@ struct Prob {
   std::vector<uint8_t> ess;
   std::vector<double> dmask;  // diagonal of the eliminated operator
   std::vector<double> ebuf;   // cached element matrices (tets / mms)
+  // eliminated operator as hypre holds it: ess rows/cols dropped, unit
+  // diagonal on ess rows, 32-bit column indices
+  std::vector<int64_t> erp;
+  std::vector<int32_t> eci;
+  std::vector<double> eva;
   int q_curl = 0, q_mass = 0;  // points per direction for element matrices (0 = exact default)
 
   virtual ~Prob() = default;
@@ -307,6 +312,33 @@ struct Prob {
       for (i64 i = b; i < e; ++i) {
         double s = 0.0;
         for (i64 k = rp[i]; k < rp[i + 1]; ++k) s += va[k] * x[ci[k]];
+        y[i] = s;
+      }
+    });
+  }
+  void build_eliminated() {
+    erp.assign(ndof + 1, 0);
+    eci.clear();
+    eva.clear();
+    for (i64 i = 0; i < ndof; ++i) {
+      if (ess[i]) {
+        eci.push_back((int32_t)i);
+        eva.push_back(1.0);
+      } else {
+        for (i64 k = rp[i]; k < rp[i + 1]; ++k)
+          if (!ess[ci[k]]) {
+            eci.push_back((int32_t)ci[k]);
+            eva.push_back(va[k]);
+          }
+      }
+      erp[i + 1] = (i64)eci.size();
+    }
+  }
+  void spmv_eliminated(const double* x, double* y, int nthreads) const {
+    parallel_for(ndof, nthreads, [&](i64 b, i64 e) {
+      for (i64 i = b; i < e; ++i) {
+        double s = 0.0;
+        for (i64 k = erp[i]; k < erp[i + 1]; ++k) s += eva[k] * x[eci[k]];
         y[i] = s;
       }
     });
@@ -940,6 +972,16 @@ void orc_apply_curlcurl(void* h, const double* x, double* y) {
     }
   }
   P->beta = saved;
+}
+
+int64_t orc_build_eliminated(void* h) {
+  auto* P = static_cast<Prob*>(h);
+  if (P->ndof > 2147483647LL) return -1;
+  P->build_eliminated();
+  return (int64_t)P->eci.size();
+}
+void orc_spmv_eliminated(void* h, const double* x, double* y, int nthreads) {
+  static_cast<Prob*>(h)->spmv_eliminated(x, y, nthreads);
 }
 
 double orc_lanczos_lmax(void* h, int steps, int nthreads) {

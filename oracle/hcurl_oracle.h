@@ -84,6 +84,10 @@ void    orc_set_ess(void* h, const uint8_t* mask);
 void    orc_apply(void* h, const double* x, double* y, int nthreads);        /* K x      */
 void    orc_apply_masked(void* h, const double* x, double* y, int nthreads); /* PKPx+(I-P)x */
 void    orc_diag_masked(void* h, double* d);
+/* Eliminated operator stored as hypre holds it (ess rows/cols removed, unit
+ * diagonal, 32-bit columns); returns its nnz.  Used for the CPU baseline.  */
+int64_t orc_build_eliminated(void* h);
+void    orc_spmv_eliminated(void* h, const double* x, double* y, int nthreads);
 /* Curl-curl part alone (alpha only) -- WeakCurlCurlKernel's C_nu action.   */
 void    orc_apply_curlcurl(void* h, const double* x, double* y);
 

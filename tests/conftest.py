@@ -10,6 +10,12 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built library")
+    # (re)build the CUDA library and the oracle when their sources changed
+    from hephaestus_gb300 import build as hb
+    from oracle import build as ob
+
+    hb.build()
+    ob.build()
 
 
 def _has_gpu():

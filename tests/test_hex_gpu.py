@@ -127,7 +127,7 @@ def test_pcg_fp64_matches_oracle(precond):
     xr, st, it, rr = ref.pcg(b, precond=1, rtol=1e-13, maxit=100000)
     assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-9
     r = b - ref.apply_masked(x)
-    assert np.linalg.norm(r) / np.linalg.norm(b) < 2e-12
+    assert np.linalg.norm(r) / np.linalg.norm(b) < 5e-12  # recursive vs true residual gap
 
 
 def test_pcg_iterates_match_oracle_iteration_counts():
@@ -182,3 +182,19 @@ def test_non_affine_hex_rejected():
     with pytest.raises(Exception) as e:
         HCurlOperator(n, n, n, 1, np.ones(8), None, vertices=v)
     assert "parallelepiped" in str(e.value)
+
+
+def test_add_mult_device_accumulates():
+    import torch
+
+    op, ref, rng = _pair(4, 2)
+    x = rng.standard_normal(op.ndof)
+    y0 = rng.standard_normal(op.ndof)
+    m = op.ess_mask() == 1
+    want = y0 + np.where(m, 0.0, ref.apply_masked(np.where(m, 0.0, x)))
+    xd = torch.tensor(x, device="cuda")
+    yd = torch.tensor(y0, device="cuda")
+    op.AddMultDevice(xd, yd)
+    torch.cuda.synchronize()
+    got = yd.cpu().numpy()
+    assert np.linalg.norm(got - want) / np.linalg.norm(want) < TOL64

@@ -158,3 +158,18 @@ def test_pcg_matches_direct_solve():
         x, st, it, rr = P.pcg(b, precond=pre, rtol=1e-12, maxit=100000, **kw)
         assert st == 0
         assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 1e-8
+
+
+def test_eliminated_csr_matches_masked_apply():
+    n, p = 3, 2
+    P = oracle.Problem.hex(n, n, n, p)
+    rng = np.random.default_rng(6)
+    P.set_coef(rng.uniform(0.5, 2, P.ne), rng.uniform(0.5, 2, P.ne))
+    P.assemble()
+    P.set_ess(P.hex_ess_mask(0x3F))
+    nnz = oracle.lib().orc_build_eliminated(P.h)
+    assert 0 < nnz < oracle.lib().orc_nnz(P.h)
+    x = rng.standard_normal(P.ndof)
+    y = np.empty_like(x)
+    oracle.lib().orc_spmv_eliminated(P.h, oracle._p(x), oracle._p(y), 2)
+    assert np.allclose(y, P.apply_masked(x), rtol=1e-14, atol=1e-14)
