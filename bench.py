@@ -313,7 +313,7 @@ def run_ours(args):
                        "replicas": "one independent problem per rank (replicas only)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic,
-                         "kernel": "hex_apply_kernel<float,2,axis-aligned>",
+                         "kernel": "hex_apply_tiled<float,p=2,axis-aligned> (brick 16x4x2, persistent, cp.async double buffer)",
                          "alg_bytes_per_launch": alg, "kernel_ms": kern_s * 1e3,
                          "peak_source": hbm_src + " (MEASURED_PEAKS.json hbm_gbs)"},
             "fp64": {"value": gd64, "unit": "GDoF/s", "ms_per_apply": float(np.mean(t64)),

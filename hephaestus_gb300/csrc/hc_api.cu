@@ -181,6 +181,7 @@ void hc_destroy(hcop_t* h) {
   cudaFree(h->work);
   cudaFree(h->xbuf);
   cudaFree(h->ybuf);
+  cudaFree(h->tab);
   delete h;
 }
 
@@ -218,6 +219,8 @@ hc_status hc_create(const hc_problem_desc* desc, hcop_t** out) {
   h->off[2] = h->off[1] + (nxo + 1) * nyo * (nzo + 1);
   h->ndof = h->off[2] + (nxo + 1) * (nyo + 1) * nzo;
   const int64_t N = h->ndof;
+  if (N >= ((int64_t)1 << 31))
+    return fail_create(h, "hc_create: more than 2^31 - 1 dofs per problem is not supported", HC_ENOTSUP);
 
   // HBM budget: resident data + the largest solve work space (6 FP64 vectors)
   size_t need = (size_t)ne * 12 * (8 + 4) + (size_t)N * (1 + 8 * 3 + 4 * 2) + (size_t)N * 8 * 8;
@@ -338,6 +341,13 @@ hc_status hc_create(const hc_problem_desc* desc, hcop_t** out) {
       !alloc((void**)&h->dinvf, N * 4) || !alloc((void**)&h->sdinv, N * 8) || !alloc((void**)&h->sdinvf, N * 4) ||
       !alloc((void**)&h->xbuf, N * 8) || !alloc((void**)&h->ybuf, N * 8))
     return fail_create(h, "hc_create: device allocation failed", HC_ENOMEM);
+  {
+    std::vector<int> tab;
+    hex_tile_table(p, nx, ny, tab);
+    if (cudaMalloc((void**)&h->tab, tab.size() * sizeof(int)) != cudaSuccess)
+      return fail_create(h, "hc_create: device allocation failed", HC_ENOMEM);
+    cudaMemcpy(h->tab, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice);
+  }
   cudaMemcpy(h->fac, fac.data(), fac.size() * 8, cudaMemcpyHostToDevice);
   cudaMemcpy(h->facf, facf.data(), facf.size() * 4, cudaMemcpyHostToDevice);
   cudaMemcpy(h->ess, h->ess_host.data(), N, cudaMemcpyHostToDevice);
@@ -379,14 +389,14 @@ hc_status hc_mult_device_f32(hcop_t* h, const float* x, float* y) {
 hc_status hc_add_mult_device(hcop_t* h, const double* x, double* y) {
   if (!h || !x || !y) return HC_EINVAL;
   const OpJ<double> op{h, h->fac};
-  HC_CUDA_TRY(h, op.apply(x, y, nullptr, nullptr, h->stream));
+  HC_CUDA_TRY(h, op.apply(x, y, nullptr, nullptr, h->stream, false));
   return HC_OK;
 }
 
 hc_status hc_add_mult_device_f32(hcop_t* h, const float* x, float* y) {
   if (!h || !x || !y) return HC_EINVAL;
   const OpJ<float> op{h, h->facf};
-  HC_CUDA_TRY(h, op.apply(x, y, nullptr, nullptr, h->stream));
+  HC_CUDA_TRY(h, op.apply(x, y, nullptr, nullptr, h->stream, false));
   return HC_OK;
 }
 
@@ -394,7 +404,7 @@ hc_status hc_apply_form_device(hcop_t* h, const double* x, double* y) {
   if (!h || !x || !y) return HC_EINVAL;
   HC_CUDA_TRY(h, cudaMemsetAsync(y, 0, h->ndof * sizeof(double), h->stream));
   HC_CUDA_TRY(h, hex_apply<double>(h->hexdev(), h->fac, x, y, h->has_mass ? 1.0 : 0.0, 1.0, false, nullptr,
-                                   nullptr, h->stream));
+                                   nullptr, h->stream, true));
   return HC_OK;
 }
 
@@ -431,7 +441,7 @@ hc_status hc_add_weak_curlcurl(hcop_t* h, const double* x, double* y, double sca
   if (st != HC_OK) return st;
   // C_nu = (dt C_nu) / dt
   HC_CUDA_TRY(h, hex_apply<double>(h->hexdev(), h->fac, h->xbuf, h->ybuf, 0.0, scale / h->dt, false, nullptr,
-                                   nullptr, h->stream));
+                                   nullptr, h->stream, false));
   return d2h_sync(h, y, h->ybuf);
 }
 

@@ -1,6 +1,8 @@
 // hc_hex.cu -- dispatch of the hex apply kernels, the operator diagonal, and
 // the 1-D tables in constant memory.  The apply kernel itself is in
 // hc_hex_impl.cuh (instantiated per order in hc_hex_p{1,2,3}.cu).
+#include <algorithm>
+
 #include "hc_hex_impl.cuh"
 
 namespace hc {
@@ -9,12 +11,17 @@ cudaError_t upload_tables_p1(const void* td, const void* tf);
 cudaError_t upload_tables_p2(const void* td, const void* tf);
 cudaError_t upload_tables_p3(const void* td, const void* tf);
 
-int hex_apply_blocks(const HexDev& d) { return (int)((d.ne + 127) / 128); }
+// upper bound on the blocks of any apply launch (sizes the reduction partials)
+int hex_apply_blocks(const HexDev& d) {
+  const int legacy = (int)((d.ne + 127) / 128);
+  const int b1 = brick_blocks<1>(d), b2 = brick_blocks<2>(d), b3 = brick_blocks<3>(d);
+  return std::max(std::max(legacy, b1), std::max(b2, b3));
+}
 
 // instantiated in hc_hex_p{1,2,3}.cu
 #define HC_EXTERN_LAUNCH(T, P)                                                                          \
   extern template cudaError_t hex_launch_p<T, P>(const HexDev&, const T*, const T*, T*, T, T, bool,     \
-                                                 KrylovScalars*, double*, cudaStream_t);
+                                                 KrylovScalars*, double*, cudaStream_t, bool);
 HC_EXTERN_LAUNCH(double, 1)
 HC_EXTERN_LAUNCH(double, 2)
 HC_EXTERN_LAUNCH(double, 3)
@@ -25,18 +32,18 @@ HC_EXTERN_LAUNCH(float, 3)
 
 template <typename T>
 cudaError_t hex_apply(const HexDev& d, const T* fac, const T* x, T* y, double ms, double cs, bool masked,
-                      KrylovScalars* S, double* partials, cudaStream_t s) {
+                      KrylovScalars* S, double* partials, cudaStream_t s, bool yz) {
   switch (d.p) {
-    case 1: return hex_launch_p<T, 1>(d, fac, x, y, (T)ms, (T)cs, masked, S, partials, s);
-    case 2: return hex_launch_p<T, 2>(d, fac, x, y, (T)ms, (T)cs, masked, S, partials, s);
-    case 3: return hex_launch_p<T, 3>(d, fac, x, y, (T)ms, (T)cs, masked, S, partials, s);
+    case 1: return hex_launch_p<T, 1>(d, fac, x, y, (T)ms, (T)cs, masked, S, partials, s, yz);
+    case 2: return hex_launch_p<T, 2>(d, fac, x, y, (T)ms, (T)cs, masked, S, partials, s, yz);
+    case 3: return hex_launch_p<T, 3>(d, fac, x, y, (T)ms, (T)cs, masked, S, partials, s, yz);
     default: return cudaErrorInvalidValue;
   }
 }
 template cudaError_t hex_apply<double>(const HexDev&, const double*, const double*, double*, double, double,
-                                       bool, KrylovScalars*, double*, cudaStream_t);
+                                       bool, KrylovScalars*, double*, cudaStream_t, bool);
 template cudaError_t hex_apply<float>(const HexDev&, const float*, const float*, float*, double, double,
-                                      bool, KrylovScalars*, double*, cudaStream_t);
+                                      bool, KrylovScalars*, double*, cudaStream_t, bool);
 
 // ---------------------------------------------------------------------------
 // Diagonal of K (FP64).  For a unit dof vector the element curl is a sum of
@@ -150,6 +157,12 @@ cudaError_t hex_diag(const HexDev& d, double* diag, cudaStream_t s) {
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
+}
+
+void hex_tile_table(int p, int nx, int ny, std::vector<int>& tab) {
+  if (p == 1) build_tile_table<1>(nx, ny, tab);
+  else if (p == 2) build_tile_table<2>(nx, ny, tab);
+  else tab.assign(1, 0);
 }
 
 cudaError_t upload_tables() {

@@ -22,7 +22,9 @@
 // fully unrolled compile-time 1-D contractions, implicit structured
 // element->dof map (no index array), atomic scatter into y.
 #pragma once
+#include <algorithm>
 #include <cstdio>
+#include <vector>
 
 #include "hc_internal.h"
 #include "hc_reduce.cuh"
@@ -407,15 +409,487 @@ __global__ void __launch_bounds__(128) hex_apply_kernel(HexDev d, const T* __res
   }
 }
 
+// ---------------------------------------------------------------------------
+// Brick-tiled apply: one CTA per brick of BX x BY x BZ elements, one thread per
+// element.  The brick's dofs (both closed boundary planes included) are
+// staged in shared memory by coalesced cooperative loads; each thread runs the
+// register-resident element operator on its element, accumulating into a
+// shared output tile (shared-memory atomics, at most 4 writers per dof); the
+// tile is then flushed with one coalesced global reduction per dof, so a
+// dof on a brick face receives one atomic per adjacent brick instead of one
+// per adjacent element.
+// ---------------------------------------------------------------------------
+template <int P, int BX, int BY, int BZ>
+struct BrickTile {
+  static constexpr int tx(int c) { return BX * P + (c != 0); }
+  static constexpr int ty(int c) { return BY * P + (c != 1); }
+  static constexpr int tz(int c) { return BZ * P + (c != 2); }
+  static constexpr int n(int c) { return tx(c) * ty(c) * tz(c); }
+  static constexpr int off(int c) { return c == 0 ? 0 : (c == 1 ? n(0) : n(0) + n(1)); }
+  static constexpr int total = n(0) + n(1) + n(2);
+};
+
+template <int P, int comp>
+__device__ __forceinline__ int64_t gdof_ijk(const HexDev& d, int64_t i, int64_t j, int64_t k) {
+  const int64_t nxo = (int64_t)d.nx * P, nyo = (int64_t)d.ny * P;
+  if constexpr (comp == 0) return d.off[0] + i + nxo * (j + (nyo + 1) * k);
+  else if constexpr (comp == 1) return d.off[1] + i + (nxo + 1) * (j + nyo * k);
+  else return d.off[2] + i + (nxo + 1) * (j + (nyo + 1) * k);
+}
+template <int P, int comp>
+__device__ __forceinline__ bool ess_ijk(const HexDev& d, int64_t g, int i, int j, int k) {
+  if (d.ess) return d.ess[g] != 0;
+  const int bits = d.ess_bits;
+  const int mx = d.nx * P, my = d.ny * P, mz = d.nz * P;
+  bool e = false;
+  if (comp != 0) e |= (i == 0 && (bits & 1)) || (i == mx && (bits & 2));
+  if (comp != 1) e |= (j == 0 && (bits & 4)) || (j == my && (bits & 8));
+  if (comp != 2) e |= (k == 0 && (bits & 16)) || (k == mz && (bits & 32));
+  return e;
+}
+
+// Visit the tile entries of component comp owned by thread t in a
+// block-strided loop: f(tile_index, global_dof, i, j, k) for entries inside the grid.
+template <int P, int BX, int BY, int BZ, int comp, typename F>
+__device__ __forceinline__ void tile_loop(const HexDev& d, int X0, int Y0, int Z0, F&& f) {
+  using TL = BrickTile<P, BX, BY, BZ>;
+  constexpr int TX = TL::tx(comp), TY = TL::ty(comp), NC = TL::n(comp), OFF = TL::off(comp);
+  const int gdx = d.nx * P + (comp != 0), gdy = d.ny * P + (comp != 1), gdz = d.nz * P + (comp != 2);
+  for (int r = threadIdx.x; r < NC; r += BX * BY * BZ) {
+    const int ti = r % TX, tj = (r / TX) % TY, tk = r / (TX * TY);
+    const int i = X0 * P + ti, j = Y0 * P + tj, k = Z0 * P + tk;
+    if (i < gdx && j < gdy && k < gdz) f(OFF + r, gdof_ijk<P, comp>(d, i, j, k), i, j, k);
+  }
+}
+
+template <typename T, int P, int BX, int BY, int BZ, int comp>
+__device__ __forceinline__ void sgather(const T* sx, int lx, int ly, int lz, T* u) {
+  using TL = BrickTile<P, BX, BY, BZ>;
+  constexpr int C = P + 1, O = P;
+  constexpr int n0 = comp == 0 ? O : C, n1 = comp == 1 ? O : C, n2 = comp == 2 ? O : C;
+  constexpr int TX = TL::tx(comp), TY = TL::ty(comp), OFF = TL::off(comp);
+#pragma unroll
+  for (int c = 0; c < n2; ++c)
+#pragma unroll
+    for (int b = 0; b < n1; ++b)
+#pragma unroll
+      for (int a = 0; a < n0; ++a)
+        u[a + n0 * (b + n1 * c)] = sx[OFF + (lx * P + a) + TX * ((ly * P + b) + TY * (lz * P + c))];
+}
+template <typename T, int P, int BX, int BY, int BZ, int comp>
+__device__ __forceinline__ void sscatter(T* sy, int lx, int ly, int lz, const T* v) {
+  using TL = BrickTile<P, BX, BY, BZ>;
+  constexpr int C = P + 1, O = P;
+  constexpr int n0 = comp == 0 ? O : C, n1 = comp == 1 ? O : C, n2 = comp == 2 ? O : C;
+  constexpr int TX = TL::tx(comp), TY = TL::ty(comp), OFF = TL::off(comp);
+#pragma unroll
+  for (int c = 0; c < n2; ++c)
+#pragma unroll
+    for (int b = 0; b < n1; ++b)
+#pragma unroll
+      for (int a = 0; a < n0; ++a)
+        atomicAdd(&sy[OFF + (lx * P + a) + TX * ((ly * P + b) + TY * (lz * P + c))], v[a + n0 * (b + n1 * c)]);
+}
+
+// cp.async (4-byte, zero-fill when src_bytes == 0): asynchronous global ->
+// shared copies that do not occupy registers, so a whole brick is in flight.
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem, int src_bytes) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem, int src_bytes) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+
+struct BrickGeom {
+  int X0, Y0, Z0;
+};
+template <int BX, int BY, int BZ>
+__device__ __forceinline__ BrickGeom brick_of(const HexDev& d, int b) {
+  const int nbx = (d.nx + BX - 1) / BX, nby = (d.ny + BY - 1) / BY;
+  BrickGeom g;
+  g.X0 = (b % nbx) * BX;
+  g.Y0 = ((b / nbx) % nby) * BY;
+  g.Z0 = (b / (nbx * nby)) * BZ;
+  return g;
+}
+
+// Issue the asynchronous copies of one brick's dofs (all three components)
+// into sx; entries outside the grid are zero-filled.
+template <typename T, int P, int BX, int BY, int BZ, int comp>
+__device__ __forceinline__ void prefetch_comp(const HexDev& d, const T* __restrict__ x, T* sx, BrickGeom bg) {
+  using TL = BrickTile<P, BX, BY, BZ>;
+  constexpr int TX = TL::tx(comp), TY = TL::ty(comp), NC = TL::n(comp), OFF = TL::off(comp);
+  const int gdx = d.nx * P + (comp != 0), gdy = d.ny * P + (comp != 1), gdz = d.nz * P + (comp != 2);
+  const int base = (int)d.off[comp] + bg.X0 * P + gdx * (bg.Y0 * P + gdy * (bg.Z0 * P));
+  const bool full = bg.X0 + BX <= d.nx && bg.Y0 + BY <= d.ny && bg.Z0 + BZ <= d.nz;
+  if (full) {
+    // precomputed relative offsets: one load and one add per entry
+#pragma unroll 4
+    for (int r = threadIdx.x; r < NC; r += BX * BY * BZ) {
+      const int t = __ldg(d.tab + OFF + r) & 0x7fffffff;
+      if constexpr (sizeof(T) == 4) cp_async4(sx + OFF + r, x + base + t, 4);
+      else cp_async8(sx + OFF + r, x + base + t, 8);
+    }
+    return;
+  }
+#pragma unroll 4
+  for (int r = threadIdx.x; r < NC; r += BX * BY * BZ) {
+    const int ti = r % TX, tj = (r / TX) % TY, tk = r / (TX * TY);
+    const bool in = (bg.X0 * P + ti < gdx) && (bg.Y0 * P + tj < gdy) && (bg.Z0 * P + tk < gdz);
+    const T* src = in ? x + (base + ti + gdx * (tj + gdy * tk)) : x;
+    if constexpr (sizeof(T) == 4) cp_async4(sx + OFF + r, src, in ? 4 : 0);
+    else cp_async8(sx + OFF + r, src, in ? 8 : 0);
+  }
+}
+
+// Zero one boundary plane (direction dir, low or high side) of component comp.
+template <typename T, int P, int BX, int BY, int BZ, int comp, int dir>
+__device__ __forceinline__ void zero_plane(T* buf, int idx) {
+  using TL = BrickTile<P, BX, BY, BZ>;
+  constexpr int TX = TL::tx(comp), TY = TL::ty(comp), TZ = TL::tz(comp), OFF = TL::off(comp);
+  constexpr int NA = dir == 0 ? TY : TX, NB = dir == 2 ? TY : TZ;
+  for (int r = threadIdx.x; r < NA * NB; r += BX * BY * BZ) {
+    const int a = r % NA, b = r / NA;
+    int ti, tj, tk;
+    if constexpr (dir == 0) { ti = idx; tj = a; tk = b; }
+    else if constexpr (dir == 1) { ti = a; tj = idx; tk = b; }
+    else { ti = a; tj = b; tk = idx; }
+    buf[OFF + ti + TX * (tj + TY * tk)] = T(0);
+  }
+}
+// Zero the essential entries of a staged brick from an explicit mask.
+template <typename T, int P, int BX, int BY, int BZ, int comp>
+__device__ __forceinline__ void mask_comp(const HexDev& d, T* sx, BrickGeom bg) {
+  using TL = BrickTile<P, BX, BY, BZ>;
+  constexpr int TX = TL::tx(comp), TY = TL::ty(comp), NC = TL::n(comp), OFF = TL::off(comp);
+  const int gdx = d.nx * P + (comp != 0), gdy = d.ny * P + (comp != 1), gdz = d.nz * P + (comp != 2);
+  for (int r = threadIdx.x; r < NC; r += BX * BY * BZ) {
+    const int i = bg.X0 * P + r % TX, j = bg.Y0 * P + (r / TX) % TY, k = bg.Z0 * P + r / (TX * TY);
+    if (i >= gdx || j >= gdy || k >= gdz) continue;
+    const int64_t g = d.off[comp] + i + (int64_t)gdx * (j + (int64_t)gdy * k);
+    if (ess_ijk<P, comp>(d, g, i, j, k)) sx[OFF + r] = T(0);
+  }
+}
+
+// Zero the tangential (essential) entries on the marked grid faces the brick
+// touches.  The high face of the grid is at local plane (n - X0) p, which is
+// the brick's last plane for full bricks and inside the tile for partial ones.
+template <typename T, int P, int BX, int BY, int BZ>
+__device__ __forceinline__ void zero_ess_planes(const HexDev& d, T* buf, BrickGeom bg) {
+  const int bits = d.ess_bits;
+  if (bg.X0 == 0 && (bits & 1)) {
+    zero_plane<T, P, BX, BY, BZ, 1, 0>(buf, 0);
+    zero_plane<T, P, BX, BY, BZ, 2, 0>(buf, 0);
+  }
+  if (bg.X0 + BX >= d.nx && (bits & 2)) {
+    const int hi = (d.nx - bg.X0) * P;
+    zero_plane<T, P, BX, BY, BZ, 1, 0>(buf, hi);
+    zero_plane<T, P, BX, BY, BZ, 2, 0>(buf, hi);
+  }
+  if (bg.Y0 == 0 && (bits & 4)) {
+    zero_plane<T, P, BX, BY, BZ, 0, 1>(buf, 0);
+    zero_plane<T, P, BX, BY, BZ, 2, 1>(buf, 0);
+  }
+  if (bg.Y0 + BY >= d.ny && (bits & 8)) {
+    const int hi = (d.ny - bg.Y0) * P;
+    zero_plane<T, P, BX, BY, BZ, 0, 1>(buf, hi);
+    zero_plane<T, P, BX, BY, BZ, 2, 1>(buf, hi);
+  }
+  if (bg.Z0 == 0 && (bits & 16)) {
+    zero_plane<T, P, BX, BY, BZ, 0, 2>(buf, 0);
+    zero_plane<T, P, BX, BY, BZ, 1, 2>(buf, 0);
+  }
+  if (bg.Z0 + BZ >= d.nz && (bits & 32)) {
+    const int hi = (d.nz - bg.Z0) * P;
+    zero_plane<T, P, BX, BY, BZ, 0, 2>(buf, hi);
+    zero_plane<T, P, BX, BY, BZ, 1, 2>(buf, hi);
+  }
+}
+
+// Flush one component of the output tile.  Entries on a brick face are shared
+// with a neighbouring brick and go out as atomic adds; brick-interior entries
+// are written with plain stores when y is known to be zero at free dofs
+// (OVERWRITE), else added atomically.  Essential rows are skipped when masked.
+// fast: full brick and (if masked) face-attribute masking already applied by
+// zeroing the essential planes of sy -- every essential dof lies on a brick
+// face, so it only ever receives an atomic add of zero.
+template <typename T, int P, int BX, int BY, int BZ, int comp, bool OVERWRITE>
+__device__ __forceinline__ void flush_comp(const HexDev& d, T* __restrict__ y, T* sy, BrickGeom bg, bool mk,
+                                           bool fast) {
+  using TL = BrickTile<P, BX, BY, BZ>;
+  constexpr int TX = TL::tx(comp), TY = TL::ty(comp), TZ = TL::tz(comp), NC = TL::n(comp), OFF = TL::off(comp);
+  const int gdx = d.nx * P + (comp != 0), gdy = d.ny * P + (comp != 1), gdz = d.nz * P + (comp != 2);
+  const int base = (int)d.off[comp] + bg.X0 * P + gdx * (bg.Y0 * P + gdy * (bg.Z0 * P));
+  if (fast) {
+#pragma unroll 4
+    for (int r = threadIdx.x; r < NC; r += BX * BY * BZ) {
+      const int t = __ldg(d.tab + OFF + r);
+      const T v = sy[OFF + r];
+      sy[OFF + r] = T(0);
+      T* dst = y + base + (t & 0x7fffffff);
+      if (OVERWRITE && t >= 0) *dst = v;
+      else atomicAdd(dst, v);
+    }
+    return;
+  }
+#pragma unroll 2
+  for (int r = threadIdx.x; r < NC; r += BX * BY * BZ) {
+    const int ti = r % TX, tj = (r / TX) % TY, tk = r / (TX * TY);
+    const int i = bg.X0 * P + ti, j = bg.Y0 * P + tj, k = bg.Z0 * P + tk;
+    const T v = sy[OFF + r];
+    sy[OFF + r] = T(0);
+    if (i >= gdx || j >= gdy || k >= gdz) continue;
+    const int g = base + ti + gdx * (tj + gdy * tk);
+    if (mk && ess_ijk<P, comp>(d, g, i, j, k)) continue;
+    // a closed-direction index on the brick's first or last plane is shared
+    const bool face = (comp != 0 && (ti == 0 || ti == TX - 1)) || (comp != 1 && (tj == 0 || tj == TY - 1)) ||
+                      (comp != 2 && (tk == 0 || tk == TZ - 1));
+    if (OVERWRITE && !face) y[g] = v;
+    else atomicAdd(y + g, v);
+  }
+}
+
+template <typename T, int P, bool FULL, int BX, int BY, int BZ, bool OVERWRITE>
+__global__ void __launch_bounds__(BX* BY* BZ, sizeof(T) == 4 ? 3 : 2)
+    hex_apply_tiled(HexDev d, const T* __restrict__ fac, const T* __restrict__ x, T* __restrict__ y, T mscale,
+                    T cscale, int masked, KrylovScalars* S, double* partials, int nbricks) {
+  if (S && S->done) return;
+  using TL = BrickTile<P, BX, BY, BZ>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sxb[2] = {reinterpret_cast<T*>(smem_raw), reinterpret_cast<T*>(smem_raw) + TL::total};
+  T* sy = reinterpret_cast<T*>(smem_raw) + 2 * TL::total;
+  const bool mk = masked != 0;
+  const bool mask_needed = mk && (d.ess != nullptr || d.ess_bits != 0);
+  constexpr int C = P + 1, O = P;
+  constexpr int NDC = O * C * C;
+  constexpr int RTC = C * O * O;
+  const int lx = threadIdx.x % BX, ly = (threadIdx.x / BX) % BY, lz = threadIdx.x / (BX * BY);
+  for (int r = threadIdx.x; r < TL::total; r += BX * BY * BZ) sy[r] = T(0);
+  double en = 0.0;
+  int b = blockIdx.x;
+  if (b < nbricks) {
+    const BrickGeom g0 = brick_of<BX, BY, BZ>(d, b);
+    prefetch_comp<T, P, BX, BY, BZ, 0>(d, x, sxb[0], g0);
+    prefetch_comp<T, P, BX, BY, BZ, 1>(d, x, sxb[0], g0);
+    prefetch_comp<T, P, BX, BY, BZ, 2>(d, x, sxb[0], g0);
+  }
+  cp_async_commit();
+  for (int it = 0; b < nbricks; b += gridDim.x, ++it) {
+    T* sx = sxb[it & 1];
+    const BrickGeom bg = brick_of<BX, BY, BZ>(d, b);
+    const int bn = b + gridDim.x;
+    if (bn < nbricks) {  // prefetch the next brick into the other buffer
+      const BrickGeom gn = brick_of<BX, BY, BZ>(d, bn);
+      T* sn = sxb[(it + 1) & 1];
+      prefetch_comp<T, P, BX, BY, BZ, 0>(d, x, sn, gn);
+      prefetch_comp<T, P, BX, BY, BZ, 1>(d, x, sn, gn);
+      prefetch_comp<T, P, BX, BY, BZ, 2>(d, x, sn, gn);
+    }
+    cp_async_commit();
+    cp_async_wait<1>();  // this brick's group has landed
+    __syncthreads();
+    const bool full = bg.X0 + BX <= d.nx && bg.Y0 + BY <= d.ny && bg.Z0 + BZ <= d.nz;
+    const bool touches = bg.X0 == 0 || bg.Y0 == 0 || bg.Z0 == 0 || bg.X0 + BX >= d.nx || bg.Y0 + BY >= d.ny ||
+                         bg.Z0 + BZ >= d.nz;
+    const bool fast = full && d.ess == nullptr;
+    if (mask_needed && (d.ess != nullptr || touches)) {
+      if (d.ess != nullptr) {
+        mask_comp<T, P, BX, BY, BZ, 0>(d, sx, bg);
+        mask_comp<T, P, BX, BY, BZ, 1>(d, sx, bg);
+        mask_comp<T, P, BX, BY, BZ, 2>(d, sx, bg);
+      } else {
+        zero_ess_planes<T, P, BX, BY, BZ>(d, sx, bg);
+      }
+      __syncthreads();
+    }
+    const int ex = bg.X0 + lx, ey = bg.Y0 + ly, ez = bg.Z0 + lz;
+    if (ex < d.nx && ey < d.ny && ez < d.nz) {
+      const int e = ex + d.nx * (ey + d.ny * ez);
+      T u0[NDC], u1[NDC], u2[NDC];
+      sgather<T, P, BX, BY, BZ, 0>(sx, lx, ly, lz, u0);
+      sgather<T, P, BX, BY, BZ, 1>(sx, lx, ly, lz, u1);
+      sgather<T, P, BX, BY, BZ, 2>(sx, lx, ly, lz, u2);
+      T fm[6], fc[6];
+      if constexpr (FULL) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+          fm[k] = mscale * __ldg(fac + (int64_t)k * d.ne + e);
+          fc[k] = cscale * __ldg(fac + (int64_t)(6 + k) * d.ne + e);
+        }
+      } else {
+        constexpr int kd[3] = {0, 3, 5};
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          fm[kd[q]] = mscale * __ldg(fac + (int64_t)kd[q] * d.ne + e);
+          fc[kd[q]] = cscale * __ldg(fac + (int64_t)(6 + kd[q]) * d.ne + e);
+        }
+      }
+      T r0[RTC], r1[RTC], r2[RTC];
+      curl_nd<T, P>(u0, u1, u2, r0, r1, r2);
+      T y0[NDC], y1[NDC], y2[NDC];
+#pragma unroll
+      for (int i = 0; i < NDC; ++i) y0[i] = y1[i] = y2[i] = T(0);
+      if (mscale != T(0)) {
+        mass_block<T, P, 0, 0>(u0, y0, fm[0]);
+        mass_block<T, P, 1, 1>(u1, y1, fm[3]);
+        mass_block<T, P, 2, 2>(u2, y2, fm[5]);
+        if constexpr (FULL) {
+          mass_block<T, P, 0, 1>(u1, y0, fm[1]);
+          mass_block<T, P, 0, 2>(u2, y0, fm[2]);
+          mass_block<T, P, 1, 0>(u0, y1, fm[1]);
+          mass_block<T, P, 1, 2>(u2, y1, fm[4]);
+          mass_block<T, P, 2, 0>(u0, y2, fm[2]);
+          mass_block<T, P, 2, 1>(u1, y2, fm[4]);
+        }
+      }
+      T eacc = T(0);
+      if (S) {
+#pragma unroll
+        for (int i = 0; i < NDC; ++i) eacc += u0[i] * y0[i] + u1[i] * y1[i] + u2[i] * y2[i];
+      }
+      T g0[RTC], g1[RTC], g2[RTC];
+#pragma unroll
+      for (int i = 0; i < RTC; ++i) g0[i] = g1[i] = g2[i] = T(0);
+      rt_block<T, P, 0, 0>(r0, g0, fc[0]);
+      rt_block<T, P, 1, 1>(r1, g1, fc[3]);
+      rt_block<T, P, 2, 2>(r2, g2, fc[5]);
+      if constexpr (FULL) {
+        rt_block<T, P, 0, 1>(r1, g0, fc[1]);
+        rt_block<T, P, 0, 2>(r2, g0, fc[2]);
+        rt_block<T, P, 1, 0>(r0, g1, fc[1]);
+        rt_block<T, P, 1, 2>(r2, g1, fc[4]);
+        rt_block<T, P, 2, 0>(r0, g2, fc[2]);
+        rt_block<T, P, 2, 1>(r1, g2, fc[4]);
+      }
+      if (S) {
+#pragma unroll
+        for (int i = 0; i < RTC; ++i) eacc += r0[i] * g0[i] + r1[i] * g1[i] + r2[i] * g2[i];
+        en += (double)eacc;
+      }
+      curl_nd_t<T, P>(g0, g1, g2, y0, y1, y2);
+      sscatter<T, P, BX, BY, BZ, 0>(sy, lx, ly, lz, y0);
+      sscatter<T, P, BX, BY, BZ, 1>(sy, lx, ly, lz, y1);
+      sscatter<T, P, BX, BY, BZ, 2>(sy, lx, ly, lz, y2);
+    }
+    __syncthreads();
+    if (fast && mk && touches && d.ess_bits) {
+      zero_ess_planes<T, P, BX, BY, BZ>(d, sy, bg);
+      __syncthreads();
+    }
+    flush_comp<T, P, BX, BY, BZ, 0, OVERWRITE>(d, y, sy, bg, mk, fast);
+    flush_comp<T, P, BX, BY, BZ, 1, OVERWRITE>(d, y, sy, bg, mk, fast);
+    flush_comp<T, P, BX, BY, BZ, 2, OVERWRITE>(d, y, sy, bg, mk, fast);
+    // the next iteration's scatter into sy and prefetch into this buffer
+    // happen after every thread passed the barrier at the top of the loop
+  }
+  cp_async_wait<0>();
+  if (S) {
+    double v[1] = {en}, tot[1];
+    block_sum_n<1>(v);
+    if (grid_sum_n<1>(v, partials, &S->counter[0], tot)) {
+      const double pq = S->pq + tot[0];
+      S->pq = pq;
+      if (!(pq > 0.0) || !isfinite(pq)) {
+        S->done = 1;
+        S->status = HC_BREAKDOWN;
+        S->alpha = 0.0;
+      } else {
+        S->alpha = S->rz / pq;
+      }
+    }
+  }
+}
+
+template <int P>
+struct BrickShape;
+template <>
+struct BrickShape<1> {
+  static constexpr int BX = 16, BY = 4, BZ = 2;
+};
+template <>
+struct BrickShape<2> {
+  static constexpr int BX = 16, BY = 4, BZ = 2;
+};
+template <>
+struct BrickShape<3> {
+  static constexpr int BX = 4, BY = 4, BZ = 4;
+};
+
+// Host: per tile entry the dof offset relative to the brick's base (bit 31 set
+// when the entry lies on a brick face, i.e. is shared with a neighbour brick).
+template <int P>
+inline void build_tile_table(int nx, int ny, std::vector<int>& tab) {
+  using B = BrickShape<P>;
+  using TL = BrickTile<P, B::BX, B::BY, B::BZ>;
+  tab.assign(TL::total, 0);
+  for (int c = 0; c < 3; ++c) {
+    const int TX = TL::tx(c), TY = TL::ty(c), TZ = TL::tz(c);
+    const int gdx = nx * P + (c != 0), gdy = ny * P + (c != 1);
+    for (int r = 0; r < TL::n(c); ++r) {
+      const int ti = r % TX, tj = (r / TX) % TY, tk = r / (TX * TY);
+      const bool face = (c != 0 && (ti == 0 || ti == TX - 1)) || (c != 1 && (tj == 0 || tj == TY - 1)) ||
+                        (c != 2 && (tk == 0 || tk == TZ - 1));
+      const int rel = ti + gdx * (tj + gdy * tk);
+      tab[TL::off(c) + r] = rel | (face ? (int)0x80000000u : 0);
+    }
+  }
+}
+
+template <int P>
+__host__ __device__ inline int brick_blocks(const HexDev& d) {
+  using B = BrickShape<P>;
+  return ((d.nx + B::BX - 1) / B::BX) * ((d.ny + B::BY - 1) / B::BY) * ((d.nz + B::BZ - 1) / B::BZ);
+}
+
 template <typename T, int P>
 cudaError_t hex_launch_p(const HexDev& d, const T* fac, const T* x, T* y, T ms, T cs, bool masked,
-                         KrylovScalars* S, double* partials, cudaStream_t s) {
-  const int blocks = (int)((d.ne + 127) / 128);
-  if (d.full)
-    hex_apply_kernel<T, P, true><<<blocks, 128, 0, s>>>(d, fac, x, y, ms, cs, masked, S, partials);
-  else
-    hex_apply_kernel<T, P, false><<<blocks, 128, 0, s>>>(d, fac, x, y, ms, cs, masked, S, partials);
-  return cudaGetLastError();
+                         KrylovScalars* S, double* partials, cudaStream_t s, bool y_zero_free) {
+  if constexpr (P <= 2) {
+    using B = BrickShape<P>;
+    using TL = BrickTile<P, B::BX, B::BY, B::BZ>;
+    const size_t sm = 3 * TL::total * sizeof(T);
+    const int nbricks = brick_blocks<P>(d);
+    constexpr int nt = B::BX * B::BY * B::BZ;
+    static int per_sm[2][2][2] = {{{0, 0}, {0, 0}}, {{0, 0}, {0, 0}}};
+    static int nsm = 0;
+    if (!nsm) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    }
+    auto go = [&](auto kern, int f, int o) {
+      int& occ = per_sm[f][o][sizeof(T) == 8];
+      if (!occ) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nt, sm);
+        if (occ < 1) occ = 1;
+      }
+      const int grid = std::min(nbricks, occ * nsm);
+      kern<<<grid, nt, sm, s>>>(d, fac, x, y, ms, cs, masked, S, partials, nbricks);
+    };
+    if (d.full) {
+      if (y_zero_free) go(hex_apply_tiled<T, P, true, B::BX, B::BY, B::BZ, true>, 1, 1);
+      else go(hex_apply_tiled<T, P, true, B::BX, B::BY, B::BZ, false>, 1, 0);
+    } else {
+      if (y_zero_free) go(hex_apply_tiled<T, P, false, B::BX, B::BY, B::BZ, true>, 0, 1);
+      else go(hex_apply_tiled<T, P, false, B::BX, B::BY, B::BZ, false>, 0, 0);
+    }
+    return cudaGetLastError();
+  } else {
+    const int blocks = (int)((d.ne + 127) / 128);
+    if (d.full)
+      hex_apply_kernel<T, P, true><<<blocks, 128, 0, s>>>(d, fac, x, y, ms, cs, masked, S, partials);
+    else
+      hex_apply_kernel<T, P, false><<<blocks, 128, 0, s>>>(d, fac, x, y, ms, cs, masked, S, partials);
+    return cudaGetLastError();
+  }
 }
 
 }  // namespace hc

@@ -4,8 +4,8 @@
 
 namespace hc {
 template cudaError_t hex_launch_p<double, 1>(const HexDev&, const double*, const double*, double*, double,
-                                             double, bool, KrylovScalars*, double*, cudaStream_t);
+                                             double, bool, KrylovScalars*, double*, cudaStream_t, bool);
 template cudaError_t hex_launch_p<float, 1>(const HexDev&, const float*, const float*, float*, float, float,
-                                            bool, KrylovScalars*, double*, cudaStream_t);
+                                            bool, KrylovScalars*, double*, cudaStream_t, bool);
 cudaError_t upload_tables_p1(const void* td, const void* tf) { return upload_tables_here(td, tf); }
 }  // namespace hc

@@ -58,6 +58,7 @@ struct HexDev {
   int ess_bits;       // face attribute bits (implicit mask)
   const uint8_t* ess; // explicit device mask or nullptr
   const double* fac;  // FP64 factors (diagonal, FP64 apply)
+  const int* tab;     // brick tile table (relative dof offsets, bit 31 = brick face)
 };
 
 }  // namespace hc
@@ -94,6 +95,7 @@ struct hcop {
   double* xbuf = nullptr;              // device staging for host-pointer calls
   double* ybuf = nullptr;
   double lmax64 = 0.0, lmax32 = 0.0;   // cached Chebyshev bounds
+  int* tab = nullptr;                  // brick tile table of the apply kernel
 
   hc::HexDev hexdev() const {
     hc::HexDev d;
@@ -110,6 +112,7 @@ struct hcop {
     d.ess_bits = ess_bits;
     d.ess = explicit_mask ? ess : nullptr;
     d.fac = fac;
+    d.tab = tab;
     return d;
   }
 };
@@ -122,10 +125,14 @@ int hex_apply_blocks(const HexDev& d);
 // (y must already hold (I-P)x for J).  mscale/cscale multiply the mass/curl
 // factors.  S != nullptr: PCG mode (energy p.Jp accumulated onto S->pq,
 // alpha formed, skipped when S->done).
+// y_zero_free: the caller guarantees y == 0 at every non-essential dof, so
+// brick-interior results may be stored instead of added.
 template <typename T>
 cudaError_t hex_apply(const HexDev& d, const T* fac, const T* x, T* y, double mscale, double cscale,
-                      bool masked, KrylovScalars* S, double* partials, cudaStream_t s);
+                      bool masked, KrylovScalars* S, double* partials, cudaStream_t s, bool y_zero_free);
 cudaError_t hex_diag(const HexDev& d, double* diag, cudaStream_t s);
+// tile table of the brick kernel for order p on an nx x ny grid (host)
+void hex_tile_table(int p, int nx, int ny, std::vector<int>& tab);
 
 // ---- hc_krylov.cu ----
 cudaError_t diag_finish(int64_t n, const uint8_t* ess, double* d, double* dinv, float* dinvf, double* sd,
@@ -138,7 +145,8 @@ template <typename T>
 struct OpJ {
   hcop* h;
   const T* fac;
-  cudaError_t apply(const T* x, T* y, KrylovScalars* S, double* partials, cudaStream_t s) const;
+  cudaError_t apply(const T* x, T* y, KrylovScalars* S, double* partials, cudaStream_t s,
+                    bool y_zero_free = true) const;
 };
 struct SolveCfg {
   int precond;

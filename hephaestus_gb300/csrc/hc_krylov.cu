@@ -77,9 +77,10 @@ template cudaError_t init_masked<double>(int64_t, const uint8_t*, const double*,
 template cudaError_t init_masked<float>(int64_t, const uint8_t*, const float*, float*, cudaStream_t);
 
 template <typename T>
-cudaError_t OpJ<T>::apply(const T* x, T* y, KrylovScalars* S, double* partials, cudaStream_t s) const {
+cudaError_t OpJ<T>::apply(const T* x, T* y, KrylovScalars* S, double* partials, cudaStream_t s,
+                          bool y_zero_free) const {
   const HexDev d = h->hexdev();
-  return hex_apply<T>(d, fac, x, y, h->has_mass ? 1.0 : 0.0, 1.0, true, S, partials, s);
+  return hex_apply<T>(d, fac, x, y, h->has_mass ? 1.0 : 0.0, 1.0, true, S, partials, s, y_zero_free);
 }
 template struct OpJ<double>;
 template struct OpJ<float>;
