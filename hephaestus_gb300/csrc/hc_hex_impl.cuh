@@ -73,8 +73,9 @@ __device__ __forceinline__ T dm(int a, int j) {
   return TabSel<T>::get(P).D[a][j];
 }
 
-// out(n0,n1,n2) += s * (A (x) B (x) Cz) in(m0,m1,m2), index i + n0 (j + n1 k)
-template <typename T, int P, int RX, int CX, int RY, int CY, int RZ, int CZ>
+// out(n0,n1,n2) (+)= s * (A (x) B (x) Cz) in(m0,m1,m2), index i + n0 (j + n1 k);
+// ACC = false assigns (first contribution), avoiding additions of zero.
+template <typename T, int P, int RX, int CX, int RY, int CY, int RZ, int CZ, bool ACC = true>
 __device__ __forceinline__ void kron3_acc(const T* in, T* out, T s) {
   constexpr int m0 = nb<P>(CX), m1n = nb<P>(CY), m2 = nb<P>(CZ);
   constexpr int n0 = nb<P>(RX), n1 = nb<P>(RY), n2 = nb<P>(RZ);
@@ -85,9 +86,9 @@ __device__ __forceinline__ void kron3_acc(const T* in, T* out, T s) {
     for (int j0 = 0; j0 < m1n; ++j0)
 #pragma unroll
       for (int i0 = 0; i0 < m0; ++i0) {
-        T acc = T(0);
+        T acc = m1<T, P, RZ, CZ>(k, 0) * in[i0 + m0 * j0];
 #pragma unroll
-        for (int k0 = 0; k0 < m2; ++k0) acc += m1<T, P, RZ, CZ>(k, k0) * in[i0 + m0 * (j0 + m1n * k0)];
+        for (int k0 = 1; k0 < m2; ++k0) acc += m1<T, P, RZ, CZ>(k, k0) * in[i0 + m0 * (j0 + m1n * k0)];
         t1[i0 + m0 * (j0 + m1n * k)] = acc;
       }
   T t2[m0 * n1 * n2];
@@ -97,9 +98,9 @@ __device__ __forceinline__ void kron3_acc(const T* in, T* out, T s) {
     for (int j = 0; j < n1; ++j)
 #pragma unroll
       for (int i0 = 0; i0 < m0; ++i0) {
-        T acc = T(0);
+        T acc = m1<T, P, RY, CY>(j, 0) * t1[i0 + m0 * (m1n * k)];
 #pragma unroll
-        for (int j0 = 0; j0 < m1n; ++j0) acc += m1<T, P, RY, CY>(j, j0) * t1[i0 + m0 * (j0 + m1n * k)];
+        for (int j0 = 1; j0 < m1n; ++j0) acc += m1<T, P, RY, CY>(j, j0) * t1[i0 + m0 * (j0 + m1n * k)];
         t2[i0 + m0 * (j + n1 * k)] = acc;
       }
 #pragma unroll
@@ -108,10 +109,11 @@ __device__ __forceinline__ void kron3_acc(const T* in, T* out, T s) {
     for (int j = 0; j < n1; ++j)
 #pragma unroll
       for (int i = 0; i < n0; ++i) {
-        T acc = T(0);
+        T acc = m1<T, P, RX, CX>(i, 0) * t2[m0 * (j + n1 * k)];
 #pragma unroll
-        for (int i0 = 0; i0 < m0; ++i0) acc += m1<T, P, RX, CX>(i, i0) * t2[i0 + m0 * (j + n1 * k)];
-        out[i + n0 * (j + n1 * k)] += s * acc;
+        for (int i0 = 1; i0 < m0; ++i0) acc += m1<T, P, RX, CX>(i, i0) * t2[i0 + m0 * (j + n1 * k)];
+        if constexpr (ACC) out[i + n0 * (j + n1 * k)] += s * acc;
+        else out[i + n0 * (j + n1 * k)] = s * acc;
       }
 }
 
@@ -126,14 +128,14 @@ struct RtT {
   static constexpr int v = (c == d) ? kC : kO;
 };
 
-template <typename T, int P, int c, int b>
+template <typename T, int P, int c, int b, bool ACC = true>
 __device__ __forceinline__ void mass_block(const T* u, T* y, T s) {
-  kron3_acc<T, P, NdT<c, 0>::v, NdT<b, 0>::v, NdT<c, 1>::v, NdT<b, 1>::v, NdT<c, 2>::v, NdT<b, 2>::v>(
+  kron3_acc<T, P, NdT<c, 0>::v, NdT<b, 0>::v, NdT<c, 1>::v, NdT<b, 1>::v, NdT<c, 2>::v, NdT<b, 2>::v, ACC>(
       u, y, s);
 }
-template <typename T, int P, int c, int b>
+template <typename T, int P, int c, int b, bool ACC = true>
 __device__ __forceinline__ void rt_block(const T* u, T* y, T s) {
-  kron3_acc<T, P, RtT<c, 0>::v, RtT<b, 0>::v, RtT<c, 1>::v, RtT<b, 1>::v, RtT<c, 2>::v, RtT<b, 2>::v>(
+  kron3_acc<T, P, RtT<c, 0>::v, RtT<b, 0>::v, RtT<c, 1>::v, RtT<b, 1>::v, RtT<c, 2>::v, RtT<b, 2>::v, ACC>(
       u, y, s);
 }
 
@@ -149,9 +151,9 @@ __device__ __forceinline__ void curl_nd(const T* u0, const T* u1, const T* u2, T
     for (int j = 0; j < O; ++j)
 #pragma unroll
       for (int i = 0; i < C; ++i) {
-        T acc = T(0);
+        T acc = dm<T, P>(j, 0) * u2[i + C * (C * k)];
 #pragma unroll
-        for (int q = 0; q < C; ++q) acc += dm<T, P>(j, q) * u2[i + C * (q + C * k)];
+        for (int q = 1; q < C; ++q) acc += dm<T, P>(j, q) * u2[i + C * (q + C * k)];
 #pragma unroll
         for (int q = 0; q < C; ++q) acc -= dm<T, P>(k, q) * u1[i + C * (j + O * q)];
         r0[i + C * (j + O * k)] = acc;
@@ -163,9 +165,9 @@ __device__ __forceinline__ void curl_nd(const T* u0, const T* u1, const T* u2, T
     for (int j = 0; j < C; ++j)
 #pragma unroll
       for (int i = 0; i < O; ++i) {
-        T acc = T(0);
+        T acc = dm<T, P>(k, 0) * u0[i + O * j];
 #pragma unroll
-        for (int q = 0; q < C; ++q) acc += dm<T, P>(k, q) * u0[i + O * (j + C * q)];
+        for (int q = 1; q < C; ++q) acc += dm<T, P>(k, q) * u0[i + O * (j + C * q)];
 #pragma unroll
         for (int q = 0; q < C; ++q) acc -= dm<T, P>(i, q) * u2[q + C * (j + C * k)];
         r1[i + O * (j + C * k)] = acc;
@@ -177,9 +179,9 @@ __device__ __forceinline__ void curl_nd(const T* u0, const T* u1, const T* u2, T
     for (int j = 0; j < O; ++j)
 #pragma unroll
       for (int i = 0; i < O; ++i) {
-        T acc = T(0);
+        T acc = dm<T, P>(i, 0) * u1[C * (j + O * k)];
 #pragma unroll
-        for (int q = 0; q < C; ++q) acc += dm<T, P>(i, q) * u1[q + C * (j + O * k)];
+        for (int q = 1; q < C; ++q) acc += dm<T, P>(i, q) * u1[q + C * (j + O * k)];
 #pragma unroll
         for (int q = 0; q < C; ++q) acc -= dm<T, P>(j, q) * u0[i + O * (q + C * k)];
         r2[i + O * (j + O * k)] = acc;
@@ -198,9 +200,9 @@ __device__ __forceinline__ void curl_nd_t(const T* g0, const T* g1, const T* g2,
     for (int j = 0; j < C; ++j)
 #pragma unroll
       for (int i = 0; i < O; ++i) {
-        T acc = T(0);
+        T acc = dm<T, P>(0, k) * g1[i + O * j];
 #pragma unroll
-        for (int q = 0; q < O; ++q) acc += dm<T, P>(q, k) * g1[i + O * (j + C * q)];
+        for (int q = 1; q < O; ++q) acc += dm<T, P>(q, k) * g1[i + O * (j + C * q)];
 #pragma unroll
         for (int q = 0; q < O; ++q) acc -= dm<T, P>(q, j) * g2[i + O * (q + O * k)];
         y0[i + O * (j + C * k)] += acc;
@@ -212,9 +214,9 @@ __device__ __forceinline__ void curl_nd_t(const T* g0, const T* g1, const T* g2,
     for (int j = 0; j < O; ++j)
 #pragma unroll
       for (int i = 0; i < C; ++i) {
-        T acc = T(0);
+        T acc = dm<T, P>(0, i) * g2[O * (j + O * k)];
 #pragma unroll
-        for (int q = 0; q < O; ++q) acc += dm<T, P>(q, i) * g2[q + O * (j + O * k)];
+        for (int q = 1; q < O; ++q) acc += dm<T, P>(q, i) * g2[q + O * (j + O * k)];
 #pragma unroll
         for (int q = 0; q < O; ++q) acc -= dm<T, P>(q, k) * g0[i + C * (j + O * q)];
         y1[i + C * (j + O * k)] += acc;
@@ -226,9 +228,9 @@ __device__ __forceinline__ void curl_nd_t(const T* g0, const T* g1, const T* g2,
     for (int j = 0; j < C; ++j)
 #pragma unroll
       for (int i = 0; i < C; ++i) {
-        T acc = T(0);
+        T acc = dm<T, P>(0, j) * g0[i + C * (O * k)];
 #pragma unroll
-        for (int q = 0; q < O; ++q) acc += dm<T, P>(q, j) * g0[i + C * (q + O * k)];
+        for (int q = 1; q < O; ++q) acc += dm<T, P>(q, j) * g0[i + C * (q + O * k)];
 #pragma unroll
         for (int q = 0; q < O; ++q) acc -= dm<T, P>(q, i) * g1[q + O * (j + C * k)];
         y2[i + C * (j + C * k)] += acc;
@@ -525,17 +527,35 @@ __device__ __forceinline__ BrickGeom brick_of(const HexDev& d, int b) {
 template <typename T, int P, int BX, int BY, int BZ, int comp>
 __device__ __forceinline__ void prefetch_comp(const HexDev& d, const T* __restrict__ x, T* sx, BrickGeom bg) {
   using TL = BrickTile<P, BX, BY, BZ>;
-  constexpr int TX = TL::tx(comp), TY = TL::ty(comp), NC = TL::n(comp), OFF = TL::off(comp);
+  constexpr int TX = TL::tx(comp), TY = TL::ty(comp), TZ = TL::tz(comp), NC = TL::n(comp), OFF = TL::off(comp);
   const int gdx = d.nx * P + (comp != 0), gdy = d.ny * P + (comp != 1), gdz = d.nz * P + (comp != 2);
   const int base = (int)d.off[comp] + bg.X0 * P + gdx * (bg.Y0 * P + gdy * (bg.Z0 * P));
   const bool full = bg.X0 + BX <= d.nx && bg.Y0 + BY <= d.ny && bg.Z0 + BZ <= d.nz;
   if (full) {
-    // precomputed relative offsets: one load and one add per entry
-#pragma unroll 4
-    for (int r = threadIdx.x; r < NC; r += BX * BY * BZ) {
-      const int t = __ldg(d.tab + OFF + r) & 0x7fffffff;
-      if constexpr (sizeof(T) == 4) cp_async4(sx + OFF + r, x + base + t, 4);
-      else cp_async8(sx + OFF + r, x + base + t, 8);
+    // rows of the tile along x: one warp per row, lane = x index; the
+    // (TX - 32) trailing entries of each row are spread one row per thread.
+    constexpr int NW = BX * BY * BZ / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int tx0 = lane < TX ? lane : 0;
+#pragma unroll 2
+    for (int row = warp; row < TY * TZ; row += NW) {
+      const int tj = row % TY, tk = row / TY;
+      const int g = base + gdx * (tj + gdy * tk);
+      if (lane < TX) {
+        if constexpr (sizeof(T) == 4) cp_async4(sx + OFF + TX * row + tx0, x + g + tx0, 4);
+        else cp_async8(sx + OFF + TX * row + tx0, x + g + tx0, 8);
+      }
+    }
+    if constexpr (TX > 32) {
+      for (int row = threadIdx.x; row < TY * TZ; row += BX * BY * BZ) {
+        const int tj = row % TY, tk = row / TY;
+        const int g = base + gdx * (tj + gdy * tk);
+#pragma unroll
+        for (int ti = 32; ti < TX; ++ti) {
+          if constexpr (sizeof(T) == 4) cp_async4(sx + OFF + TX * row + ti, x + g + ti, 4);
+          else cp_async8(sx + OFF + TX * row + ti, x + g + ti, 8);
+        }
+      }
     }
     return;
   }
@@ -628,14 +648,33 @@ __device__ __forceinline__ void flush_comp(const HexDev& d, T* __restrict__ y, T
   const int gdx = d.nx * P + (comp != 0), gdy = d.ny * P + (comp != 1), gdz = d.nz * P + (comp != 2);
   const int base = (int)d.off[comp] + bg.X0 * P + gdx * (bg.Y0 * P + gdy * (bg.Z0 * P));
   if (fast) {
-#pragma unroll 4
-    for (int r = threadIdx.x; r < NC; r += BX * BY * BZ) {
-      const int t = __ldg(d.tab + OFF + r);
-      const T v = sy[OFF + r];
-      sy[OFF + r] = T(0);
-      T* dst = y + base + (t & 0x7fffffff);
-      if (OVERWRITE && t >= 0) *dst = v;
-      else atomicAdd(dst, v);
+    constexpr int NW = BX * BY * BZ / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll 2
+    for (int row = warp; row < TY * TZ; row += NW) {
+      const int tj = row % TY, tk = row / TY;
+      const bool rowface = (comp != 1 && (tj == 0 || tj == TY - 1)) || (comp != 2 && (tk == 0 || tk == TZ - 1));
+      if (lane < TX) {
+        T* src = sy + OFF + TX * row + lane;
+        const T v = *src;
+        *src = T(0);
+        T* dst = y + base + gdx * (tj + gdy * tk) + lane;
+        const bool face = rowface || (comp != 0 && (lane == 0 || lane == TX - 1));
+        if (OVERWRITE && !face) *dst = v;
+        else atomicAdd(dst, v);
+      }
+    }
+    if constexpr (TX > 32) {
+      for (int row = threadIdx.x; row < TY * TZ; row += BX * BY * BZ) {
+        const int tj = row % TY, tk = row / TY;
+#pragma unroll
+        for (int ti = 32; ti < TX; ++ti) {
+          T* src = sy + OFF + TX * row + ti;
+          const T v = *src;
+          *src = T(0);
+          atomicAdd(y + base + gdx * (tj + gdy * tk) + ti, v);  // last x plane: always a face
+        }
+      }
     }
     return;
   }
@@ -662,9 +701,12 @@ __global__ void __launch_bounds__(BX* BY* BZ, sizeof(T) == 4 ? 3 : 2)
                     T cscale, int masked, KrylovScalars* S, double* partials, int nbricks) {
   if (S && S->done) return;
   using TL = BrickTile<P, BX, BY, BZ>;
+  constexpr int NT = BX * BY * BZ;
+  constexpr int NF = FULL ? 12 : 6;  // factors staged per element
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sxb[2] = {reinterpret_cast<T*>(smem_raw), reinterpret_cast<T*>(smem_raw) + TL::total};
   T* sy = reinterpret_cast<T*>(smem_raw) + 2 * TL::total;
+  T* sfb[2] = {sy + TL::total, sy + TL::total + NF * NT};
   const bool mk = masked != 0;
   const bool mask_needed = mk && (d.ess != nullptr || d.ess_bits != 0);
   constexpr int C = P + 1, O = P;
@@ -674,11 +716,24 @@ __global__ void __launch_bounds__(BX* BY* BZ, sizeof(T) == 4 ? 3 : 2)
   for (int r = threadIdx.x; r < TL::total; r += BX * BY * BZ) sy[r] = T(0);
   double en = 0.0;
   int b = blockIdx.x;
+  // each thread stages its own element's factors (SoA rows are coalesced)
+  auto prefetch_fac = [&](BrickGeom g, T* sf) {
+    const int ex = g.X0 + lx, ey = g.Y0 + ly, ez = g.Z0 + lz;
+    const bool in = ex < d.nx && ey < d.ny && ez < d.nz;
+    const int64_t e = in ? ex + (int64_t)d.nx * (ey + (int64_t)d.ny * ez) : 0;
+#pragma unroll
+    for (int q = 0; q < NF; ++q) {
+      const int k = FULL ? q : (q < 3 ? (q == 0 ? 0 : (q == 1 ? 3 : 5)) : (q == 3 ? 6 : (q == 4 ? 9 : 11)));
+      if constexpr (sizeof(T) == 4) cp_async4(sf + q * NT + threadIdx.x, fac + (int64_t)k * d.ne + e, in ? 4 : 0);
+      else cp_async8(sf + q * NT + threadIdx.x, fac + (int64_t)k * d.ne + e, in ? 8 : 0);
+    }
+  };
   if (b < nbricks) {
     const BrickGeom g0 = brick_of<BX, BY, BZ>(d, b);
     prefetch_comp<T, P, BX, BY, BZ, 0>(d, x, sxb[0], g0);
     prefetch_comp<T, P, BX, BY, BZ, 1>(d, x, sxb[0], g0);
     prefetch_comp<T, P, BX, BY, BZ, 2>(d, x, sxb[0], g0);
+    prefetch_fac(g0, sfb[0]);
   }
   cp_async_commit();
   for (int it = 0; b < nbricks; b += gridDim.x, ++it) {
@@ -691,6 +746,7 @@ __global__ void __launch_bounds__(BX* BY* BZ, sizeof(T) == 4 ? 3 : 2)
       prefetch_comp<T, P, BX, BY, BZ, 0>(d, x, sn, gn);
       prefetch_comp<T, P, BX, BY, BZ, 1>(d, x, sn, gn);
       prefetch_comp<T, P, BX, BY, BZ, 2>(d, x, sn, gn);
+      prefetch_fac(gn, sfb[(it + 1) & 1]);
     }
     cp_async_commit();
     cp_async_wait<1>();  // this brick's group has landed
@@ -711,7 +767,7 @@ __global__ void __launch_bounds__(BX* BY* BZ, sizeof(T) == 4 ? 3 : 2)
     }
     const int ex = bg.X0 + lx, ey = bg.Y0 + ly, ez = bg.Z0 + lz;
     if (ex < d.nx && ey < d.ny && ez < d.nz) {
-      const int e = ex + d.nx * (ey + d.ny * ez);
+      const T* sf = sfb[it & 1];
       T u0[NDC], u1[NDC], u2[NDC];
       sgather<T, P, BX, BY, BZ, 0>(sx, lx, ly, lz, u0);
       sgather<T, P, BX, BY, BZ, 1>(sx, lx, ly, lz, u1);
@@ -720,26 +776,27 @@ __global__ void __launch_bounds__(BX* BY* BZ, sizeof(T) == 4 ? 3 : 2)
       if constexpr (FULL) {
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
-          fm[k] = mscale * __ldg(fac + (int64_t)k * d.ne + e);
-          fc[k] = cscale * __ldg(fac + (int64_t)(6 + k) * d.ne + e);
+          fm[k] = mscale * sf[k * NT + threadIdx.x];
+          fc[k] = cscale * sf[(6 + k) * NT + threadIdx.x];
         }
       } else {
         constexpr int kd[3] = {0, 3, 5};
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
-          fm[kd[q]] = mscale * __ldg(fac + (int64_t)kd[q] * d.ne + e);
-          fc[kd[q]] = cscale * __ldg(fac + (int64_t)(6 + kd[q]) * d.ne + e);
+          fm[kd[q]] = mscale * sf[q * NT + threadIdx.x];
+          fc[kd[q]] = cscale * sf[(3 + q) * NT + threadIdx.x];
         }
       }
       T r0[RTC], r1[RTC], r2[RTC];
       curl_nd<T, P>(u0, u1, u2, r0, r1, r2);
       T y0[NDC], y1[NDC], y2[NDC];
+      if (mscale == T(0)) {
 #pragma unroll
-      for (int i = 0; i < NDC; ++i) y0[i] = y1[i] = y2[i] = T(0);
-      if (mscale != T(0)) {
-        mass_block<T, P, 0, 0>(u0, y0, fm[0]);
-        mass_block<T, P, 1, 1>(u1, y1, fm[3]);
-        mass_block<T, P, 2, 2>(u2, y2, fm[5]);
+        for (int i = 0; i < NDC; ++i) y0[i] = y1[i] = y2[i] = T(0);
+      } else {
+        mass_block<T, P, 0, 0, false>(u0, y0, fm[0]);
+        mass_block<T, P, 1, 1, false>(u1, y1, fm[3]);
+        mass_block<T, P, 2, 2, false>(u2, y2, fm[5]);
         if constexpr (FULL) {
           mass_block<T, P, 0, 1>(u1, y0, fm[1]);
           mass_block<T, P, 0, 2>(u2, y0, fm[2]);
@@ -755,11 +812,9 @@ __global__ void __launch_bounds__(BX* BY* BZ, sizeof(T) == 4 ? 3 : 2)
         for (int i = 0; i < NDC; ++i) eacc += u0[i] * y0[i] + u1[i] * y1[i] + u2[i] * y2[i];
       }
       T g0[RTC], g1[RTC], g2[RTC];
-#pragma unroll
-      for (int i = 0; i < RTC; ++i) g0[i] = g1[i] = g2[i] = T(0);
-      rt_block<T, P, 0, 0>(r0, g0, fc[0]);
-      rt_block<T, P, 1, 1>(r1, g1, fc[3]);
-      rt_block<T, P, 2, 2>(r2, g2, fc[5]);
+      rt_block<T, P, 0, 0, false>(r0, g0, fc[0]);
+      rt_block<T, P, 1, 1, false>(r1, g1, fc[3]);
+      rt_block<T, P, 2, 2, false>(r2, g2, fc[5]);
       if constexpr (FULL) {
         rt_block<T, P, 0, 1>(r1, g0, fc[1]);
         rt_block<T, P, 0, 2>(r2, g0, fc[2]);
@@ -854,7 +909,8 @@ cudaError_t hex_launch_p(const HexDev& d, const T* fac, const T* x, T* y, T ms, 
   if constexpr (P <= 2) {
     using B = BrickShape<P>;
     using TL = BrickTile<P, B::BX, B::BY, B::BZ>;
-    const size_t sm = 3 * TL::total * sizeof(T);
+    constexpr int nthr = B::BX * B::BY * B::BZ;
+    const size_t sm = (3 * TL::total + 2 * (d.full ? 12 : 6) * nthr) * sizeof(T);
     const int nbricks = brick_blocks<P>(d);
     constexpr int nt = B::BX * B::BY * B::BZ;
     static int per_sm[2][2][2] = {{{0, 0}, {0, 0}}, {{0, 0}, {0, 0}}};
