@@ -78,6 +78,10 @@ class SolveInfo(C.Structure):
     ]
 
 
+class Coil(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("I0", "xc", "yc", "r0", "r1", "z0", "z1")]
+
+
 _lib = None
 
 _SIGS = {
@@ -102,6 +106,12 @@ _SIGS = {
     "hc_solve_device": (C.c_int, [C.c_void_p, C.POINTER(SolveParams), C.c_void_p, C.c_void_p,
                                   C.POINTER(SolveInfo)]),
     "hc_lanczos_lmax": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
+    "hc_num_rt_dofs": (C.c_int64, [C.c_void_p]),
+    "hc_hex_rt_dof_index": (C.c_int64, [C.c_void_p, C.c_int, C.c_int64, C.c_int64, C.c_int64]),
+    "hc_curl": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hc_curl_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hc_load_coil": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    "hc_load_coil_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
 }
 
 

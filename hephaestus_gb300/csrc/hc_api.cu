@@ -181,6 +181,7 @@ void hc_destroy(hcop_t* h) {
   cudaFree(h->work);
   cudaFree(h->xbuf);
   cudaFree(h->ybuf);
+  cudaFree(h->verts);
   cudaFree(h->tab);
   delete h;
 }
@@ -348,6 +349,9 @@ hc_status hc_create(const hc_problem_desc* desc, hcop_t** out) {
       return fail_create(h, "hc_create: device allocation failed", HC_ENOMEM);
     cudaMemcpy(h->tab, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice);
   }
+  if (cudaMalloc((void**)&h->verts, nv * 3 * sizeof(double)) != cudaSuccess)
+    return fail_create(h, "hc_create: device allocation failed", HC_ENOMEM);
+  cudaMemcpy(h->verts, V, nv * 3 * sizeof(double), cudaMemcpyHostToDevice);
   cudaMemcpy(h->fac, fac.data(), fac.size() * 8, cudaMemcpyHostToDevice);
   cudaMemcpy(h->facf, facf.data(), facf.size() * 4, cudaMemcpyHostToDevice);
   cudaMemcpy(h->ess, h->ess_host.data(), N, cudaMemcpyHostToDevice);
@@ -448,6 +452,73 @@ hc_status hc_add_weak_curlcurl(hcop_t* h, const double* x, double* y, double sca
 hc_status hc_diag(hcop_t* h, double* d) {
   if (!h || !d) return HC_EINVAL;
   return d2h_sync(h, d, h->diag);
+}
+
+// ---- curl, load vector ------------------------------------------------------------
+int64_t hc_num_rt_dofs(const hcop_t* h) {
+  if (!h) return -1;
+  int64_t o1, o2, n;
+  hex_rt_layout(h->hexdev(), &o1, &o2, &n);
+  return n;
+}
+
+int64_t hc_hex_rt_dof_index(const hcop_t* h, int c, int64_t i, int64_t j, int64_t k) {
+  if (!h || c < 0 || c > 2) return -1;
+  const int64_t mx = (int64_t)h->nx * h->p, my = (int64_t)h->ny * h->p, mz = (int64_t)h->nz * h->p;
+  const int64_t n0 = mx + (c == 0), n1 = my + (c == 1), n2 = mz + (c == 2);
+  if (i < 0 || j < 0 || k < 0 || i >= n0 || j >= n1 || k >= n2) return -1;
+  int64_t o1, o2, n;
+  hex_rt_layout(h->hexdev(), &o1, &o2, &n);
+  const int64_t off = c == 0 ? 0 : (c == 1 ? o1 : o2);
+  return off + i + n0 * (j + n1 * k);
+}
+
+hc_status hc_curl_device(hcop_t* h, const double* A, double* B) {
+  if (!h || !A || !B) return HC_EINVAL;
+  HC_CUDA_TRY(h, hex_curl(h->hexdev(), A, B, h->stream));
+  return HC_OK;
+}
+
+hc_status hc_curl(hcop_t* h, const double* A, double* B) {
+  if (!h || !A || !B) return HC_EINVAL;
+  const int64_t nrt = hc_num_rt_dofs(h);
+  double* dB = nullptr;
+  HC_CUDA_TRY(h, cudaMallocAsync((void**)&dB, nrt * sizeof(double), h->stream));
+  hc_status st = h2d(h, h->xbuf, A);
+  if (st == HC_OK) st = hc_curl_device(h, h->xbuf, dB);
+  if (st == HC_OK) {
+    cudaMemcpyAsync(B, dB, nrt * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) st = HC_ECUDA;
+  }
+  cudaFreeAsync(dB, h->stream);
+  return st;
+}
+
+hc_status hc_load_coil_device(hcop_t* h, const hc_coil* coil, int q, double* b) {
+  if (!h || !coil || !b || q < 1 || q > 8) {
+    if (h) h->err = "hc_load_coil: need a coil and 1 <= q <= 8";
+    return HC_EINVAL;
+  }
+  std::vector<double> xq(q), wq(q), bc(q * (h->p + 1)), bo(q * h->p);
+  gl01(q, xq.data(), wq.data());
+  double xc[kMaxP + 1], xo[kMaxP], wo[kMaxP], d1[kMaxP + 1];
+  gll01(h->p + 1, xc);
+  gl01(h->p, xo, wo);
+  for (int k = 0; k < q; ++k) {
+    lagrange(xc, h->p + 1, xq[k], &bc[k * (h->p + 1)], d1);
+    lagrange(xo, h->p, xq[k], &bo[k * h->p], d1);
+  }
+  const double cv[7] = {coil->I0, coil->xc, coil->yc, coil->r0, coil->r1, coil->z0, coil->z1};
+  HC_CUDA_TRY(h, hex_load_coil(h->hexdev(), h->verts, cv, q, xq.data(), wq.data(), bc.data(), bo.data(), b,
+                               h->stream));
+  return HC_OK;
+}
+
+hc_status hc_load_coil(hcop_t* h, const hc_coil* coil, int q, double* b) {
+  if (!h || !b) return HC_EINVAL;
+  hc_status st = hc_load_coil_device(h, coil, q, h->ybuf);
+  if (st != HC_OK) return st;
+  return d2h_sync(h, b, h->ybuf);
 }
 
 // ---- solves ---------------------------------------------------------------------

@@ -10,6 +10,7 @@ namespace hc {
 cudaError_t upload_tables_p1(const void* td, const void* tf);
 cudaError_t upload_tables_p2(const void* td, const void* tf);
 cudaError_t upload_tables_p3(const void* td, const void* tf);
+cudaError_t upload_tables_post(const void* td, const void* tf);
 
 // upper bound on the blocks of any apply launch (sizes the reduction partials)
 int hex_apply_blocks(const HexDev& d) {
@@ -180,6 +181,7 @@ cudaError_t upload_tables() {
   if (e == cudaSuccess) e = upload_tables_p1(td, tf);
   if (e == cudaSuccess) e = upload_tables_p2(td, tf);
   if (e == cudaSuccess) e = upload_tables_p3(td, tf);
+  if (e == cudaSuccess) e = upload_tables_post(td, tf);
   return e;
 }
 

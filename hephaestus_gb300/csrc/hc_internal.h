@@ -95,6 +95,7 @@ struct hcop {
   double* xbuf = nullptr;              // device staging for host-pointer calls
   double* ybuf = nullptr;
   double lmax64 = 0.0, lmax32 = 0.0;   // cached Chebyshev bounds
+  double* verts = nullptr;             // device vertex coordinates (hex grid)
   int* tab = nullptr;                  // brick tile table of the apply kernel
 
   hc::HexDev hexdev() const {
@@ -133,6 +134,12 @@ cudaError_t hex_apply(const HexDev& d, const T* fac, const T* x, T* y, double ms
 cudaError_t hex_diag(const HexDev& d, double* diag, cudaStream_t s);
 // tile table of the brick kernel for order p on an nx x ny grid (host)
 void hex_tile_table(int p, int nx, int ny, std::vector<int>& tab);
+
+// ---- hc_post.cu ----
+void hex_rt_layout(const HexDev& d, int64_t* off1, int64_t* off2, int64_t* n);
+cudaError_t hex_curl(const HexDev& d, const double* A, double* B, cudaStream_t s);
+cudaError_t hex_load_coil(const HexDev& d, const double* V, const double coil[7], int q, const double* xq,
+                          const double* wq, const double* bc, const double* bo, double* b, cudaStream_t s);
 
 // ---- hc_krylov.cu ----
 cudaError_t diag_finish(int64_t n, const uint8_t* ess, double* d, double* dinv, float* dinvf, double* sd,

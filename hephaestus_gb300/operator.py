@@ -223,6 +223,30 @@ class HCurlOperator:
         N.check(N.lib().hc_apply_form_device(self.h, _dev_ptr(x, "float64"), _dev_ptr(y, "float64")), self.h)
         return y
 
+    # -- around the solve --
+    def Curl(self, A):
+        """B = curl A as Raviart-Thomas dofs (CurlAuxSolver)."""
+        A = self._h(A)
+        B = np.empty(N.lib().hc_num_rt_dofs(self.h))
+        N.check(N.lib().hc_curl(self.h, _ptr(A), _ptr(B)), self.h)
+        return B
+
+    def rt_dof_index(self, c, i, j, k):
+        return N.lib().hc_hex_rt_dof_index(self.h, c, i, j, k)
+
+    def LoadCoil(self, I0=1.0, xc=0.5, yc=0.5, r0=0.2, r1=0.35, z0=0.3, z1=0.7, q=None):
+        """b_i = (J, w_i) of the loop coil (DivFreeSource's right-hand side)."""
+        coil = N.Coil(I0, xc, yc, r0, r1, z0, z1)
+        b = np.empty(self.ndof)
+        N.check(N.lib().hc_load_coil(self.h, C.byref(coil), int(q or self.order + 2), _ptr(b)), self.h)
+        return b
+
+    def LoadCoilDevice(self, b, I0=1.0, xc=0.5, yc=0.5, r0=0.2, r1=0.35, z0=0.3, z1=0.7, q=None):
+        coil = N.Coil(I0, xc, yc, r0, r1, z0, z1)
+        N.check(N.lib().hc_load_coil_device(self.h, C.byref(coil), int(q or self.order + 2),
+                                            _dev_ptr(b, "float64")), self.h)
+        return b
+
     def LanczosLmax(self, steps=20):
         v = C.c_double(0)
         N.check(N.lib().hc_lanczos_lmax(self.h, steps, C.byref(v)), self.h)

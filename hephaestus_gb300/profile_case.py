@@ -1,0 +1,43 @@
+"""Small, self-contained operator-apply case for profiling (ncu) runs.
+
+    python -m hephaestus_gb300.profile_case N P [mult|add|fp64]
+
+Builds an N^3-hex, order-P operator with nu = 10^U(0,3), sigma = 10^U(-2,6),
+dt = 0.01 (the benchmark's coefficient distributions) and applies it:
+  mult  - y = J x in FP32 (masked init + apply), 5 times
+  add   - y += P K P x in FP32 (the accumulate-form apply kernel alone), 5 times
+  fp64  - y = J x in FP64, 3 times
+"""
+import sys
+
+import numpy as np
+
+
+def main(argv):
+    import torch
+
+    from hephaestus_gb300 import HCurlOperator, meshes
+
+    n = int(argv[0]) if argv else 96
+    p = int(argv[1]) if len(argv) > 1 else 2
+    mode = argv[2] if len(argv) > 2 else "mult"
+    rng = np.random.default_rng(0)
+    nu = meshes.loguniform(n ** 3, 1, 1e3, rng)
+    sg = meshes.loguniform(n ** 3, 1e-2, 1e6, rng)
+    op = HCurlOperator(n, n, n, p, nu, sg, dt=0.01)
+    if mode == "fp64":
+        x = torch.randn(op.ndof, device="cuda", dtype=torch.float64)
+        y = torch.empty_like(x)
+        for _ in range(3):
+            op.MultDevice(x, y)
+    else:
+        x = torch.randn(op.ndof, device="cuda")
+        y = torch.zeros_like(x)
+        for _ in range(5):
+            (op.AddMultDevice if mode == "add" else op.MultDevice)(x, y)
+    torch.cuda.synchronize()
+    print("ok", mode, op.ndof)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

@@ -155,6 +155,27 @@ hc_status hc_apply_form_device(hcop_t* h, const double* x, double* y);
 hc_status hc_add_mult_device(hcop_t* h, const double* x, double* y);
 hc_status hc_add_mult_device_f32(hcop_t* h, const float* x, float* y);
 
+/* ---- around the solve ---------------------------------------------------- */
+/* B = curl A into the Raviart-Thomas space of the grid (CurlAuxSolver with
+ * MFEM's CurlInterpolator, src/auxsolvers/curl_aux.cpp:13-30).  Component c
+ * is closed (Gauss-Lobatto nodal) in direction c and open (Gauss-Legendre
+ * nodal) in the other two; layout as hc_hex_rt_dof_index.  B is the
+ * reference-element flux: B_phys = J B_ref / det J at a point.             */
+int64_t hc_num_rt_dofs(const hcop_t* h);
+int64_t hc_hex_rt_dof_index(const hcop_t* h, int c, int64_t i, int64_t j, int64_t k);
+hc_status hc_curl(hcop_t* h, const double* A, double* B);
+hc_status hc_curl_device(hcop_t* h, const double* A, double* B);
+
+/* Loop coil J = I0 (-(y-yc), x-xc, 0) for r0 <= r <= r1, z0 <= z <= z1 (r about
+ * (xc, yc)), else 0.  b_i = (J, w_i) with a q^3 Gauss-Legendre rule per hex
+ * (1 <= q <= 8): the right-hand side DivFreeSource adds
+ * (src/sources/div_free_source.cpp:72-114).                                  */
+typedef struct {
+  double I0, xc, yc, r0, r1, z0, z1;
+} hc_coil;
+hc_status hc_load_coil(hcop_t* h, const hc_coil* coil, int q, double* b);
+hc_status hc_load_coil_device(hcop_t* h, const hc_coil* coil, int q, double* b);
+
 /* ---- linear solve --------------------------------------------------------- */
 /* Solve J x = b for x (x holds the initial guess on entry).  Replaces the
  * HyprePCG solve of HCurlFormulation::ConstructJacobianSolver

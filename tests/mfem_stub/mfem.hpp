@@ -1,0 +1,48 @@
+// Minimal stand-in for the parts of mfem.hpp that include/hcurl_mfem.hpp uses,
+// so that the shim can be type-checked where MFEM is not installed.
+#pragma once
+#include <cstdlib>
+#include <iostream>
+#include <vector>
+
+#define MFEM_ABORT(msg)                  \
+  do {                                   \
+    std::cerr << msg << std::endl;       \
+    std::abort();                        \
+  } while (0)
+
+namespace mfem {
+class Vector {
+public:
+  explicit Vector(int n = 0) : d_(n, 0.0) {}
+  int Size() const { return (int)d_.size(); }
+  const double* HostRead() const { return d_.data(); }
+  double* HostWrite() { return d_.data(); }
+  double* HostReadWrite() { return d_.data(); }
+  Vector& operator=(double v) {
+    for (auto& x : d_) x = v;
+    return *this;
+  }
+  double& operator()(int i) { return d_[i]; }
+
+private:
+  std::vector<double> d_;
+};
+class Operator {
+public:
+  virtual ~Operator() = default;
+  int Height() const { return height; }
+  int Width() const { return width; }
+  virtual void Mult(const Vector& x, Vector& y) const = 0;
+  virtual Operator& GetGradient(const Vector&) const { std::abort(); }
+  virtual void AssembleDiagonal(Vector&) const {}
+
+protected:
+  int height = 0, width = 0;
+};
+class Solver : public Operator {
+public:
+  bool iterative_mode = false;
+  virtual void SetOperator(const Operator& op) = 0;
+};
+}  // namespace mfem

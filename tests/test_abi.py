@@ -77,3 +77,30 @@ def test_tets_not_yet_supported_is_reported():
     d = _desc(elem_type=N.HC_TET, nu=nu.ctypes.data_as(C.c_void_p))
     h = C.c_void_p()
     assert N.lib().hc_create(C.byref(d), C.byref(h)) == N.HC_ENOTSUP
+
+
+def test_mfem_shim_compiles_against_stub():
+    """include/hcurl_mfem.hpp (the reference-side binding) type-checks and
+    links against the library."""
+    import os
+    import subprocess
+    import tempfile
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = os.path.join(tempfile.mkdtemp(), "shim.so")
+    cmd = ["g++", "-std=c++17", "-shared", "-fPIC", "-I", os.path.join(root, "include"),
+           "-I", os.path.join(root, "tests", "mfem_stub"), os.path.join(root, "tests", "mfem_shim_check.cpp"),
+           "-o", out, "-L", os.path.dirname(N.LIB_PATH), "-lhcurl_gb300"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def test_header_is_plain_c():
+    """The ABI header compiles as C (no C++ or torch types)."""
+    import os
+    import subprocess
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run(["gcc", "-std=c99", "-fsyntax-only", "-x", "c", os.path.join(root, "include", "hcurl_op.h")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr

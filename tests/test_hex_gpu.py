@@ -255,3 +255,44 @@ def test_apply_parity_explicit_mask(p):
     yr = ref.apply_masked(x)
     assert np.linalg.norm(op.Mult(x) - yr) / np.linalg.norm(yr) < TOL64
     del nd
+
+
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_curl_matches_oracle(p):
+    """B = curl A (CurlAuxSolver) against the oracle's curl at element centres."""
+    n = 3
+    v = _sheared(n)
+    op = HCurlOperator(n, n, n, p, np.ones(n ** 3), None, vertices=v, ess_attr_bits=0)
+    ref = oracle.Problem.hex(n, n, n, p, v)
+    rng = np.random.default_rng(11)
+    A = rng.standard_normal(op.ndof)
+    B = op.Curl(A)
+    assert B.shape == (3 * (n * p + 1) * (n * p) ** 2,)
+    for e in (0, 7, 13, 26):
+        xi = np.array([0.5, 0.3, 0.7])
+        _, cref = ref.eval(A, e, xi)
+        bref = hexref.rt_eval_ref(B, n, n, n, p, e, xi)
+        ex, ey, ez = e % n, (e // n) % n, e // (n * n)
+        vid = lambda i, j, k: i + (n + 1) * (j + (n + 1) * k)  # noqa: E731
+        v0 = v[vid(ex, ey, ez)]
+        J = np.stack([v[vid(ex + 1, ey, ez)] - v0, v[vid(ex, ey + 1, ez)] - v0, v[vid(ex, ey, ez + 1)] - v0], axis=1)
+        bphys = J @ bref / np.linalg.det(J)
+        assert np.allclose(bphys, cref, rtol=1e-11, atol=1e-11 * np.abs(cref).max())
+
+
+def test_curl_of_gradient_is_zero_rt():
+    n, p = 4, 2
+    op = HCurlOperator(n, n, n, p, np.ones(n ** 3), None, vertices=_sheared(n), ess_attr_bits=0)
+    phi = np.random.default_rng(12).standard_normal((n * p + 1,) * 3)
+    B = op.Curl(hexref.discrete_gradient(n, n, n, p, phi))
+    assert np.abs(B).max() < 1e-12 * np.abs(phi).max() * 10
+
+
+@pytest.mark.parametrize("p,q", [(1, 3), (2, 4), (3, 5)])
+def test_load_coil_matches_oracle(p, q):
+    n = 6
+    op = HCurlOperator(n, n, n, p, np.ones(n ** 3), np.ones(n ** 3), ess_attr_bits=0)
+    ref = oracle.Problem.hex(n, n, n, p)
+    b = op.LoadCoil(I0=1.5, xc=0.45, yc=0.55, q=q)
+    br = ref.load_coil(I0=1.5, xc=0.45, yc=0.55, q=q)
+    assert np.linalg.norm(b - br) / np.linalg.norm(br) < 1e-13
