@@ -106,6 +106,9 @@ _SIGS = {
     "hc_solve_device": (C.c_int, [C.c_void_p, C.POINTER(SolveParams), C.c_void_p, C.c_void_p,
                                   C.POINTER(SolveInfo)]),
     "hc_lanczos_lmax": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
+    "hc_mult_multi_device": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
+    "hc_elem_type": (C.c_int32, [C.c_void_p]),
+    "hc_tet_element_matrix": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
     "hc_num_rt_dofs": (C.c_int64, [C.c_void_p]),
     "hc_hex_rt_dof_index": (C.c_int64, [C.c_void_p, C.c_int, C.c_int64, C.c_int64, C.c_int64]),
     "hc_curl": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),

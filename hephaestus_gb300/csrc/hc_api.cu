@@ -133,6 +133,63 @@ static hc_status fail_create(hcop* h, const std::string& msg, hc_status st) {
   return st;
 }
 
+static bool alloc_common(hcop* h) {
+  const int64_t N = h->ndof;
+  auto ok = [](cudaError_t e) { return e == cudaSuccess; };
+  return ok(cudaMalloc((void**)&h->ess, N)) && ok(cudaMalloc((void**)&h->diag, N * 8)) &&
+         ok(cudaMalloc((void**)&h->dinv, N * 8)) && ok(cudaMalloc((void**)&h->dinvf, N * 4)) &&
+         ok(cudaMalloc((void**)&h->sdinv, N * 8)) && ok(cudaMalloc((void**)&h->sdinvf, N * 4)) &&
+         ok(cudaMalloc((void**)&h->xbuf, N * 8)) && ok(cudaMalloc((void**)&h->ybuf, N * 8));
+}
+
+// Tetrahedral mesh: host topology + closed-form FP64 element matrices on the device.
+static hc_status create_tet(const hc_problem_desc* desc, hcop_t** out) {
+  if (desc->order < 1 || desc->order > 2) return fail_create(nullptr, "hc_create: tet order must be 1 or 2", HC_EINVAL);
+  if (desc->n_vert < 4 || desc->n_elem < 1 || !desc->vertices || !desc->elem_verts)
+    return fail_create(nullptr, "hc_create: tet mesh needs vertices and elem_verts", HC_EINVAL);
+  if (!desc->nu) return fail_create(nullptr, "hc_create: nu is required", HC_EINVAL);
+  if (!(desc->dt > 0.0) || !std::isfinite(desc->dt))
+    return fail_create(nullptr, "hc_create: dt must be finite and > 0", HC_EINVAL);
+  if (!finite_nonneg(desc->nu, desc->n_elem))
+    return fail_create(nullptr, "hc_create: nu must be finite and >= 0", HC_EINVAL);
+  if (desc->sigma && !finite_nonneg(desc->sigma, desc->n_elem))
+    return fail_create(nullptr, "hc_create: sigma must be finite and >= 0", HC_EINVAL);
+  hcop* h = new hcop();
+  h->type = HC_TET;
+  h->p = desc->order;
+  h->ne = desc->n_elem;
+  h->dt = desc->dt;
+  h->has_mass = desc->sigma != nullptr;
+  std::vector<int32_t> edofs, sv;
+  hc_status st = tet_topology(h, desc, edofs, sv);
+  if (st != HC_OK) return fail_create(h, h->err, st);
+  const int L = h->p == 1 ? 6 : 20;
+  const int64_t N = h->ndof;
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return fail_create(h, "hc_create: no CUDA device available", HC_ECUDA);
+  const size_t need = (size_t)h->ne * L * L * 12 + (size_t)h->ne * L * 4 + (size_t)N * (1 + 8 * 3 + 4 * 2 + 8 * 8);
+  if (need > fr) return fail_create(h, "hc_create: problem exceeds free device memory", HC_ENOMEM);
+  static bool tables_ok = false;
+  if (!tables_ok) {
+    if (upload_tables() != cudaSuccess) return fail_create(h, "hc_create: constant table upload failed", HC_ECUDA);
+    tables_ok = true;
+  }
+  if (!alloc_common(h)) return fail_create(h, "hc_create: device allocation failed", HC_ENOMEM);
+  cudaMemcpy(h->ess, h->ess_host.data(), N, cudaMemcpyHostToDevice);
+  cudaError_t e = tet_setup_device(h, desc, edofs, sv);
+  if (e == cudaErrorInvalidValue && h->err.empty())
+    return fail_create(h, "hc_create: degenerate (zero-volume) tet", HC_EINVAL);
+  if (e != cudaSuccess) return fail_create(h, "hc_create: " + h->err + " " + cudaGetErrorString(e), HC_ECUDA);
+  e = diag_finish(N, h->ess, h->diag, h->dinv, h->dinvf, h->sdinv, h->sdinvf, nullptr);
+  if (e == cudaErrorInvalidValue)
+    return fail_create(h, "hc_create: operator diagonal is not positive (nu = 0 and sigma = 0 somewhere?)",
+                       HC_EINVAL);
+  if (e != cudaSuccess) return fail_create(h, std::string("hc_create: ") + cudaGetErrorString(e), HC_ECUDA);
+  if (ensure_scalars(h) != cudaSuccess) return fail_create(h, "hc_create: scalar allocation failed", HC_ENOMEM);
+  *out = h;
+  return HC_OK;
+}
+
 extern "C" {
 
 hc_status hc_last_error(const hcop_t* h, char* buf, size_t n) {
@@ -182,6 +239,9 @@ void hc_destroy(hcop_t* h) {
   cudaFree(h->xbuf);
   cudaFree(h->ybuf);
   cudaFree(h->verts);
+  cudaFree(h->tet_edofs);
+  cudaFree(h->tetK64);
+  cudaFree(h->tetK32);
   cudaFree(h->tab);
   delete h;
 }
@@ -189,8 +249,7 @@ void hc_destroy(hcop_t* h) {
 hc_status hc_create(const hc_problem_desc* desc, hcop_t** out) {
   if (!desc || !out) return fail_create(nullptr, "hc_create: null argument", HC_EINVAL);
   *out = nullptr;
-  if (desc->elem_type == HC_TET)
-    return fail_create(nullptr, "hc_create: tetrahedral meshes are not supported by this build", HC_ENOTSUP);
+  if (desc->elem_type == HC_TET) return create_tet(desc, out);
   if (desc->elem_type != HC_HEX) return fail_create(nullptr, "hc_create: unknown elem_type", HC_EINVAL);
   if (desc->order < 1 || desc->order > kMaxP)
     return fail_create(nullptr, "hc_create: hex order must be 1..3", HC_EINVAL);
@@ -406,6 +465,11 @@ hc_status hc_add_mult_device_f32(hcop_t* h, const float* x, float* y) {
 
 hc_status hc_apply_form_device(hcop_t* h, const double* x, double* y) {
   if (!h || !x || !y) return HC_EINVAL;
+  if (h->type == HC_TET) {
+    HC_CUDA_TRY(h, cudaMemsetAsync(y, 0, h->ndof * sizeof(double), h->stream));
+    HC_CUDA_TRY(h, tet_apply_launch<double>(h, h->tetK64, x, y, 1, false, 1.0, nullptr, h->stream));
+    return HC_OK;
+  }
   HC_CUDA_TRY(h, cudaMemsetAsync(y, 0, h->ndof * sizeof(double), h->stream));
   HC_CUDA_TRY(h, hex_apply<double>(h->hexdev(), h->fac, x, y, h->has_mass ? 1.0 : 0.0, 1.0, false, nullptr,
                                    nullptr, h->stream, true));
@@ -440,6 +504,10 @@ hc_status hc_apply_form(hcop_t* h, const double* x, double* y) {
 
 hc_status hc_add_weak_curlcurl(hcop_t* h, const double* x, double* y, double scale) {
   if (!h || !x || !y || !std::isfinite(scale)) return HC_EINVAL;
+  if (h->type != HC_HEX) {
+    h->err = "hc_add_weak_curlcurl: structured hex grids only in this build";
+    return HC_ENOTSUP;
+  }
   hc_status st = h2d(h, h->xbuf, x);
   if (st == HC_OK) st = h2d(h, h->ybuf, y);
   if (st != HC_OK) return st;
@@ -454,9 +522,49 @@ hc_status hc_diag(hcop_t* h, double* d) {
   return d2h_sync(h, d, h->diag);
 }
 
+// ---- multi right-hand-side apply ------------------------------------------------
+hc_status hc_mult_multi_device(hcop_t* h, int precision, int nrhs, const void* X, void* Y) {
+  if (!h || !X || !Y) return HC_EINVAL;
+  if (nrhs != 1 && nrhs != 2 && nrhs != 4 && nrhs != 8 && nrhs != 16 && nrhs != 32) {
+    h->err = "hc_mult_multi_device: nrhs must be 1, 2, 4, 8, 16 or 32";
+    return HC_EINVAL;
+  }
+  if (precision != HC_FP64 && precision != HC_FP32) {
+    h->err = "hc_mult_multi_device: precision must be HC_FP64 or HC_FP32";
+    return HC_EINVAL;
+  }
+  if (h->type != HC_TET) {
+    if (nrhs != 1) {
+      h->err = "hc_mult_multi_device: hex grids take one right-hand side per call in this build";
+      return HC_ENOTSUP;
+    }
+    return precision == HC_FP64 ? hc_mult_device(h, (const double*)X, (double*)Y)
+                                : hc_mult_device_f32(h, (const float*)X, (float*)Y);
+  }
+  if (precision == HC_FP64) {
+    HC_CUDA_TRY(h, init_masked_multi<double>(h->ndof, nrhs, h->ess, (const double*)X, (double*)Y, h->stream));
+    HC_CUDA_TRY(h, tet_apply_launch<double>(h, h->tetK64, (const double*)X, (double*)Y, nrhs, true, 1.0, nullptr,
+                                            h->stream));
+  } else {
+    HC_CUDA_TRY(h, init_masked_multi<float>(h->ndof, nrhs, h->ess, (const float*)X, (float*)Y, h->stream));
+    HC_CUDA_TRY(h, tet_apply_launch<float>(h, h->tetK32, (const float*)X, (float*)Y, nrhs, true, 1.0, nullptr,
+                                           h->stream));
+  }
+  return HC_OK;
+}
+
+int32_t hc_elem_type(const hcop_t* h) { return h ? h->type : -1; }
+
+hc_status hc_tet_element_matrix(hcop_t* h, int64_t e, double* out) {
+  if (!h || !out || h->type != HC_TET || e < 0 || e >= h->ne) return HC_EINVAL;
+  const int L = h->p == 1 ? 6 : 20;
+  HC_CUDA_TRY(h, cudaMemcpy(out, h->tetK64 + e * L * L, L * L * sizeof(double), cudaMemcpyDeviceToHost));
+  return HC_OK;
+}
+
 // ---- curl, load vector ------------------------------------------------------------
 int64_t hc_num_rt_dofs(const hcop_t* h) {
-  if (!h) return -1;
+  if (!h || h->type != HC_HEX) return -1;
   int64_t o1, o2, n;
   hex_rt_layout(h->hexdev(), &o1, &o2, &n);
   return n;
@@ -475,12 +583,20 @@ int64_t hc_hex_rt_dof_index(const hcop_t* h, int c, int64_t i, int64_t j, int64_
 
 hc_status hc_curl_device(hcop_t* h, const double* A, double* B) {
   if (!h || !A || !B) return HC_EINVAL;
+  if (h->type != HC_HEX) {
+    h->err = "hc_curl: structured hex grids only in this build";
+    return HC_ENOTSUP;
+  }
   HC_CUDA_TRY(h, hex_curl(h->hexdev(), A, B, h->stream));
   return HC_OK;
 }
 
 hc_status hc_curl(hcop_t* h, const double* A, double* B) {
   if (!h || !A || !B) return HC_EINVAL;
+  if (h->type != HC_HEX) {
+    h->err = "hc_curl: structured hex grids only in this build";
+    return HC_ENOTSUP;
+  }
   const int64_t nrt = hc_num_rt_dofs(h);
   double* dB = nullptr;
   HC_CUDA_TRY(h, cudaMallocAsync((void**)&dB, nrt * sizeof(double), h->stream));
@@ -495,6 +611,10 @@ hc_status hc_curl(hcop_t* h, const double* A, double* B) {
 }
 
 hc_status hc_load_coil_device(hcop_t* h, const hc_coil* coil, int q, double* b) {
+  if (h && h->type != HC_HEX) {
+    h->err = "hc_load_coil: structured hex grids only in this build";
+    return HC_ENOTSUP;
+  }
   if (!h || !coil || !b || q < 1 || q > 8) {
     if (h) h->err = "hc_load_coil: need a coil and 1 <= q <= 8";
     return HC_EINVAL;

@@ -96,6 +96,11 @@ struct hcop {
   double* ybuf = nullptr;
   double lmax64 = 0.0, lmax32 = 0.0;   // cached Chebyshev bounds
   double* verts = nullptr;             // device vertex coordinates (hex grid)
+  // tetrahedral meshes
+  int64_t n_edges = 0, n_faces = 0;
+  int32_t* tet_edofs = nullptr;        // ne * L element dofs
+  double* tetK64 = nullptr;            // ne * L * L element matrices (FP64)
+  float* tetK32 = nullptr;             // FP32 copy
   int* tab = nullptr;                  // brick tile table of the apply kernel
 
   hc::HexDev hexdev() const {
@@ -141,11 +146,26 @@ cudaError_t hex_curl(const HexDev& d, const double* A, double* B, cudaStream_t s
 cudaError_t hex_load_coil(const HexDev& d, const double* V, const double coil[7], int q, const double* xq,
                           const double* wq, const double* bc, const double* bo, double* b, cudaStream_t s);
 
+// ---- hc_tet.cu ----
+hc_status tet_topology(hcop* h, const hc_problem_desc* d, std::vector<int32_t>& edofs,
+                       std::vector<int32_t>& sorted_verts);
+cudaError_t tet_setup_device(hcop* h, const hc_problem_desc* desc, const std::vector<int32_t>& edofs,
+                             const std::vector<int32_t>& sv);
+template <typename T>
+cudaError_t tet_apply_launch(const hcop* h, const T* K, const T* x, T* y, int nrhs, bool masked, double scale,
+                             const int* done, cudaStream_t s);
+// pq = p.q over all dofs, then alpha = rz / pq (PCG mode of operators without a fused energy)
+template <typename T>
+cudaError_t dot_alpha(int64_t n, const T* p, const T* q, KrylovScalars* S, double* partials, cudaStream_t s);
+
 // ---- hc_krylov.cu ----
 cudaError_t diag_finish(int64_t n, const uint8_t* ess, double* d, double* dinv, float* dinvf, double* sd,
                         float* sdf, cudaStream_t s);
 template <typename T>
 cudaError_t init_masked(int64_t n, const uint8_t* ess, const T* x, T* y, cudaStream_t s);
+// y[i*nrhs + r] = ess[i] ? x[i*nrhs + r] : 0
+template <typename T>
+cudaError_t init_masked_multi(int64_t n, int nrhs, const uint8_t* ess, const T* x, T* y, cudaStream_t s);
 // operator callback used by the solvers: y = J x with y pre-initialised by the
 // callee; S/partials as in hex_apply
 template <typename T>

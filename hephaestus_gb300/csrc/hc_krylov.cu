@@ -74,11 +74,79 @@ cudaError_t init_masked(int64_t n, const uint8_t* ess, const T* x, T* y, cudaStr
   return cudaGetLastError();
 }
 template cudaError_t init_masked<double>(int64_t, const uint8_t*, const double*, double*, cudaStream_t);
+template <typename T>
+__global__ void k_init_masked_multi(int64_t n, int nrhs, const uint8_t* __restrict__ ess, const T* __restrict__ x,
+                                    T* __restrict__ y) {
+  GS_LOOP(i, n * nrhs) y[i] = ess[i / nrhs] ? x[i] : T(0);
+}
+template <typename T>
+cudaError_t init_masked_multi(int64_t n, int nrhs, const uint8_t* ess, const T* x, T* y, cudaStream_t s) {
+  k_init_masked_multi<T><<<vgrid(n * nrhs), kRedThreads, 0, s>>>(n, nrhs, ess, x, y);
+  return cudaGetLastError();
+}
+template cudaError_t init_masked_multi<double>(int64_t, int, const uint8_t*, const double*, double*, cudaStream_t);
+template cudaError_t init_masked_multi<float>(int64_t, int, const uint8_t*, const float*, float*, cudaStream_t);
 template cudaError_t init_masked<float>(int64_t, const uint8_t*, const float*, float*, cudaStream_t);
 
+// q.p over all dofs; alpha = rz / pq with the breakdown test (PCG mode of an
+// operator without a fused energy reduction)
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+    k_dot_alpha(int64_t n, const T* __restrict__ p, const T* __restrict__ q, KrylovScalars* S, double* partials) {
+  if (S->done) return;
+  double v[1] = {0.0}, tot[1];
+  T acc = T(0);
+  int c = 0;
+  GS_LOOP(i, n) {
+    acc += p[i] * q[i];
+    if (++c == 8) {
+      v[0] += (double)acc;
+      acc = T(0);
+      c = 0;
+    }
+  }
+  v[0] += (double)acc;
+  block_sum_n<1>(v);
+  if (grid_sum_n<1>(v, partials, &S->counter[0], tot)) {
+    const double pq = tot[0];
+    S->pq = pq;
+    if (!(pq > 0.0) || !isfinite(pq)) {
+      S->done = 1;
+      S->status = HC_BREAKDOWN;
+      S->alpha = 0.0;
+    } else {
+      S->alpha = S->rz / pq;
+    }
+  }
+}
+template <typename T>
+cudaError_t dot_alpha(int64_t n, const T* p, const T* q, KrylovScalars* S, double* partials, cudaStream_t s) {
+  k_dot_alpha<T><<<vgrid(n), kRedThreads, 0, s>>>(n, p, q, S, partials);
+  return cudaGetLastError();
+}
+template cudaError_t dot_alpha<double>(int64_t, const double*, const double*, KrylovScalars*, double*, cudaStream_t);
+template cudaError_t dot_alpha<float>(int64_t, const float*, const float*, KrylovScalars*, double*, cudaStream_t);
+
+template <typename T>
+static const T* tetK_of(const hcop* h);
+template <>
+const double* tetK_of<double>(const hcop* h) {
+  return h->tetK64;
+}
+template <>
+const float* tetK_of<float>(const hcop* h) {
+  return h->tetK32;
+}
+
+// y += P K P x on top of the caller's initialisation of y ((I-P)x for J).
 template <typename T>
 cudaError_t OpJ<T>::apply(const T* x, T* y, KrylovScalars* S, double* partials, cudaStream_t s,
                           bool y_zero_free) const {
+  if (h->type == HC_TET) {
+    cudaError_t e = tet_apply_launch<T>(h, tetK_of<T>(h), x, y, 1, true, 1.0, S ? &S->done : nullptr, s);
+    if (e == cudaSuccess && S) e = dot_alpha<T>(h->ndof, x, y, S, partials, s);
+    return e;
+  }
   const HexDev d = h->hexdev();
   return hex_apply<T>(d, fac, x, y, h->has_mass ? 1.0 : 0.0, 1.0, true, S, partials, s, y_zero_free);
 }

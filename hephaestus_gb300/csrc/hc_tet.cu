@@ -1,0 +1,409 @@
+// hc_tet.cu -- Nedelec (first kind) element-matrix path on tetrahedra, orders 1 and 2.
+//
+// Basis on the element's vertices sorted by global index (conforming without
+// sign flips):  W_bc = l_b grad l_c - l_c grad l_b,
+//   p = 1: W_ij on the 6 edges;
+//   p = 2: l_i W_ij, l_j W_ij on each edge ij, and l_k W_ij, l_j W_ik on each face ijk.
+// Edges / faces are numbered in lexicographic order of their sorted vertex
+// tuples; dofs: p*edge + s, then 2*n_edges + 2*face + s.
+//
+// Element matrices K_e = dt nu_e C_e + sigma_e M_e are built in FP64 in closed
+// form: every basis function is a sum of (coefficient x barycentric monomial x
+// constant vector) terms, its curl likewise, and integrals of barycentric
+// monomials over a tet are exact (6|T| prod k_i! / (sum k + 3)!).  They are the
+// element matrices MFEM's CurlCurlIntegrator + VectorFEMassIntegrator form
+// for element-constant coefficients (src/kernels/curl_curl_kernel.cpp:21-24,
+// src/kernels/vector_fe_mass_kernel.cpp:21-24), in this basis.
+//
+// Apply: one warp per element; lane = (right-hand side, half of the rows); the
+// element's dof vectors are gathered (coalesced over right-hand sides), the
+// 20 x 20 product accumulated in FP32/FP64, rows scattered with atomic adds.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "hc_internal.h"
+#include "hc_reduce.cuh"
+
+namespace hc {
+
+namespace {
+const int kEdges[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+const int kFaces[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
+}  // namespace
+
+// ---- host topology -------------------------------------------------------------
+hc_status tet_topology(hcop* h, const hc_problem_desc* d, std::vector<int32_t>& edofs,
+                       std::vector<int32_t>& sorted_verts) {
+  const int64_t ne = d->n_elem, nv = d->n_vert;
+  const int p = d->order;
+  sorted_verts.resize(ne * 4);
+  for (int64_t e = 0; e < ne; ++e) {
+    int64_t s[4];
+    for (int k = 0; k < 4; ++k) {
+      s[k] = d->elem_verts[4 * e + k];
+      if (s[k] < 0 || s[k] >= nv) {
+        h->err = "hc_create: tet vertex index out of range";
+        return HC_EINVAL;
+      }
+    }
+    std::sort(s, s + 4);
+    if (s[0] == s[1] || s[1] == s[2] || s[2] == s[3]) {
+      h->err = "hc_create: degenerate tet (repeated vertex)";
+      return HC_EINVAL;
+    }
+    for (int k = 0; k < 4; ++k) sorted_verts[4 * e + k] = (int32_t)s[k];
+  }
+  std::vector<uint64_t> ekeys;
+  ekeys.reserve(ne * 6);
+  for (int64_t e = 0; e < ne; ++e)
+    for (auto& ed : kEdges)
+      ekeys.push_back((uint64_t)sorted_verts[4 * e + ed[0]] * (uint64_t)nv + (uint64_t)sorted_verts[4 * e + ed[1]]);
+  std::sort(ekeys.begin(), ekeys.end());
+  ekeys.erase(std::unique(ekeys.begin(), ekeys.end()), ekeys.end());
+  std::vector<std::array<int32_t, 3>> fkeys;
+  if (p == 2) {
+    fkeys.reserve(ne * 4);
+    for (int64_t e = 0; e < ne; ++e)
+      for (auto& f : kFaces)
+        fkeys.push_back({sorted_verts[4 * e + f[0]], sorted_verts[4 * e + f[1]], sorted_verts[4 * e + f[2]]});
+    std::sort(fkeys.begin(), fkeys.end());
+    fkeys.erase(std::unique(fkeys.begin(), fkeys.end()), fkeys.end());
+  }
+  const int64_t nE = (int64_t)ekeys.size(), nF = (int64_t)fkeys.size();
+  const int L = p == 1 ? 6 : 20;
+  h->ndof = p == 1 ? nE : 2 * nE + 2 * nF;
+  h->n_edges = nE;
+  h->n_faces = nF;
+  if (h->ndof >= ((int64_t)1 << 31)) {
+    h->err = "hc_create: more than 2^31 - 1 dofs per problem is not supported";
+    return HC_ENOTSUP;
+  }
+  edofs.resize(ne * L);
+  for (int64_t e = 0; e < ne; ++e) {
+    int32_t* dd = &edofs[e * L];
+    for (int k = 0; k < 6; ++k) {
+      const uint64_t key =
+          (uint64_t)sorted_verts[4 * e + kEdges[k][0]] * (uint64_t)nv + (uint64_t)sorted_verts[4 * e + kEdges[k][1]];
+      const int64_t g = std::lower_bound(ekeys.begin(), ekeys.end(), key) - ekeys.begin();
+      if (p == 1) dd[k] = (int32_t)g;
+      else {
+        dd[2 * k] = (int32_t)(2 * g);
+        dd[2 * k + 1] = (int32_t)(2 * g + 1);
+      }
+    }
+    if (p == 2)
+      for (int f = 0; f < 4; ++f) {
+        const std::array<int32_t, 3> key{sorted_verts[4 * e + kFaces[f][0]], sorted_verts[4 * e + kFaces[f][1]],
+                                         sorted_verts[4 * e + kFaces[f][2]]};
+        const int64_t g = std::lower_bound(fkeys.begin(), fkeys.end(), key) - fkeys.begin();
+        dd[12 + 2 * f] = (int32_t)(2 * nE + 2 * g);
+        dd[12 + 2 * f + 1] = (int32_t)(2 * nE + 2 * g + 1);
+      }
+  }
+  // essential dofs from marked boundary triangles
+  h->ess_host.assign(h->ndof, 0);
+  if (d->ess_mask) {
+    for (int64_t i = 0; i < h->ndof; ++i) h->ess_host[i] = d->ess_mask[i] ? 1 : 0;
+    h->explicit_mask = true;
+  } else if (d->n_bdr > 0 && d->bdr_tris && d->bdr_attr) {
+    for (int64_t b = 0; b < d->n_bdr; ++b) {
+      const int a = d->bdr_attr[b];
+      if (a < 1 || a > 31 || !((d->ess_attr_bits >> (a - 1)) & 1)) continue;
+      int64_t s[3] = {d->bdr_tris[3 * b], d->bdr_tris[3 * b + 1], d->bdr_tris[3 * b + 2]};
+      std::sort(s, s + 3);
+      const int pr[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+      for (auto& q : pr) {
+        const uint64_t key = (uint64_t)s[q[0]] * (uint64_t)nv + (uint64_t)s[q[1]];
+        auto it = std::lower_bound(ekeys.begin(), ekeys.end(), key);
+        if (it == ekeys.end() || *it != key) {
+          h->err = "hc_create: boundary triangle edge is not an edge of the mesh";
+          return HC_EINVAL;
+        }
+        const int64_t g = it - ekeys.begin();
+        if (p == 1) h->ess_host[g] = 1;
+        else h->ess_host[2 * g] = h->ess_host[2 * g + 1] = 1;
+      }
+      if (p == 2) {
+        const std::array<int32_t, 3> key{(int32_t)s[0], (int32_t)s[1], (int32_t)s[2]};
+        auto it = std::lower_bound(fkeys.begin(), fkeys.end(), key);
+        if (it == fkeys.end() || *it != key) {
+          h->err = "hc_create: boundary triangle is not a face of the mesh";
+          return HC_EINVAL;
+        }
+        const int64_t g = it - fkeys.begin();
+        h->ess_host[2 * nE + 2 * g] = h->ess_host[2 * nE + 2 * g + 1] = 1;
+      }
+    }
+  }
+  return HC_OK;
+}
+
+// ---- closed-form element matrices ------------------------------------------------
+__constant__ int c_tet_edges[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+__constant__ int c_tet_faces[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
+__device__ __forceinline__ int kEdgesD(int k, int s) { return c_tet_edges[k][s]; }
+__device__ __forceinline__ int kFacesD(int f, int s) { return c_tet_faces[f][s]; }
+
+// basis function as value terms (coef, lambda multiset, grad index) and curl
+// terms (coef, lambda index or -1, cross(grad u, grad v))
+struct VTerm {
+  double c;
+  int l0, l1;  // lambda indices (-1 = none)
+  int g;       // gradient index
+};
+struct CTerm {
+  double c;
+  int l;       // lambda index (-1 = none)
+  int u, v;    // cross(grad l_u, grad l_v)
+};
+
+__device__ __forceinline__ void basis_terms(int p, int I, VTerm* vt, int* nv, CTerm* ct, int* nc) {
+  // p = 1: W_bc ; p = 2: l_a W_bc
+  int a = -1, b, c;
+  if (p == 1) {
+    b = kEdgesD(I, 0);
+    c = kEdgesD(I, 1);
+  } else if (I < 12) {
+    const int k = I / 2;
+    b = kEdgesD(k, 0);
+    c = kEdgesD(k, 1);
+    a = (I % 2 == 0) ? b : c;
+  } else {
+    const int f = (I - 12) / 2, s = (I - 12) % 2;
+    const int i = kFacesD(f, 0), j = kFacesD(f, 1), k = kFacesD(f, 2);
+    if (s == 0) {
+      a = k;
+      b = i;
+      c = j;
+    } else {
+      a = j;
+      b = i;
+      c = k;
+    }
+  }
+  // value: l_a l_b grad l_c - l_a l_c grad l_b
+  vt[0] = {1.0, a, b, c};
+  vt[1] = {-1.0, a, c, b};
+  *nv = 2;
+  if (a < 0) {
+    // curl W_bc = 2 grad l_b x grad l_c
+    ct[0] = {2.0, -1, b, c};
+    *nc = 1;
+  } else {
+    // curl(l_a W_bc) = l_b (grad a x grad c) - l_c (grad a x grad b) + 2 l_a (grad b x grad c)
+    ct[0] = {1.0, b, a, c};
+    ct[1] = {-1.0, c, a, b};
+    ct[2] = {2.0, a, b, c};
+    *nc = 3;
+  }
+}
+
+// integral over the unit-volume-normalised tet of prod lambda_i^{k_i}:
+// 6 prod k_i! / (K + 3)!  (multiply by |T|)
+__device__ __forceinline__ double mono_int(const int k[4]) {
+  const double fact[7] = {1, 1, 2, 6, 24, 120, 720};
+  const double inv_fact3[8] = {1.0 / 6, 1.0 / 24, 1.0 / 120, 1.0 / 720, 1.0 / 5040, 1.0 / 40320, 1.0 / 362880,
+                               1.0 / 3628800};
+  const int K = k[0] + k[1] + k[2] + k[3];
+  return 6.0 * fact[k[0]] * fact[k[1]] * fact[k[2]] * fact[k[3]] * inv_fact3[K];
+}
+
+__global__ void tet_elem_matrix_kernel(int64_t ne, int p, const double* __restrict__ V,
+                                       const int32_t* __restrict__ sv, const double* __restrict__ nu,
+                                       const double* __restrict__ sigma, double dt, double* __restrict__ K64,
+                                       float* __restrict__ K32, int* __restrict__ bad) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const int L = p == 1 ? 6 : 20;
+  const double* v0 = V + 3 * (int64_t)sv[4 * e];
+  double J[9];
+  for (int cidx = 0; cidx < 3; ++cidx) {
+    const double* vc = V + 3 * (int64_t)sv[4 * e + cidx + 1];
+    for (int r = 0; r < 3; ++r) J[3 * r + cidx] = vc[r] - v0[r];
+  }
+  const double det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) +
+                     J[2] * (J[3] * J[7] - J[4] * J[6]);
+  if (!(fabs(det) > 0.0) || !isfinite(det)) {
+    atomicExch(bad, 1);
+    return;
+  }
+  // rows of J^-1 are grad lambda_1..3 (J columns are v_k - v_0)
+  double gl[4][3];
+  gl[1][0] = (J[4] * J[8] - J[5] * J[7]) / det;
+  gl[1][1] = (J[2] * J[7] - J[1] * J[8]) / det;
+  gl[1][2] = (J[1] * J[5] - J[2] * J[4]) / det;
+  gl[2][0] = (J[5] * J[6] - J[3] * J[8]) / det;
+  gl[2][1] = (J[0] * J[8] - J[2] * J[6]) / det;
+  gl[2][2] = (J[2] * J[3] - J[0] * J[5]) / det;
+  gl[3][0] = (J[3] * J[7] - J[4] * J[6]) / det;
+  gl[3][1] = (J[1] * J[6] - J[0] * J[7]) / det;
+  gl[3][2] = (J[0] * J[4] - J[1] * J[3]) / det;
+  for (int r = 0; r < 3; ++r) gl[0][r] = -(gl[1][r] + gl[2][r] + gl[3][r]);
+  double G[4][4];
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) G[i][j] = gl[i][0] * gl[j][0] + gl[i][1] * gl[j][1] + gl[i][2] * gl[j][2];
+  // cross products grad u x grad v, indexed [u][v]
+  double X[4][4][3];
+  for (int u = 0; u < 4; ++u)
+    for (int v = 0; v < 4; ++v) {
+      X[u][v][0] = gl[u][1] * gl[v][2] - gl[u][2] * gl[v][1];
+      X[u][v][1] = gl[u][2] * gl[v][0] - gl[u][0] * gl[v][2];
+      X[u][v][2] = gl[u][0] * gl[v][1] - gl[u][1] * gl[v][0];
+    }
+  const double vol = fabs(det) / 6.0;
+  const double a = dt * nu[e], s = sigma ? sigma[e] : 0.0;
+  for (int I = 0; I < L; ++I) {
+    VTerm vi[2], vj[2];
+    CTerm ci[3], cj[3];
+    int nvi, nci, nvj, ncj;
+    basis_terms(p, I, vi, &nvi, ci, &nci);
+    for (int Jj = I; Jj < L; ++Jj) {
+      basis_terms(p, Jj, vj, &nvj, cj, &ncj);
+      double m = 0.0, c = 0.0;
+      for (int x = 0; x < nvi; ++x)
+        for (int y = 0; y < nvj; ++y) {
+          int k[4] = {0, 0, 0, 0};
+          if (vi[x].l0 >= 0) k[vi[x].l0]++;
+          k[vi[x].l1]++;
+          if (vj[y].l0 >= 0) k[vj[y].l0]++;
+          k[vj[y].l1]++;
+          m += vi[x].c * vj[y].c * G[vi[x].g][vj[y].g] * mono_int(k);
+        }
+      for (int x = 0; x < nci; ++x)
+        for (int y = 0; y < ncj; ++y) {
+          int k[4] = {0, 0, 0, 0};
+          if (ci[x].l >= 0) k[ci[x].l]++;
+          if (cj[y].l >= 0) k[cj[y].l]++;
+          const double* A = X[ci[x].u][ci[x].v];
+          const double* B = X[cj[y].u][cj[y].v];
+          c += ci[x].c * cj[y].c * (A[0] * B[0] + A[1] * B[1] + A[2] * B[2]) * mono_int(k);
+        }
+      const double val = vol * (a * c + s * m);
+      K64[(e * L + I) * L + Jj] = val;
+      K64[(e * L + Jj) * L + I] = val;
+      K32[(e * L + I) * L + Jj] = (float)val;
+      K32[(e * L + Jj) * L + I] = (float)val;
+    }
+  }
+}
+
+// ---- apply -----------------------------------------------------------------------
+// y (+)= P K P x for nrhs right-hand sides stored row-major ([dof][rhs]).
+// One warp per element: lane = rhs + nrhs * part, rows split between parts.
+template <typename T, int L>
+__global__ void __launch_bounds__(256) tet_apply_kernel(int64_t ne, const int32_t* __restrict__ edofs,
+                                                        const T* __restrict__ K, const uint8_t* __restrict__ ess,
+                                                        int masked, int nrhs, T scale, const T* __restrict__ x,
+                                                        T* __restrict__ y, const int* done) {
+  if (done && *done) return;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int nparts = 32 / nrhs;  // nrhs in {1, 2, 4, 8, 16, 32}
+  const int r = lane % nrhs, part = lane / nrhs;
+  for (int64_t e = warp; e < ne; e += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    int dof[L];
+    T xe[L];
+#pragma unroll
+    for (int j = 0; j < L; ++j) {
+      dof[j] = __ldg(edofs + e * L + j);
+      T v = __ldg(x + (int64_t)dof[j] * nrhs + r);
+      if (masked && ess[dof[j]]) v = T(0);
+      xe[j] = v;
+    }
+    const T* Ke = K + e * L * L;
+    for (int i = part; i < L; i += nparts) {
+      if (masked && ess[dof[i]]) continue;
+      T acc = T(0);
+#pragma unroll
+      for (int j = 0; j < L; ++j) acc += __ldg(Ke + i * L + j) * xe[j];
+      atomicAdd(y + (int64_t)dof[i] * nrhs + r, scale * acc);
+    }
+  }
+}
+
+template <typename T>
+cudaError_t tet_apply_launch(const hcop* h, const T* K, const T* x, T* y, int nrhs, bool masked, double scale,
+                             const int* done, cudaStream_t s) {
+  {
+    const cudaError_t prior = cudaGetLastError();  // report a failure of an earlier call
+    if (prior != cudaSuccess) return prior;
+  }
+  const int warps_per_block = 8;
+  int64_t blocks = (h->ne + warps_per_block - 1) / warps_per_block;
+  blocks = std::min<int64_t>(blocks, 152 * 16);
+  if (h->p == 1)
+    tet_apply_kernel<T, 6><<<(unsigned)blocks, 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess, masked ? 1 : 0,
+                                                            nrhs, (T)scale, x, y, done);
+  else
+    tet_apply_kernel<T, 20><<<(unsigned)blocks, 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess, masked ? 1 : 0,
+                                                             nrhs, (T)scale, x, y, done);
+  return cudaGetLastError();
+}
+template cudaError_t tet_apply_launch<double>(const hcop*, const double*, const double*, double*, int, bool, double,
+                                              const int*, cudaStream_t);
+template cudaError_t tet_apply_launch<float>(const hcop*, const float*, const float*, float*, int, bool, double,
+                                             const int*, cudaStream_t);
+
+template <int L>
+__global__ void tet_diag_kernel(int64_t ne, const int32_t* __restrict__ edofs, const double* __restrict__ K,
+                                double* __restrict__ d) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  for (int i = 0; i < L; ++i) atomicAdd(d + edofs[e * L + i], K[(e * L + i) * L + i]);
+}
+
+cudaError_t tet_setup_device(hcop* h, const hc_problem_desc* desc, const std::vector<int32_t>& edofs,
+                             const std::vector<int32_t>& sv) {
+  const int L = h->p == 1 ? 6 : 20;
+  const int64_t ne = h->ne;
+  double* V = nullptr;
+  int32_t* dsv = nullptr;
+  double *dnu = nullptr, *dsig = nullptr;
+  int* bad = nullptr;
+  cudaError_t e = cudaMalloc((void**)&h->tet_edofs, edofs.size() * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&h->tetK64, (size_t)ne * L * L * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&h->tetK32, (size_t)ne * L * L * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&V, desc->n_vert * 3 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&dsv, sv.size() * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&dnu, ne * sizeof(double));
+  if (e == cudaSuccess && desc->sigma) e = cudaMalloc((void**)&dsig, ne * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&bad, sizeof(int));
+  if (e == cudaSuccess) {
+    cudaMemcpy(h->tet_edofs, edofs.data(), edofs.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+    cudaMemcpy(V, desc->vertices, desc->n_vert * 3 * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(dsv, sv.data(), sv.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+    cudaMemcpy(dnu, desc->nu, ne * sizeof(double), cudaMemcpyHostToDevice);
+    if (dsig) cudaMemcpy(dsig, desc->sigma, ne * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemset(bad, 0, sizeof(int));
+    tet_elem_matrix_kernel<<<(unsigned)((ne + 127) / 128), 128>>>(ne, h->p, V, dsv, dnu, dsig, h->dt, h->tetK64,
+                                                                  h->tetK32, bad);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+      h->err = std::string("tet element-matrix kernel: ") + cudaGetErrorString(e);
+    } else {
+      cudaMemset(h->diag, 0, h->ndof * sizeof(double));
+      if (L == 6)
+        tet_diag_kernel<6><<<(unsigned)((ne + 127) / 128), 128>>>(ne, h->tet_edofs, h->tetK64, h->diag);
+      else
+        tet_diag_kernel<20><<<(unsigned)((ne + 127) / 128), 128>>>(ne, h->tet_edofs, h->tetK64, h->diag);
+      e = cudaGetLastError();
+      if (e == cudaSuccess) e = cudaDeviceSynchronize();
+      if (e != cudaSuccess) h->err = std::string("tet diagonal kernel: ") + cudaGetErrorString(e);
+      int hb = 0;
+      cudaMemcpy(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost);
+      if (e == cudaSuccess && hb) e = cudaErrorInvalidValue;
+    }
+  }
+  cudaFree(V);
+  cudaFree(dsv);
+  cudaFree(dnu);
+  cudaFree(dsig);
+  cudaFree(bad);
+  return e;
+}
+
+}  // namespace hc

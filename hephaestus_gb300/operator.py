@@ -99,6 +99,56 @@ class HCurlOperator:
     right-hand side.
     """
 
+    @classmethod
+    def from_tets(cls, verts, tets, order, nu, sigma=None, dt=1.0, btris=None, battr=None, ess_attr_bits=~0,
+                  ess_mask=None, stream=None):
+        """Tetrahedral mesh (vertices n x 3, tets m x 4), Nedelec order 1 or 2.
+        Essential dofs: boundary triangles with attributes selected by
+        ess_attr_bits, or an explicit per-dof mask."""
+        self = cls.__new__(cls)
+        keep = dict(verts=np.ascontiguousarray(verts, dtype=np.float64),
+                    tets=np.ascontiguousarray(tets, dtype=np.int64),
+                    nu=np.ascontiguousarray(nu, dtype=np.float64),
+                    sigma=None if sigma is None else np.ascontiguousarray(sigma, dtype=np.float64),
+                    btris=None if btris is None else np.ascontiguousarray(btris, dtype=np.int64),
+                    battr=None if battr is None else np.ascontiguousarray(battr, dtype=np.int32),
+                    mask=None if ess_mask is None else np.ascontiguousarray(ess_mask, dtype=np.uint8))
+        d = N.ProblemDesc()
+        d.elem_type = N.HC_TET
+        d.order = order
+        d.n_vert = keep["verts"].shape[0]
+        d.n_elem = keep["tets"].shape[0]
+        d.vertices = _ptr(keep["verts"])
+        d.elem_verts = _ptr(keep["tets"])
+        d.nu = _ptr(keep["nu"])
+        d.sigma = _ptr(keep["sigma"])
+        d.dt = dt
+        d.ess_mask = _ptr(keep["mask"])
+        d.ess_attr_bits = ess_attr_bits & 0x7FFFFFFF
+        if keep["btris"] is not None:
+            d.n_bdr = keep["btris"].shape[0]
+            d.bdr_tris = _ptr(keep["btris"])
+            d.bdr_attr = _ptr(keep["battr"])
+        self._finish(d, keep, dt, order, stream)
+        self.nx = self.ny = self.nz = None
+        return self
+
+    def _finish(self, d, keep, dt, order, stream):
+        L = N.lib()
+        h = C.c_void_p()
+        st = L.hc_create(C.byref(d), C.byref(h))
+        if st != N.HC_OK:
+            raise N.HcError(st, N.last_error(None))
+        self._keep = keep
+        self._nu = keep["nu"]
+        self.h = h
+        self.order, self.dt = order, dt
+        self.ndof = L.hc_num_dofs(h)
+        self.ne = L.hc_num_elems(h)
+        self.height = self.width = self.ndof
+        if stream is not None:
+            self.set_stream(stream)
+
     def __init__(self, nx, ny, nz, order, nu, sigma=None, dt=1.0, vertices=None, ess_attr_bits=0x3F,
                  ess_mask=None, stream=None):
         L = N.lib()
@@ -218,6 +268,21 @@ class HCurlOperator:
         else:
             N.check(N.lib().hc_add_mult_device(self.h, _dev_ptr(x, "float64"), _dev_ptr(y, "float64")), self.h)
         return y
+
+    def ElementMatrix(self, e):
+        """FP64 element matrix of tet e (local dof order of the basis)."""
+        L = 6 if self.order == 1 else 20
+        out = np.empty((L, L))
+        N.check(N.lib().hc_tet_element_matrix(self.h, e, _ptr(out)), self.h)
+        return out
+
+    def MultMultiDevice(self, X, Y):
+        """Y = J X for a (ndof, nrhs) row-major CUDA tensor (float32 or float64)."""
+        prec = N.HC_FP32 if str(X.dtype) == "torch.float32" else N.HC_FP64
+        name = "float32" if prec == N.HC_FP32 else "float64"
+        nrhs = 1 if X.dim() == 1 else X.shape[1]
+        N.check(N.lib().hc_mult_multi_device(self.h, prec, nrhs, _dev_ptr(X, name), _dev_ptr(Y, name)), self.h)
+        return Y
 
     def ApplyFormDevice(self, x, y):
         N.check(N.lib().hc_apply_form_device(self.h, _dev_ptr(x, "float64"), _dev_ptr(y, "float64")), self.h)

@@ -3,7 +3,8 @@
  *
  * One handle owns one discretised problem on the device: the Nedelec space on
  * a structured hex grid (sum-factorised partial assembly) or on a tet mesh
- * (element matrices), the per-element coefficient factors, the essential
+ * (closed-form FP64 element matrices, orders 1-2), the per-element
+ * coefficient factors, the essential
  * (tangential Dirichlet) dof set and all Krylov work space.  The operator is
  * the reference's A/E-formulation bilinear form
  *
@@ -175,6 +176,17 @@ typedef struct {
 } hc_coil;
 hc_status hc_load_coil(hcop_t* h, const hc_coil* coil, int q, double* b);
 hc_status hc_load_coil_device(hcop_t* h, const hc_coil* coil, int q, double* b);
+
+/* Y = J X for nrhs right-hand sides stored row-major ([dof][rhs]), device
+ * pointers of the given precision (HC_FP64: double, HC_FP32: float);
+ * nrhs in {1, 2, 4, 8, 16, 32}.  Tet meshes apply each element matrix to all
+ * right-hand sides at once (config 3's batched element-matrix apply).      */
+hc_status hc_mult_multi_device(hcop_t* h, int precision, int nrhs, const void* X, void* Y);
+/* HC_HEX or HC_TET */
+int32_t hc_elem_type(const hcop_t* h);
+/* Tet meshes: the FP64 element matrix (L x L, L = 6 or 20) of element e,
+ * rows/columns in the local dof order of the basis.                        */
+hc_status hc_tet_element_matrix(hcop_t* h, int64_t e, double* out);
 
 /* ---- linear solve --------------------------------------------------------- */
 /* Solve J x = b for x (x holds the initial guess on entry).  Replaces the

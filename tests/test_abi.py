@@ -72,13 +72,6 @@ def test_null_arguments_return_einval():
     L.hc_destroy(None)  # no-op
 
 
-def test_tets_not_yet_supported_is_reported():
-    nu = np.ones(8)
-    d = _desc(elem_type=N.HC_TET, nu=nu.ctypes.data_as(C.c_void_p))
-    h = C.c_void_p()
-    assert N.lib().hc_create(C.byref(d), C.byref(h)) == N.HC_ENOTSUP
-
-
 def test_mfem_shim_compiles_against_stub():
     """include/hcurl_mfem.hpp (the reference-side binding) type-checks and
     links against the library."""
@@ -104,3 +97,20 @@ def test_header_is_plain_c():
     r = subprocess.run(["gcc", "-std=c99", "-fsyntax-only", "-x", "c", os.path.join(root, "include", "hcurl_op.h")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_tet_descriptor_validation():
+    L = N.lib()
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=np.float64)
+    t = np.array([[0, 1, 2, 3]], dtype=np.int64)
+    nu = np.ones(1)
+    P = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    for order, tets, msg in ((3, t, "order"), (1, np.array([[0, 1, 1, 3]], dtype=np.int64), "degenerate"),
+                             (1, np.array([[0, 1, 2, 7]], dtype=np.int64), "range")):
+        d = N.ProblemDesc()
+        d.elem_type, d.order, d.dt = N.HC_TET, order, 1.0
+        d.n_vert, d.n_elem = 4, 1
+        d.vertices, d.elem_verts, d.nu = P(v), P(tets), P(nu)
+        h = C.c_void_p()
+        assert L.hc_create(C.byref(d), C.byref(h)) == N.HC_EINVAL
+        assert msg in N.last_error(None)
