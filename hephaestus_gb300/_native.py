@@ -113,6 +113,7 @@ _SIGS = {
     "hc_hex_rt_dof_index": (C.c_int64, [C.c_void_p, C.c_int, C.c_int64, C.c_int64, C.c_int64]),
     "hc_curl": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "hc_curl_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hc_curl_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "hc_load_coil": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "hc_load_coil_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
 }

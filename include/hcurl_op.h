@@ -166,6 +166,15 @@ int64_t hc_num_rt_dofs(const hcop_t* h);
 int64_t hc_hex_rt_dof_index(const hcop_t* h, int c, int64_t i, int64_t j, int64_t k);
 hc_status hc_curl(hcop_t* h, const double* A, double* B);
 hc_status hc_curl_device(hcop_t* h, const double* A, double* B);
+/* hc_curl without any device allocation in the call: B is staged in a static
+ * device area of HC_CURL_STATIC_MAX_RT_DOFS doubles (8 MiB) instead of a
+ * buffer allocated per call.  Grids with more Raviart-Thomas dofs return
+ * HC_EINVAL.  The first call on each device looks the area up with
+ * cudaGetSymbolAddress (make it before any stream capture).  The area is
+ * shared by every caller on a device: calls that overlap in time there race
+ * and must be serialised.  No counterpart in the reference.               */
+#define HC_CURL_STATIC_MAX_RT_DOFS (1 << 20)
+hc_status hc_curl_static(hcop_t* h, const double* A, double* B);
 
 /* Loop coil J = I0 (-(y-yc), x-xc, 0) for r0 <= r <= r1, z0 <= z <= z1 (r about
  * (xc, yc)), else 0.  b_i = (J, w_i) with a q^3 Gauss-Legendre rule per hex
