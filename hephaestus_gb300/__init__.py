@@ -6,5 +6,5 @@ interface, and synthetic-workload generators.
 """
 from . import meshes  # noqa: F401
 from ._native import HcError, NativeUnavailable  # noqa: F401
-from .operator import (CurlCurlKernel, GpuHCurlPCGSolver, HCurlForm, HCurlOperator,  # noqa: F401
-                       VectorFEMassKernel)
+from .operator import (CurlCurlKernel, GpuComplexCOCGSolver, GpuHCurlPCGSolver, HCurlForm,  # noqa: F401
+                       HCurlOperator, VectorFEMassKernel)

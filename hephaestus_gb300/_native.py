@@ -114,6 +114,17 @@ _SIGS = {
     "hc_curl": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "hc_curl_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "hc_curl_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hc_mult_complex": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]),
+    "hc_mult_complex_device": (C.c_int, [C.c_void_p, C.c_double] + [C.c_void_p] * 4),
+    "hc_mult_complex_device_f32": (C.c_int, [C.c_void_p, C.c_double] + [C.c_void_p] * 4),
+    "hc_solve_complex": (C.c_int, [C.c_void_p, C.POINTER(SolveParams), C.c_double, C.c_void_p, C.c_void_p,
+                                   C.POINTER(SolveInfo)]),
+    "hc_solve_complex_device": (C.c_int, [C.c_void_p, C.POINTER(SolveParams), C.c_double] + [C.c_void_p] * 4
+                                + [C.POINTER(SolveInfo)]),
+    "hc_solve_complex_graph": (C.c_int, [C.c_void_p, C.POINTER(SolveParams), C.c_double] + [C.c_void_p] * 4),
+    "hc_graph_solve_info": (C.c_int, [C.c_void_p, C.POINTER(SolveInfo)]),
+    "hc_solve_complex_batch": (C.c_int, [C.c_int32, C.c_void_p, C.POINTER(SolveParams), C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(SolveInfo)]),
     "hc_load_coil": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "hc_load_coil_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
 }

@@ -224,6 +224,7 @@ hc_status hc_set_stream(hcop_t* h, void* stream) {
 
 void hc_destroy(hcop_t* h) {
   if (!h) return;
+  complex_free(h);
   cudaFree(h->fac);
   cudaFree(h->facf);
   cudaFree(h->ess);

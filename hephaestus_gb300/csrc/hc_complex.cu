@@ -1,0 +1,989 @@
+// hc_complex.cu -- frequency-domain operator A = C_nu + i omega M_sigma and its
+// complex-symmetric solve.
+//
+// Reference: ComplexMaxwellOperator::Solve assembles a ParSesquilinearForm with
+// CurlCurlIntegrator(nu) in the real part and VectorFEMassIntegrator(omega
+// sigma) in the imaginary part (src/formulations/ComplexMaxwell/complex_maxwell_formulation.cpp:171-222)
+// and solves the 2N x 2N real system (Hermitian convention) with SuperLU.  The
+// same system is the complex-symmetric A u = b, solved here matrix-free by
+// COCG (conjugate orthogonal CG, van der Vorst & Melissen 1990) with a complex
+// Jacobi preconditioner, in FP64 or as FP32 inner COCG inside FP64 iterative
+// refinement.  Vectors are planar (separate real and imaginary arrays).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "hc_graph.h"
+#include "hc_internal.h"
+#include "hc_reduce.cuh"
+
+namespace hc {
+
+#define GS_LOOP(i, n) \
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
+
+static inline unsigned cgrid(int64_t n) {
+  int64_t b = (n + kRedThreads - 1) / kRedThreads;
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, kRedBlocks));
+}
+
+struct CScalars {
+  double rho_r, rho_i;    // r^T z
+  double alpha_r, alpha_i;
+  double beta_r, beta_i;
+  double rr, bb, tol2;  // tol2 = max(rtol2 |b|^2, atol2), set by k_c_setup
+  double rtol2, atol2;
+  int it, done, status, maxit;
+  int trips;  // WHILE-loop trips of a graph-driven solve
+  unsigned int counter[4];
+};
+
+// ---- complex operator -------------------------------------------------------------
+// y = (I-P) x + P (C + i w M) P x, planar.  The curl factor of the handle
+// carries dt, so C_nu = (dt C_nu) / dt.
+#define HC_EXTERN_CPLX(T, P)                                                                              \
+  extern template cudaError_t hex_launch_cplx_p<T, P>(const HexDev&, const T*, const T*, const T*, T*, T*, T, T, \
+                                                      bool, const int*, cudaStream_t);
+HC_EXTERN_CPLX(double, 1)
+HC_EXTERN_CPLX(double, 2)
+HC_EXTERN_CPLX(float, 1)
+HC_EXTERN_CPLX(float, 2)
+#undef HC_EXTERN_CPLX
+
+// y = (I-P) x for both parts in one launch; skipped when *done != 0.
+template <typename T>
+__global__ void k_c_init_masked(int64_t n, const uint8_t* __restrict__ ess, const T* __restrict__ xr,
+                                const T* __restrict__ xi, T* __restrict__ yr, T* __restrict__ yi,
+                                const int* __restrict__ done) {
+  if (done && *done) return;
+  GS_LOOP(k, n) {
+    const bool e = ess[k] != 0;
+    yr[k] = e ? xr[k] : T(0);
+    yi[k] = e ? xi[k] : T(0);
+  }
+}
+
+// One init for both parts ((I-P) x) and one fused kernel (orders 1-2); `done`
+// (may be null) skips both once a COCG batch has stopped.
+template <typename T>
+cudaError_t complex_apply_done(hcop* h, double omega, const T* xr, const T* xi, T* yr, T* yi, const int* done,
+                               cudaStream_t s) {
+  const T* fac = sizeof(T) == 8 ? (const T*)h->fac : (const T*)h->facf;
+  const HexDev d = h->hexdev();
+  const T cs = (T)(1.0 / h->dt);
+  const T om = h->has_mass ? (T)omega : T(0);
+  k_c_init_masked<T><<<cgrid(h->ndof), kRedThreads, 0, s>>>(h->ndof, h->ess, xr, xi, yr, yi, done);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  switch (h->p) {
+    case 1: return hex_launch_cplx_p<T, 1>(d, fac, xr, xi, yr, yi, om, cs, true, done, s);
+    case 2: return hex_launch_cplx_p<T, 2>(d, fac, xr, xi, yr, yi, om, cs, true, done, s);
+    case 3: {
+      // order 3: four launches of the real kernel (no fused variant)
+      (void)done;
+      e = hex_apply<T>(d, fac, xr, yr, 0.0, (double)cs, true, nullptr, nullptr, s, false);
+      if (e == cudaSuccess && om != T(0)) e = hex_apply<T>(d, fac, xi, yr, -omega, 0.0, true, nullptr, nullptr, s, false);
+      if (e == cudaSuccess) e = hex_apply<T>(d, fac, xi, yi, 0.0, (double)cs, true, nullptr, nullptr, s, false);
+      if (e == cudaSuccess && om != T(0)) e = hex_apply<T>(d, fac, xr, yi, omega, 0.0, true, nullptr, nullptr, s, false);
+      return e;
+    }
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename T>
+cudaError_t complex_apply(hcop* h, double omega, const T* xr, const T* xi, T* yr, T* yi, cudaStream_t s) {
+  return complex_apply_done<T>(h, omega, xr, xi, yr, yi, nullptr, s);
+}
+
+// Complex inverse diagonal: 1 / (dC + i w dM) at free dofs, 1 at essential rows.
+__global__ void k_cinv_diag(int64_t n, const uint8_t* __restrict__ ess, const double* __restrict__ dC,
+                            const double* __restrict__ dM, double omega, double* __restrict__ ir,
+                            double* __restrict__ ii, float* __restrict__ irf, float* __restrict__ iif) {
+  GS_LOOP(k, n) {
+    double a = 1.0, b = 0.0;
+    if (!ess[k]) {
+      a = dC[k];
+      b = omega * dM[k];
+    }
+    double den = a * a + b * b;
+    if (!(den > 0.0) || !isfinite(den)) {
+      a = 1.0;
+      b = 0.0;
+      den = 1.0;
+    }
+    const double r = a / den, im = -b / den;
+    ir[k] = r;
+    ii[k] = im;
+    irf[k] = (float)r;
+    iif[k] = (float)im;
+  }
+}
+
+// ---- COCG kernels ---------------------------------------------------------------------
+// r = b - Ax (q holds Ax); z = D^-1 r; p = z; rho = r^T z; rr = |r|^2; bb = |b|^2
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+    k_c_setup(int64_t n, const T* br, const T* bi, const T* qr, const T* qi, T* rr_, T* ri_, T* pr, T* pi,
+              const T* dr, const T* di, CScalars* S, double* partials, const int* active) {
+  // active (may be null): 0 skips the launch (a stopped refinement loop);
+  // qr == nullptr: x = 0, r = b
+  if (active && !*active) return;
+  double v[4] = {0, 0, 0, 0}, tot[4];
+  GS_LOOP(k, n) {
+    const double a = qr ? (double)br[k] - (double)qr[k] : (double)br[k];
+    const double b = qr ? (double)bi[k] - (double)qi[k] : (double)bi[k];
+    rr_[k] = (T)a;
+    ri_[k] = (T)b;
+    const double zr = a * (double)dr[k] - b * (double)di[k], zi = a * (double)di[k] + b * (double)dr[k];
+    pr[k] = (T)zr;
+    pi[k] = (T)zi;
+    v[0] += a * zr - b * zi;
+    v[1] += a * zi + b * zr;
+    v[2] += a * a + b * b;
+    v[3] += (double)br[k] * (double)br[k] + (double)bi[k] * (double)bi[k];
+  }
+  block_sum_n<4>(v);
+  if (grid_sum_n<4>(v, partials, &S->counter[0], tot)) {
+    S->rho_r = tot[0];
+    S->rho_i = tot[1];
+    S->rr = tot[2];
+    S->bb = tot[3];
+    S->it = 0;
+    S->done = 0;
+    S->status = HC_NOT_CONVERGED;
+    S->tol2 = fmax(S->rtol2 * tot[3], S->atol2);
+    if (!isfinite(tot[2]) || !isfinite(tot[3])) {
+      S->done = 1;
+      S->status = HC_BREAKDOWN;
+    } else if (tot[2] <= S->tol2) {
+      S->done = 1;
+      S->status = HC_OK;
+    }
+  }
+}
+
+// alpha = rho / (p^T q)
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+    k_c_alpha(int64_t n, const T* pr, const T* pi, const T* qr, const T* qi, CScalars* S, double* partials) {
+  if (S->done) return;
+  double v[2] = {0, 0}, tot[2];
+  GS_LOOP(k, n) {
+    const double a = pr[k], b = pi[k], c = qr[k], d = qi[k];
+    v[0] += a * c - b * d;
+    v[1] += a * d + b * c;
+  }
+  block_sum_n<2>(v);
+  if (grid_sum_n<2>(v, partials, &S->counter[1], tot)) {
+    const double den = tot[0] * tot[0] + tot[1] * tot[1];
+    if (!(den > 0.0) || !isfinite(den)) {
+      S->done = 1;
+      S->status = HC_BREAKDOWN;
+      S->alpha_r = S->alpha_i = 0.0;
+    } else {
+      // (rho_r + i rho_i) / (t_r + i t_i)
+      S->alpha_r = (S->rho_r * tot[0] + S->rho_i * tot[1]) / den;
+      S->alpha_i = (S->rho_i * tot[0] - S->rho_r * tot[1]) / den;
+    }
+  }
+}
+
+// x += alpha p; r -= alpha q; z = D^-1 r; rho' = r^T z; rr = |r|^2; beta = rho'/rho
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+    k_c_update(int64_t n, T* xr, T* xi, T* rr_, T* ri_, const T* pr, const T* pi, const T* qr, const T* qi,
+               const T* dr, const T* di, CScalars* S, double* partials) {
+  if (S->done) return;
+  const T ar = (T)S->alpha_r, ai = (T)S->alpha_i;
+  double v[3] = {0, 0, 0}, tot[3];
+  GS_LOOP(k, n) {
+    const T p_r = pr[k], p_i = pi[k];
+    xr[k] += ar * p_r - ai * p_i;
+    xi[k] += ar * p_i + ai * p_r;
+    const T q_r = qr[k], q_i = qi[k];
+    const T a = rr_[k] - (ar * q_r - ai * q_i), b = ri_[k] - (ar * q_i + ai * q_r);
+    rr_[k] = a;
+    ri_[k] = b;
+    const double da = a, db = b, zr = da * (double)dr[k] - db * (double)di[k],
+                 zi = da * (double)di[k] + db * (double)dr[k];
+    v[0] += da * zr - db * zi;
+    v[1] += da * zi + db * zr;
+    v[2] += da * da + db * db;
+  }
+  block_sum_n<3>(v);
+  if (grid_sum_n<3>(v, partials, &S->counter[2], tot)) {
+    S->it += 1;
+    S->rr = tot[2];
+    const double den = S->rho_r * S->rho_r + S->rho_i * S->rho_i;
+    if (!isfinite(tot[2]) || !(den > 0.0)) {
+      S->done = 1;
+      S->status = HC_BREAKDOWN;
+    } else if (tot[2] <= S->tol2) {
+      S->done = 1;
+      S->status = HC_OK;
+    } else if (S->it >= S->maxit) {
+      S->done = 1;
+      S->status = HC_NOT_CONVERGED;
+    }
+    if (den > 0.0) {
+      S->beta_r = (tot[0] * S->rho_r + tot[1] * S->rho_i) / den;
+      S->beta_i = (tot[1] * S->rho_r - tot[0] * S->rho_i) / den;
+    }
+    S->rho_r = tot[0];
+    S->rho_i = tot[1];
+  }
+}
+
+// p = D^-1 r + beta p
+template <typename T>
+__global__ void k_c_dir(int64_t n, const T* rr_, const T* ri_, const T* dr, const T* di, T* pr, T* pi,
+                        const CScalars* S) {
+  if (S->done) return;
+  const T br = (T)S->beta_r, bi = (T)S->beta_i;
+  GS_LOOP(k, n) {
+    const T a = rr_[k], b = ri_[k];
+    const T zr = a * dr[k] - b * di[k], zi = a * di[k] + b * dr[k];
+    const T p_r = pr[k], p_i = pi[k];
+    pr[k] = zr + br * p_r - bi * p_i;
+    pi[k] = zi + br * p_i + bi * p_r;
+  }
+}
+
+// ---- host drivers -----------------------------------------------------------------------
+struct ComplexWork {
+  double *dC = nullptr, *dM = nullptr, *ir = nullptr, *ii = nullptr;
+  float *irf = nullptr, *iif = nullptr;
+  double omega = -1.0;
+  CScalars* S = nullptr;
+  CScalars* hS = nullptr;
+  void* vec = nullptr;
+  size_t vec_bytes = 0;
+  void* graph = nullptr;  // ComplexGraph of the graph-driven solve
+};
+
+static void cgraph_free(ComplexWork* w);
+
+static ComplexWork* cwork(hcop* h) {
+  if (!h->cwork) h->cwork = new ComplexWork();
+  return static_cast<ComplexWork*>(h->cwork);
+}
+
+void complex_free(hcop* h) {
+  if (!h->cwork) return;
+  ComplexWork* w = static_cast<ComplexWork*>(h->cwork);
+  cgraph_free(w);
+  cudaFree(w->dC);
+  cudaFree(w->dM);
+  cudaFree(w->ir);
+  cudaFree(w->ii);
+  cudaFree(w->irf);
+  cudaFree(w->iif);
+  cudaFree(w->S);
+  cudaFreeHost(w->hS);
+  cudaFree(w->vec);
+  delete w;
+  h->cwork = nullptr;
+}
+
+static hc_status complex_prepare(hcop* h, double omega) {
+  ComplexWork* w = cwork(h);
+  const int64_t n = h->ndof;
+  if (!w->dC) {
+    if (cudaMalloc((void**)&w->dC, n * 8) != cudaSuccess || cudaMalloc((void**)&w->dM, n * 8) != cudaSuccess ||
+        cudaMalloc((void**)&w->ir, n * 8) != cudaSuccess || cudaMalloc((void**)&w->ii, n * 8) != cudaSuccess ||
+        cudaMalloc((void**)&w->irf, n * 4) != cudaSuccess || cudaMalloc((void**)&w->iif, n * 4) != cudaSuccess ||
+        cudaMalloc((void**)&w->S, sizeof(CScalars)) != cudaSuccess ||
+        cudaMallocHost((void**)&w->hS, sizeof(CScalars)) != cudaSuccess) {
+      h->err = "complex work space allocation failed";
+      return HC_ENOMEM;
+    }
+    cudaMemset(w->S, 0, sizeof(CScalars));
+    HexDev d = h->hexdev();
+    HC_CUDA_TRY(h, cudaMemsetAsync(w->dC, 0, n * 8, h->stream));
+    HC_CUDA_TRY(h, cudaMemsetAsync(w->dM, 0, n * 8, h->stream));
+    HC_CUDA_TRY(h, hex_diag_scaled(d, w->dC, 0.0, 1.0 / h->dt, h->stream));
+    HC_CUDA_TRY(h, hex_diag_scaled(d, w->dM, 1.0, 0.0, h->stream));
+  }
+  if (w->omega != omega) {
+    k_cinv_diag<<<cgrid(n), kRedThreads, 0, h->stream>>>(n, h->ess, w->dC, w->dM, omega, w->ir, w->ii, w->irf,
+                                                         w->iif);
+    HC_CUDA_TRY(h, cudaGetLastError());
+    w->omega = omega;
+  }
+  return HC_OK;
+}
+
+// work vectors: FP64 path 6n doubles; mixed: 2n doubles (residual) + 2n
+// floats (rhs) + 2n floats (correction) + 6n floats (COCG)
+static hc_status complex_vectors(hcop* h) {
+  ComplexWork* w = cwork(h);
+  const int64_t n = h->ndof;
+  const size_t need = std::max((size_t)6 * n * sizeof(double), (size_t)2 * n * sizeof(double) + (size_t)10 * n * 4);
+  if (w->vec_bytes >= need) return HC_OK;
+  if (w->graph) cgraph_free(w);  // built on the old vectors
+  cudaFree(w->vec);
+  w->vec = nullptr;
+  w->vec_bytes = 0;
+  if (cudaMalloc(&w->vec, need) != cudaSuccess) {
+    h->err = "complex work vectors allocation failed";
+    return HC_ENOMEM;
+  }
+  w->vec_bytes = need;
+  return HC_OK;
+}
+
+template <typename T>
+static const T* cdr(ComplexWork* w);
+template <>
+const double* cdr<double>(ComplexWork* w) {
+  return w->ir;
+}
+template <>
+const float* cdr<float>(ComplexWork* w) {
+  return w->irf;
+}
+template <typename T>
+static const T* cdi(ComplexWork* w);
+template <>
+const double* cdi<double>(ComplexWork* w) {
+  return w->ii;
+}
+template <>
+const float* cdi<float>(ComplexWork* w) {
+  return w->iif;
+}
+
+// COCG on A x = b (planar).  wk: 6 n-vectors of T (r, p, q each re/im).
+template <typename T>
+static hc_status cocg_run(hcop* h, double omega, double rtol, double atol, int maxit, const T* br, const T* bi, T* xr,
+                          T* xi, T* wk, int* iters) {
+  ComplexWork* w = cwork(h);
+  const int64_t n = h->ndof;
+  cudaStream_t s = h->stream;
+  T *rr_ = wk, *ri_ = wk + n, *pr = wk + 2 * n, *pi = wk + 3 * n, *qr = wk + 4 * n, *qi = wk + 5 * n;
+  const T *dr = cdr<T>(w), *di = cdi<T>(w);
+  CScalars* S = w->S;
+  CScalars* hs = w->hS;
+  std::memset(hs, 0, sizeof(CScalars));
+  hs->rtol2 = rtol * rtol;
+  hs->atol2 = atol * atol;
+  hs->maxit = maxit;
+  HC_CUDA_TRY(h, cudaMemcpyAsync(S, hs, sizeof(CScalars), cudaMemcpyHostToDevice, s));
+  HC_CUDA_TRY(h, complex_apply<T>(h, omega, xr, xi, qr, qi, s));
+  k_c_setup<T><<<cgrid(n), kRedThreads, 0, s>>>(n, br, bi, qr, qi, rr_, ri_, pr, pi, dr, di, S, h->partials,
+                                                 nullptr);
+  HC_CUDA_TRY(h, cudaGetLastError());
+  const int chunk = 20;
+  int launched = 0;
+  for (;;) {
+    for (int k = 0; k < chunk && launched < maxit; ++k, ++launched) {
+      HC_CUDA_TRY(h, complex_apply_done<T>(h, omega, pr, pi, qr, qi, &S->done, s));
+      k_c_alpha<T><<<cgrid(n), kRedThreads, 0, s>>>(n, pr, pi, qr, qi, S, h->partials);
+      k_c_update<T><<<cgrid(n), kRedThreads, 0, s>>>(n, xr, xi, rr_, ri_, pr, pi, qr, qi, dr, di, S, h->partials);
+      k_c_dir<T><<<cgrid(n), kRedThreads, 0, s>>>(n, rr_, ri_, dr, di, pr, pi, S);
+    }
+    HC_CUDA_TRY(h, cudaGetLastError());
+    HC_CUDA_TRY(h, cudaMemcpyAsync(hs, S, sizeof(CScalars), cudaMemcpyDeviceToHost, s));
+    HC_CUDA_TRY(h, cudaStreamSynchronize(s));
+    if (hs->done || launched >= maxit) break;
+  }
+  *iters = hs->it;
+  return hs->done ? (hc_status)hs->status : HC_NOT_CONVERGED;
+}
+
+__global__ void k_c_resid64(int64_t n, const double* br, const double* bi, double* rr_, double* ri_, CScalars* S,
+                            double* partials) {
+  double v[2] = {0, 0}, tot[2];
+  GS_LOOP(k, n) {
+    const double a = br[k] - rr_[k], b = bi[k] - ri_[k];
+    rr_[k] = a;
+    ri_[k] = b;
+    v[0] += a * a + b * b;
+    v[1] += br[k] * br[k] + bi[k] * bi[k];
+  }
+  block_sum_n<2>(v);
+  if (grid_sum_n<2>(v, partials, &S->counter[3], tot)) {
+    S->rr = tot[0];
+    S->bb = tot[1];
+  }
+}
+__global__ void k_c_d2f(int64_t n, const double* a, const double* b, float* af, float* bf, double s) {
+  GS_LOOP(k, n) {
+    af[k] = (float)(a[k] * s);
+    bf[k] = (float)(b[k] * s);
+  }
+}
+__global__ void k_c_axpy(int64_t n, const float* cr, const float* ci, double* xr, double* xi, double s) {
+  GS_LOOP(k, n) {
+    xr[k] += s * (double)cr[k];
+    xi[k] += s * (double)ci[k];
+  }
+}
+
+hc_status complex_solve_device(hcop* h, const hc_solve_params* prm, double omega, const double* br,
+                               const double* bi, double* xr, double* xi, hc_solve_info* info) {
+  if (h->type != HC_HEX) {
+    h->err = "complex solves: structured hex grids only in this build";
+    return HC_ENOTSUP;
+  }
+  hc_status st = complex_prepare(h, omega);
+  if (st != HC_OK) return st;
+  st = complex_vectors(h);
+  if (st != HC_OK) return st;
+  ComplexWork* w = cwork(h);
+  const int64_t n = h->ndof;
+  std::memset(info, 0, sizeof(*info));
+  cudaStream_t s = h->stream;
+  if (prm->precision == HC_FP64) {
+    int it = 0;
+    st = cocg_run<double>(h, omega, prm->rtol, prm->atol, prm->maxit, br, bi, xr, xi, (double*)w->vec, &it);
+    info->status = st;
+    info->iterations = it;
+    info->outer_iterations = 1;
+    info->rel_residual = w->hS->bb > 0 ? std::sqrt(w->hS->rr / w->hS->bb) : std::sqrt(w->hS->rr);
+    return st;
+  }
+  // FP32 inner COCG inside FP64 refinement
+  double* r64 = (double*)w->vec;
+  double* i64 = r64 + n;
+  float* rf = (float*)(i64 + n);
+  float* if_ = rf + n;
+  float* cr = if_ + n;
+  float* ci = cr + n;
+  float* wk = ci + n;
+  const unsigned g = cgrid(n);
+  int total = 0, outer = 0;
+  auto residual = [&](double* rn2, double* bn2) -> hc_status {
+    HC_CUDA_TRY(h, complex_apply<double>(h, omega, xr, xi, r64, i64, s));
+    k_c_resid64<<<g, kRedThreads, 0, s>>>(n, br, bi, r64, i64, w->S, h->partials);
+    HC_CUDA_TRY(h, cudaMemcpyAsync(w->hS, w->S, sizeof(CScalars), cudaMemcpyDeviceToHost, s));
+    HC_CUDA_TRY(h, cudaStreamSynchronize(s));
+    *rn2 = w->hS->rr;
+    *bn2 = w->hS->bb;
+    return HC_OK;
+  };
+  double rn2 = 0, bn2 = 0;
+  st = residual(&rn2, &bn2);
+  if (st != HC_OK) return st;
+  const double bn = std::sqrt(bn2), tol = std::max(prm->rtol * bn, prm->atol);
+  const double inner = prm->inner_rtol > 0 ? prm->inner_rtol : 1e-4;
+  const int max_outer = prm->max_outer > 0 ? prm->max_outer : 50;
+  hc_status result = HC_NOT_CONVERGED;
+  for (;;) {
+    const double rn = std::sqrt(rn2);
+    if (!std::isfinite(rn)) {
+      result = HC_BREAKDOWN;
+      break;
+    }
+    if (rn <= tol) {
+      result = HC_OK;
+      break;
+    }
+    if (outer >= max_outer || total >= prm->maxit) break;
+    ++outer;
+    k_c_d2f<<<g, kRedThreads, 0, s>>>(n, r64, i64, rf, if_, 1.0 / rn);
+    HC_CUDA_TRY(h, cudaMemsetAsync(cr, 0, 2 * n * sizeof(float), s));
+    int it = 0;
+    hc_status ist = cocg_run<float>(h, omega, inner, 0.0, prm->maxit - total, rf, if_, cr, ci, wk, &it);
+    total += it;
+    if (ist == HC_ECUDA || ist == HC_ENOMEM) return ist;
+    k_c_axpy<<<g, kRedThreads, 0, s>>>(n, cr, ci, xr, xi, rn);
+    HC_CUDA_TRY(h, cudaGetLastError());
+    st = residual(&rn2, &bn2);
+    if (st != HC_OK) return st;
+    if (ist == HC_BREAKDOWN && it == 0) {
+      result = HC_BREAKDOWN;
+      break;
+    }
+  }
+  info->status = result;
+  info->iterations = total;
+  info->outer_iterations = outer;
+  info->rel_residual = bn > 0 ? std::sqrt(rn2) / bn : std::sqrt(rn2);
+  return result;
+}
+
+}  // namespace hc
+
+namespace hc {
+hc_status complex_graph_launch(hcop* h, const hc_solve_params* prm, double omega, const double* br,
+                               const double* bi, double* xr, double* xi, int chunk);
+hc_status complex_graph_result(hcop* h, hc_solve_info* info);
+}  // namespace hc
+
+using namespace hc;
+
+// ---- C entry points -------------------------------------------------------------------
+static hc_status complex_check(hcop* h, double omega) {
+  if (h->type != HC_HEX) {
+    h->err = "complex operator: structured hex grids only in this build";
+    return HC_ENOTSUP;
+  }
+  if (!std::isfinite(omega) || omega < 0.0) {
+    h->err = "complex operator: omega must be finite and >= 0";
+    return HC_EINVAL;
+  }
+  return HC_OK;
+}
+
+extern "C" {
+
+hc_status hc_mult_complex_device(hcop_t* h, double omega, const double* xr, const double* xi, double* yr,
+                                 double* yi) {
+  if (!h || !xr || !xi || !yr || !yi) return HC_EINVAL;
+  hc_status st = complex_check(h, omega);
+  if (st != HC_OK) return st;
+  HC_CUDA_TRY(h, complex_apply<double>(h, omega, xr, xi, yr, yi, h->stream));
+  return HC_OK;
+}
+
+hc_status hc_mult_complex_device_f32(hcop_t* h, double omega, const float* xr, const float* xi, float* yr,
+                                     float* yi) {
+  if (!h || !xr || !xi || !yr || !yi) return HC_EINVAL;
+  hc_status st = complex_check(h, omega);
+  if (st != HC_OK) return st;
+  HC_CUDA_TRY(h, complex_apply<float>(h, omega, xr, xi, yr, yi, h->stream));
+  return HC_OK;
+}
+
+// Host vectors: x = [xr | xi] and y = [yr | yi], each 2 n_dof doubles (the
+// real-then-imaginary block layout of MFEM's ComplexOperator).
+hc_status hc_mult_complex(hcop_t* h, double omega, const double* x, double* y) {
+  if (!h || !x || !y) return HC_EINVAL;
+  hc_status st = complex_check(h, omega);
+  if (st != HC_OK) return st;
+  const int64_t n = h->ndof;
+  double* d = nullptr;
+  HC_CUDA_TRY(h, cudaMallocAsync((void**)&d, 4 * n * sizeof(double), h->stream));
+  cudaError_t e = cudaMemcpyAsync(d, x, 2 * n * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) e = complex_apply<double>(h, omega, d, d + n, d + 2 * n, d + 3 * n, h->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(y, d + 2 * n, 2 * n * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+  cudaFreeAsync(d, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) {
+    h->err = std::string("hc_mult_complex: ") + cudaGetErrorString(e);
+    return HC_ECUDA;
+  }
+  return HC_OK;
+}
+
+static hc_status complex_params(hcop* h, const hc_solve_params* p) {
+  if (!p) {
+    h->err = "null solve parameters";
+    return HC_EINVAL;
+  }
+  if (p->precision != HC_FP64 && p->precision != HC_MIXED) {
+    h->err = "precision must be HC_FP64 or HC_MIXED";
+    return HC_EINVAL;
+  }
+  if (p->precond != HC_PRECOND_JACOBI) {
+    h->err = "complex solves take the (complex) Jacobi preconditioner only";
+    return HC_ENOTSUP;
+  }
+  if (!(p->rtol >= 0.0) || !(p->atol >= 0.0) || p->maxit < 1) {
+    h->err = "rtol, atol must be >= 0 and maxit >= 1";
+    return HC_EINVAL;
+  }
+  return HC_OK;
+}
+
+hc_status hc_solve_complex_device(hcop_t* h, const hc_solve_params* prm, double omega, const double* br,
+                                  const double* bi, double* xr, double* xi, hc_solve_info* info) {
+  if (!h || !br || !bi || !xr || !xi) return HC_EINVAL;
+  hc_status st = complex_check(h, omega);
+  if (st == HC_OK) st = complex_params(h, prm);
+  if (st != HC_OK) return st;
+  hc_solve_info loc{};
+  return complex_solve_device(h, prm, omega, br, bi, xr, xi, info ? info : &loc);
+}
+
+hc_status hc_solve_complex(hcop_t* h, const hc_solve_params* prm, double omega, const double* b, double* x,
+                           hc_solve_info* info) {
+  if (!h || !b || !x) return HC_EINVAL;
+  hc_status st = complex_check(h, omega);
+  if (st == HC_OK) st = complex_params(h, prm);
+  if (st != HC_OK) return st;
+  const int64_t n = h->ndof;
+  double* d = nullptr;
+  HC_CUDA_TRY(h, cudaMallocAsync((void**)&d, 4 * n * sizeof(double), h->stream));
+  cudaError_t e = cudaMemcpyAsync(d, b, 2 * n * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d + 2 * n, x, 2 * n * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+  hc_status sst = HC_ECUDA;
+  if (e == cudaSuccess) {
+    hc_solve_info loc{};
+    sst = complex_solve_device(h, prm, omega, d, d + n, d + 2 * n, d + 3 * n, info ? info : &loc);
+  }
+  if (e == cudaSuccess && sst != HC_ECUDA && sst != HC_ENOMEM)
+    e = cudaMemcpyAsync(x, d + 2 * n, 2 * n * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+  cudaFreeAsync(d, h->stream);
+  cudaError_t e2 = cudaStreamSynchronize(h->stream);
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) {
+    h->err = std::string("hc_solve_complex: ") + cudaGetErrorString(e);
+    return HC_ECUDA;
+  }
+  return sst;
+}
+
+hc_status hc_solve_complex_graph(hcop_t* h, const hc_solve_params* prm, double omega, const double* br,
+                                 const double* bi, double* xr, double* xi) {
+  if (!h || !br || !bi || !xr || !xi) return HC_EINVAL;
+  hc_status st = complex_check(h, omega);
+  if (st == HC_OK) st = complex_params(h, prm);
+  if (st != HC_OK) return st;
+  return complex_graph_launch(h, prm, omega, br, bi, xr, xi, 0);
+}
+
+hc_status hc_graph_solve_info(hcop_t* h, hc_solve_info* info) {
+  if (!h || !info) return HC_EINVAL;
+  return complex_graph_result(h, info);
+}
+
+hc_status hc_solve_complex_batch(int32_t n, hcop_t* const* hs, const hc_solve_params* prm, const double* omega,
+                                 const double* const* br, const double* const* bi, double* const* xr,
+                                 double* const* xi, hc_solve_info* info) {
+  if (n < 0 || (n > 0 && (!hs || !prm || !omega || !br || !bi || !xr || !xi || !info))) return HC_EINVAL;
+  hc_status first = HC_OK;
+  for (int32_t i = 0; i < n; ++i) {
+    std::memset(&info[i], 0, sizeof(hc_solve_info));
+    const hc_status st = hc_solve_complex_graph(hs[i], prm, omega[i], br[i], bi[i], xr[i], xi[i]);
+    if (st != HC_OK) {
+      info[i].status = st;
+      if (first == HC_OK) first = st;
+    }
+  }
+  for (int32_t i = 0; i < n; ++i) {
+    if (info[i].status != HC_OK) continue;  // not launched
+    const hc_status st = hc_graph_solve_info(hs[i], &info[i]);
+    info[i].status = st;
+    if (st != HC_OK && first == HC_OK) first = st;
+  }
+  return first;
+}
+
+}  // extern "C"
+
+namespace hc {
+// ---- graph-driven solves ----------------------------------------------------------------
+// The same COCG (and refinement) as above, built once per argument set into
+// one CUDA graph whose loops are conditional WHILE nodes.  Stopping decisions
+// are taken on the device; every loop has a hard trip bound.
+struct CRefine {
+  double rn, bn, tol, rtol, atol;
+  int outer, total, max_outer, maxit, status, active, trips, pad;
+};
+
+__global__ void k_g_init(CScalars* S, double rtol2, double atol2, int maxit) {
+  S->rtol2 = rtol2;
+  S->atol2 = atol2;
+  S->maxit = maxit;
+  S->trips = 0;
+}
+
+// end of a COCG WHILE body: continue while not done and under the trip bound
+__global__ void k_c_cond(CScalars* S, cudaGraphConditionalHandle hnd, int max_trips) {
+  const int t = ++S->trips;
+  const int go = (!S->done && t < max_trips) ? 1 : 0;
+  if (!go && !S->done) {
+    S->done = 1;
+    S->status = HC_NOT_CONVERGED;
+  }
+  cudaGraphSetConditional(hnd, (unsigned)go);
+}
+
+__global__ void k_r_init(CRefine* R, double rtol, double atol, int maxit, int max_outer) {
+  R->rtol = rtol;
+  R->atol = atol;
+  R->tol = -1.0;
+  R->rn = R->bn = 0.0;
+  R->maxit = maxit;
+  R->max_outer = max_outer;
+  R->outer = R->total = R->trips = R->active = 0;
+  R->status = HC_NOT_CONVERGED;
+}
+
+// refinement step decision from the FP64 residual in S->rr (and |b|^2 in S->bb)
+__global__ void k_r_check(CRefine* R, const CScalars* S, cudaGraphConditionalHandle hnd, int max_trips) {
+  const double rn = sqrt(S->rr);
+  if (R->tol < 0.0) {
+    R->bn = sqrt(S->bb);
+    R->tol = fmax(R->rtol * R->bn, R->atol);
+  }
+  const int t = ++R->trips;
+  int stop = 1;
+  if (R->status == HC_BREAKDOWN) {
+  } else if (!isfinite(rn)) {
+    R->status = HC_BREAKDOWN;
+  } else if (rn <= R->tol) {
+    R->status = HC_OK;
+  } else if (R->outer >= R->max_outer || R->total >= R->maxit || t >= max_trips) {
+    R->status = HC_NOT_CONVERGED;
+  } else {
+    stop = 0;
+  }
+  R->rn = rn;
+  R->active = !stop;
+  if (!stop) R->outer += 1;
+  cudaGraphSetConditional(hnd, stop ? 0u : 1u);
+}
+
+// rf = r / |r| in FP32, correction = 0
+__global__ void k_r_d2f(int64_t n, const CRefine* R, const double* a, const double* b, float* af, float* bf,
+                        float* cr, float* ci) {
+  if (!R->active) return;
+  const double s = 1.0 / R->rn;
+  GS_LOOP(k, n) {
+    af[k] = (float)(a[k] * s);
+    bf[k] = (float)(b[k] * s);
+    cr[k] = 0.0f;
+    ci[k] = 0.0f;
+  }
+}
+
+__global__ void k_r_inner_init(CScalars* S, const CRefine* R, double rtol2, cudaGraphConditionalHandle hnd) {
+  S->rtol2 = rtol2;
+  S->atol2 = 0.0;
+  S->maxit = R->maxit - R->total;
+  S->trips = 0;
+  if (!R->active) S->done = 1;
+  cudaGraphSetConditional(hnd, R->active ? 1u : 0u);
+}
+
+// x += |r| c
+__global__ void k_r_accum(int64_t n, CRefine* R, const CScalars* S, const float* cr, const float* ci, double* xr,
+                          double* xi) {
+  if (!R->active) return;
+  const double s = R->rn;
+  GS_LOOP(k, n) {
+    xr[k] += s * (double)cr[k];
+    xi[k] += s * (double)ci[k];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    R->total += S->it;
+    if (S->status == HC_BREAKDOWN && S->it == 0) R->status = HC_BREAKDOWN;
+  }
+}
+
+struct ComplexGraph {
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t cap = nullptr;
+  CRefine* R = nullptr;
+  CRefine* hR = nullptr;
+  // arguments the graph was built for
+  int precision = -1, maxit = 0, max_outer = 0, chunk = 0;
+  double omega = 0, rtol = 0, atol = 0, inner = 0;
+  const void* ptr[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+static ComplexGraph* cgraph(hcop* h) {
+  ComplexWork* w = cwork(h);
+  if (!w->graph) w->graph = new ComplexGraph();
+  return static_cast<ComplexGraph*>(w->graph);
+}
+
+static void cgraph_free(ComplexWork* w) {
+  ComplexGraph* g = static_cast<ComplexGraph*>(w->graph);
+  if (!g) return;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->cap) cudaStreamDestroy(g->cap);
+  cudaFree(g->R);
+  cudaFreeHost(g->hR);
+  delete g;
+  w->graph = nullptr;
+}
+
+static hc_status complex_graph_build(hcop* h, const hc_solve_params* prm, double omega, const double* br,
+                                     const double* bi, double* xr, double* xi, int chunk) {
+  ComplexWork* w = cwork(h);
+  ComplexGraph* G = cgraph(h);
+  const int64_t n = h->ndof;
+  if (!G->cap) HC_CUDA_TRY(h, cudaStreamCreateWithFlags(&G->cap, cudaStreamNonBlocking));
+  if (!G->R) {
+    HC_CUDA_TRY(h, cudaMalloc((void**)&G->R, sizeof(CRefine)));
+    HC_CUDA_TRY(h, cudaMallocHost((void**)&G->hR, sizeof(CRefine)));
+    std::memset(G->hR, 0, sizeof(CRefine));
+  }
+  if (G->exec) {
+    cudaGraphExecDestroy(G->exec);
+    G->exec = nullptr;
+  }
+  CScalars* S = w->S;
+  const int unit = prm->maxit / chunk + 3;  // trip bound of one COCG loop
+  cudaGraph_t top = nullptr;
+  HC_CUDA_TRY(h, cudaGraphCreate(&top, 0));
+  GraphChain c{top, nullptr};
+  cudaError_t e = cudaSuccess;
+  if (prm->precision == HC_FP64) {
+    double* wk = (double*)w->vec;
+    e = chain_segment(c, G->cap, [&](cudaStream_t s) {
+      k_g_init<<<1, 1, 0, s>>>(S, prm->rtol * prm->rtol, prm->atol * prm->atol, prm->maxit);
+      cudaError_t ee = complex_apply_done<double>(h, omega, xr, xi, wk + 4 * n, wk + 5 * n, nullptr, s);
+      if (ee != cudaSuccess) return ee;
+      k_c_setup<double><<<cgrid(n), kRedThreads, 0, s>>>(n, br, bi, wk + 4 * n, wk + 5 * n, wk, wk + n, wk + 2 * n,
+                                                          wk + 3 * n, w->ir, w->ii, S, h->partials, nullptr);
+      return cudaGetLastError();
+    });
+    cudaGraphConditionalHandle hl = 0;
+    GraphChain body;
+    if (e == cudaSuccess) e = chain_handle(c, &hl);
+    if (e == cudaSuccess) e = chain_while(c, hl, &body);
+    // x is updated in place by k_c_update through the work layout below
+    if (e == cudaSuccess)
+      e = chain_segment(body, G->cap, [&](cudaStream_t s) {
+        const int64_t nn = n;
+        double *rr_ = wk, *ri_ = wk + nn, *pr = wk + 2 * nn, *pi = wk + 3 * nn, *qr = wk + 4 * nn, *qi = wk + 5 * nn;
+        for (int k = 0; k < chunk; ++k) {
+          cudaError_t ee = complex_apply_done<double>(h, omega, pr, pi, qr, qi, &S->done, s);
+          if (ee != cudaSuccess) return ee;
+          k_c_alpha<double><<<cgrid(nn), kRedThreads, 0, s>>>(nn, pr, pi, qr, qi, S, h->partials);
+          k_c_update<double><<<cgrid(nn), kRedThreads, 0, s>>>(nn, xr, xi, rr_, ri_, pr, pi, qr, qi, w->ir, w->ii,
+                                                               S, h->partials);
+          k_c_dir<double><<<cgrid(nn), kRedThreads, 0, s>>>(nn, rr_, ri_, w->ir, w->ii, pr, pi, S);
+        }
+        k_c_cond<<<1, 1, 0, s>>>(S, hl, unit);
+        return cudaGetLastError();
+      });
+  } else {
+    double* r64 = (double*)w->vec;
+    double* i64 = r64 + n;
+    float* rf = (float*)(i64 + n);
+    float* if_ = rf + n;
+    float* cr = if_ + n;
+    float* ci = cr + n;
+    float* wk = ci + n;
+    CRefine* R = G->R;
+    const double inner = prm->inner_rtol > 0 ? prm->inner_rtol : 1e-4;
+    const int max_outer = prm->max_outer > 0 ? prm->max_outer : 50;
+    e = chain_segment(c, G->cap, [&](cudaStream_t s) {
+      k_r_init<<<1, 1, 0, s>>>(R, prm->rtol, prm->atol, prm->maxit, max_outer);
+      return cudaGetLastError();
+    });
+    cudaGraphConditionalHandle ho = 0, hi = 0;
+    GraphChain ob, ib;
+    if (e == cudaSuccess) e = chain_handle(c, &ho);
+    if (e == cudaSuccess) e = chain_while(c, ho, &ob);
+    if (e == cudaSuccess) e = chain_handle(ob, &hi);
+    if (e == cudaSuccess)
+      e = chain_segment(ob, G->cap, [&](cudaStream_t s) {
+        cudaError_t ee = complex_apply_done<double>(h, omega, xr, xi, r64, i64, nullptr, s);
+        if (ee != cudaSuccess) return ee;
+        k_c_resid64<<<cgrid(n), kRedThreads, 0, s>>>(n, br, bi, r64, i64, S, h->partials);
+        k_r_check<<<1, 1, 0, s>>>(R, S, ho, max_outer + 2);
+        k_r_d2f<<<cgrid(n), kRedThreads, 0, s>>>(n, R, r64, i64, rf, if_, cr, ci);
+        k_r_inner_init<<<1, 1, 0, s>>>(S, R, inner * inner, hi);
+        k_c_setup<float><<<cgrid(n), kRedThreads, 0, s>>>(n, rf, if_, nullptr, nullptr, wk, wk + n, wk + 2 * n,
+                                                           wk + 3 * n, w->irf, w->iif, S, h->partials, &R->active);
+        return cudaGetLastError();
+      });
+    if (e == cudaSuccess) e = chain_while(ob, hi, &ib);
+    if (e == cudaSuccess)
+      e = chain_segment(ib, G->cap, [&](cudaStream_t s) {
+        const int64_t nn = n;
+        float *rr_ = wk, *ri_ = wk + nn, *pr = wk + 2 * nn, *pi = wk + 3 * nn, *qr = wk + 4 * nn, *qi = wk + 5 * nn;
+        for (int k = 0; k < chunk; ++k) {
+          cudaError_t ee = complex_apply_done<float>(h, omega, pr, pi, qr, qi, &S->done, s);
+          if (ee != cudaSuccess) return ee;
+          k_c_alpha<float><<<cgrid(nn), kRedThreads, 0, s>>>(nn, pr, pi, qr, qi, S, h->partials);
+          k_c_update<float><<<cgrid(nn), kRedThreads, 0, s>>>(nn, cr, ci, rr_, ri_, pr, pi, qr, qi, w->irf, w->iif,
+                                                              S, h->partials);
+          k_c_dir<float><<<cgrid(nn), kRedThreads, 0, s>>>(nn, rr_, ri_, w->irf, w->iif, pr, pi, S);
+        }
+        k_c_cond<<<1, 1, 0, s>>>(S, hi, unit);
+        return cudaGetLastError();
+      });
+    if (e == cudaSuccess)
+      e = chain_segment(ob, G->cap, [&](cudaStream_t s) {
+        k_r_accum<<<cgrid(n), kRedThreads, 0, s>>>(n, R, S, cr, ci, xr, xi);
+        return cudaGetLastError();
+      });
+    if (e == cudaSuccess)
+      e = chain_segment(c, G->cap, [&](cudaStream_t s) {
+        return cudaMemcpyAsync(G->hR, R, sizeof(CRefine), cudaMemcpyDeviceToHost, s);
+      });
+  }
+  if (e == cudaSuccess)
+    e = chain_segment(c, G->cap, [&](cudaStream_t s) {
+      return cudaMemcpyAsync(w->hS, S, sizeof(CScalars), cudaMemcpyDeviceToHost, s);
+    });
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&G->exec, top, 0);
+  cudaGraphDestroy(top);
+  if (e != cudaSuccess) {
+    G->exec = nullptr;
+    h->err = std::string("solve graph construction failed: ") + cudaGetErrorString(e);
+    return HC_ECUDA;
+  }
+  G->precision = prm->precision;
+  G->maxit = prm->maxit;
+  G->max_outer = prm->max_outer;
+  G->chunk = chunk;
+  G->omega = omega;
+  G->rtol = prm->rtol;
+  G->atol = prm->atol;
+  G->inner = prm->inner_rtol;
+  G->ptr[0] = br;
+  G->ptr[1] = bi;
+  G->ptr[2] = xr;
+  G->ptr[3] = xi;
+  return HC_OK;
+}
+
+static int default_chunk(int64_t n) { return n < 200000 ? 16 : 8; }
+
+hc_status complex_graph_launch(hcop* h, const hc_solve_params* prm, double omega, const double* br,
+                               const double* bi, double* xr, double* xi, int chunk) {
+  if (h->type != HC_HEX) {
+    h->err = "complex solves: structured hex grids only in this build";
+    return HC_ENOTSUP;
+  }
+  hc_status st = complex_prepare(h, omega);
+  if (st != HC_OK) return st;
+  st = complex_vectors(h);
+  if (st != HC_OK) return st;
+  if (chunk <= 0) chunk = default_chunk(h->ndof);
+  ComplexGraph* G = cgraph(h);
+  const bool same = G->exec && G->precision == prm->precision && G->maxit == prm->maxit &&
+                    G->max_outer == prm->max_outer && G->chunk == chunk && G->omega == omega && G->rtol == prm->rtol &&
+                    G->atol == prm->atol && G->inner == prm->inner_rtol && G->ptr[0] == br && G->ptr[1] == bi &&
+                    G->ptr[2] == xr && G->ptr[3] == xi;
+  if (!same) {
+    // warm the launch-shape caches outside of capture
+    HC_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    st = complex_graph_build(h, prm, omega, br, bi, xr, xi, chunk);
+    if (st != HC_OK) return st;
+  }
+  HC_CUDA_TRY(h, cudaGraphLaunch(G->exec, h->stream));
+  return HC_OK;
+}
+
+hc_status complex_graph_result(hcop* h, hc_solve_info* info) {
+  ComplexWork* w = static_cast<ComplexWork*>(h->cwork);
+  ComplexGraph* G = w ? static_cast<ComplexGraph*>(w->graph) : nullptr;
+  if (!G || !G->exec) {
+    h->err = "no graph-driven solve has been launched on this handle";
+    return HC_EINVAL;
+  }
+  HC_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  std::memset(info, 0, sizeof(*info));
+  const CScalars* hs = w->hS;
+  if (G->precision == HC_FP64) {
+    info->status = hs->status;
+    info->iterations = hs->it;
+    info->outer_iterations = 1;
+    info->rel_residual = hs->bb > 0 ? std::sqrt(hs->rr / hs->bb) : std::sqrt(hs->rr);
+  } else {
+    const CRefine* R = G->hR;
+    info->status = R->status;
+    info->iterations = R->total;
+    info->outer_iterations = R->outer;
+    info->rel_residual = R->bn > 0 ? R->rn / R->bn : R->rn;
+  }
+  return (hc_status)info->status;
+}
+
+template cudaError_t complex_apply<double>(hcop*, double, const double*, const double*, double*, double*,
+                                           cudaStream_t);
+template cudaError_t complex_apply<float>(hcop*, double, const float*, const float*, float*, float*, cudaStream_t);
+
+}  // namespace hc

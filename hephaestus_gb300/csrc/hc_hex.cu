@@ -70,7 +70,7 @@ __device__ double q1d(int tr, int tc, const double* vr, const double* vc) {
 }
 
 template <int P>
-__global__ void hex_diag_kernel(HexDev d, double* __restrict__ diag) {
+__global__ void hex_diag_kernel(HexDev d, double* __restrict__ diag, double ms, double cs) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= d.ne) return;
   constexpr int C = P + 1, O = P;
@@ -144,21 +144,23 @@ __global__ void hex_diag_kernel(HexDev d, double* __restrict__ diag) {
           if (comp == 0) g = gdof<P, 0>(d, ex, ey, ez, a, b, c);
           else if (comp == 1) g = gdof<P, 1>(d, ex, ey, ez, a, b, c);
           else g = gdof<P, 2>(d, ex, ey, ez, a, b, c);
-          atomicAdd(diag + g, mv + cv);
+          atomicAdd(diag + g, ms * mv + cs * cv);
         }
   }
 }
 
-cudaError_t hex_diag(const HexDev& d, double* diag, cudaStream_t s) {
+cudaError_t hex_diag_scaled(const HexDev& d, double* diag, double ms, double cs, cudaStream_t s) {
   const int blocks = (int)((d.ne + 127) / 128);
   switch (d.p) {
-    case 1: hex_diag_kernel<1><<<blocks, 128, 0, s>>>(d, diag); break;
-    case 2: hex_diag_kernel<2><<<blocks, 128, 0, s>>>(d, diag); break;
-    case 3: hex_diag_kernel<3><<<blocks, 128, 0, s>>>(d, diag); break;
+    case 1: hex_diag_kernel<1><<<blocks, 128, 0, s>>>(d, diag, ms, cs); break;
+    case 2: hex_diag_kernel<2><<<blocks, 128, 0, s>>>(d, diag, ms, cs); break;
+    case 3: hex_diag_kernel<3><<<blocks, 128, 0, s>>>(d, diag, ms, cs); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }
+
+cudaError_t hex_diag(const HexDev& d, double* diag, cudaStream_t s) { return hex_diag_scaled(d, diag, 1.0, 1.0, s); }
 
 void hex_tile_table(int p, int nx, int ny, std::vector<int>& tab) {
   if (p == 1) build_tile_table<1>(nx, ny, tab);

@@ -102,6 +102,7 @@ struct hcop {
   double* tetK64 = nullptr;            // ne * L * L element matrices (FP64)
   float* tetK32 = nullptr;             // FP32 copy
   int* tab = nullptr;                  // brick tile table of the apply kernel
+  void* cwork = nullptr;               // complex (frequency-domain) work space, hc_complex.cu
 
   hc::HexDev hexdev() const {
     hc::HexDev d;
@@ -137,6 +138,8 @@ template <typename T>
 cudaError_t hex_apply(const HexDev& d, const T* fac, const T* x, T* y, double mscale, double cscale,
                       bool masked, KrylovScalars* S, double* partials, cudaStream_t s, bool y_zero_free);
 cudaError_t hex_diag(const HexDev& d, double* diag, cudaStream_t s);
+// diag += mscale * diag(M) + cscale * diag(dt C) (the two parts of hex_diag, scaled)
+cudaError_t hex_diag_scaled(const HexDev& d, double* diag, double mscale, double cscale, cudaStream_t s);
 // tile table of the brick kernel for order p on an nx x ny grid (host)
 void hex_tile_table(int p, int nx, int ny, std::vector<int>& tab);
 
@@ -157,6 +160,21 @@ cudaError_t tet_apply_launch(const hcop* h, const T* K, const T* x, T* y, int nr
 // pq = p.q over all dofs, then alpha = rz / pq (PCG mode of operators without a fused energy)
 template <typename T>
 cudaError_t dot_alpha(int64_t n, const T* p, const T* q, KrylovScalars* S, double* partials, cudaStream_t s);
+
+// fused complex apply, orders 1-2 (hc_hex_cplx.cuh, instantiated in hc_hex_p{1,2}.cu):
+// y_r += C x_r - omega M x_i, y_i += C x_i + omega M x_r with the curl factor
+// scaled by cscale; skipped when *done != 0
+template <typename T, int P>
+cudaError_t hex_launch_cplx_p(const HexDev& d, const T* fac, const T* xr, const T* xi, T* yr, T* yi, T omega,
+                              T cs, bool masked, const int* done, cudaStream_t s);
+// ---- hc_complex.cu ----
+// y = (I-P) x + P (C_nu + i omega M_sigma) P x on planar (re, im) vectors
+template <typename T>
+cudaError_t complex_apply(hcop* h, double omega, const T* xr, const T* xi, T* yr, T* yi, cudaStream_t s);
+// COCG with complex Jacobi (FP64, or FP32 inner in FP64 refinement)
+hc_status complex_solve_device(hcop* h, const hc_solve_params* prm, double omega, const double* br,
+                               const double* bi, double* xr, double* xi, hc_solve_info* info);
+void complex_free(hcop* h);
 
 // ---- hc_krylov.cu ----
 cudaError_t diag_finish(int64_t n, const uint8_t* ess, double* d, double* dinv, float* dinvf, double* sd,

@@ -312,6 +312,28 @@ class HCurlOperator:
                                             _dev_ptr(b, "float64")), self.h)
         return b
 
+    # -- frequency domain: C_nu + i omega M_sigma (ComplexMaxwellOperator, eps = 0) --
+    def MultComplex(self, omega, x):
+        """y = J x for the eliminated complex operator, complex host vectors."""
+        x = np.asarray(x, dtype=np.complex128)
+        xb = np.ascontiguousarray(np.concatenate([x.real, x.imag]))
+        yb = np.empty_like(xb)
+        N.check(N.lib().hc_mult_complex(self.h, float(omega), _ptr(xb), _ptr(yb)), self.h)
+        n = self.ndof
+        return yb[:n] + 1j * yb[n:]
+
+    def MultComplexDevice(self, omega, xr, xi, yr, yi):
+        """Planar device tensors (all float64 or all float32)."""
+        import torch
+
+        if xr.dtype == torch.float64:
+            f, t = N.lib().hc_mult_complex_device, "float64"
+        else:
+            f, t = N.lib().hc_mult_complex_device_f32, "float32"
+        N.check(f(self.h, float(omega), _dev_ptr(xr, t), _dev_ptr(xi, t), _dev_ptr(yr, t), _dev_ptr(yi, t)),
+                self.h)
+        return yr, yi
+
     def LanczosLmax(self, steps=20):
         v = C.c_double(0)
         N.check(N.lib().hc_lanczos_lmax(self.h, steps, C.byref(v)), self.h)
@@ -383,3 +405,85 @@ class GpuHCurlPCGSolver:
         return {"status": N.STATUS_NAMES[i.status], "iterations": i.iterations,
                 "outer_iterations": i.outer_iterations, "applies": i.applies,
                 "rel_residual": i.rel_residual, "lmax": i.lmax}
+
+
+class GpuComplexCOCGSolver(GpuHCurlPCGSolver):
+    """COCG on J = P (C_nu + i omega M_sigma) P + (I - P) with the complex
+    Jacobi preconditioner: the solve of ComplexMaxwellOperator::Solve
+    (src/formulations/ComplexMaxwell/complex_maxwell_formulation.cpp:171-222)
+    with an iterative solver in place of SuperLU.  Options as
+    GpuHCurlPCGSolver (Precision 'fp64' | 'mixed'); the preconditioner is
+    always Jacobi."""
+
+    def __init__(self, params=None, op=None, omega=0.0):
+        params = dict(params or {})
+        params["Preconditioner"] = "jacobi"
+        super().__init__(params, op)
+        self.omega = float(omega)
+
+    def Mult(self, b, x):
+        """Solve J x = b; b, x complex host arrays (x: initial guess, updated in place)."""
+        op = self.op
+        if not (isinstance(x, np.ndarray) and x.dtype == np.complex128):
+            raise TypeError("x must be a complex128 array (updated in place)")
+        b = np.asarray(b, dtype=np.complex128)
+        bb = np.ascontiguousarray(np.concatenate([b.real, b.imag]))
+        xb = np.ascontiguousarray(np.concatenate([x.real, x.imag]))
+        st = N.lib().hc_solve_complex(op.h, C.byref(self.p), self.omega, _ptr(bb), _ptr(xb), C.byref(self.info))
+        self._check(st)
+        n = op.ndof
+        x[:] = xb[:n] + 1j * xb[n:]
+        return x
+
+    def MultGraph(self, br, bi, xr, xi):
+        """Enqueue the graph-driven solve (planar float64 device tensors); the
+        result is read by Finish().  The graph is reused while the tensors stay
+        the same."""
+        op = self.op
+        st = N.lib().hc_solve_complex_graph(op.h, C.byref(self.p), self.omega, _dev_ptr(br, "float64"),
+                                            _dev_ptr(bi, "float64"), _dev_ptr(xr, "float64"),
+                                            _dev_ptr(xi, "float64"))
+        if st != N.HC_OK:
+            raise N.HcError(st, N.last_error(op.h))
+        return xr, xi
+
+    def Finish(self):
+        """Wait for the graph-driven solve of MultGraph and record its report."""
+        self._check(N.lib().hc_graph_solve_info(self.op.h, C.byref(self.info)))
+        return self.result
+
+    def MultDevice(self, br, bi, xr, xi):
+        """Planar float64 device tensors (xr, xi updated in place)."""
+        op = self.op
+        st = N.lib().hc_solve_complex_device(op.h, C.byref(self.p), self.omega, _dev_ptr(br, "float64"),
+                                             _dev_ptr(bi, "float64"), _dev_ptr(xr, "float64"),
+                                             _dev_ptr(xi, "float64"), C.byref(self.info))
+        self._check(st)
+        return xr, xi
+
+
+def solve_complex_batch(solvers, rhs, sols):
+    """Run several GpuComplexCOCGSolver solves at once (hc_solve_complex_batch).
+
+    solvers: list of GpuComplexCOCGSolver (same parameters; each operator
+    should have its own stream); rhs / sols: lists of (re, im) float64 device
+    tensors.  Returns the list of result dicts.
+    """
+    n = len(solvers)
+    if n == 0:
+        return []
+    hs = (C.c_void_p * n)(*[s.op.h.value for s in solvers])
+    om = (C.c_double * n)(*[s.omega for s in solvers])
+    br = (C.c_void_p * n)(*[_dev_ptr(b[0], "float64").value for b in rhs])
+    bi = (C.c_void_p * n)(*[_dev_ptr(b[1], "float64").value for b in rhs])
+    xr = (C.c_void_p * n)(*[_dev_ptr(x[0], "float64").value for x in sols])
+    xi = (C.c_void_p * n)(*[_dev_ptr(x[1], "float64").value for x in sols])
+    infos = (N.SolveInfo * n)()
+    st = N.lib().hc_solve_complex_batch(n, hs, C.byref(solvers[0].p), om, br, bi, xr, xi, infos)
+    if st not in (N.HC_OK, N.HC_NOT_CONVERGED, N.HC_BREAKDOWN):
+        raise N.HcError(st, N.last_error(solvers[0].op.h))
+    out = []
+    for s, i in zip(solvers, infos):
+        s.info = i
+        out.append(s.result)
+    return out

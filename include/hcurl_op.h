@@ -197,6 +197,48 @@ int32_t hc_elem_type(const hcop_t* h);
  * rows/columns in the local dof order of the basis.                        */
 hc_status hc_tet_element_matrix(hcop_t* h, int64_t e, double* out);
 
+/* ---- frequency domain: A = C_nu + i omega M_sigma ------------------------------
+ * The complex operator of ComplexMaxwellOperator::Solve
+ * (src/formulations/ComplexMaxwell/complex_maxwell_formulation.cpp:171-222:
+ * CurlCurlIntegrator in the real part, VectorFEMassIntegrator(omega sigma) in
+ * the imaginary part) with permittivity 0 (eddy-current limit).  C_nu is the
+ * curl-curl form with the handle's nu alone (no dt), M_sigma the mass form with
+ * its sigma; after elimination J = P A P + (I - P).  Structured hex grids.
+ * Host vectors use the real-then-imaginary block layout of MFEM's
+ * ComplexOperator ([re | im], 2 n_dof doubles); device forms take planar
+ * re/im arrays.  omega >= 0.                                                */
+hc_status hc_mult_complex(hcop_t* h, double omega, const double* x, double* y);
+hc_status hc_mult_complex_device(hcop_t* h, double omega, const double* xr, const double* xi, double* yr,
+                                 double* yi);
+hc_status hc_mult_complex_device_f32(hcop_t* h, double omega, const float* xr, const float* xi, float* yr,
+                                     float* yi);
+/* Solve J x = b by COCG (conjugate orthogonal CG: bilinear u^T v products on
+ * the complex-symmetric J) with the complex Jacobi preconditioner, in FP64
+ * (HC_FP64) or as FP32 inner COCG inside FP64 iterative refinement
+ * (HC_MIXED).  Replaces the SuperLU solve of complex_maxwell_formulation.cpp:209-218.
+ * precond must be HC_PRECOND_JACOBI; x holds the initial guess.            */
+hc_status hc_solve_complex(hcop_t* h, const hc_solve_params* prm, double omega, const double* b, double* x,
+                           hc_solve_info* info);
+hc_status hc_solve_complex_device(hcop_t* h, const hc_solve_params* prm, double omega, const double* br,
+                                  const double* bi, double* xr, double* xi, hc_solve_info* info);
+/* Graph-driven form of hc_solve_complex_device: the COCG loop, and for
+ * HC_MIXED the refinement loop around it, run inside one CUDA graph whose
+ * loops are conditional WHILE nodes with device-side stopping tests (and a
+ * hard trip bound), so a solve needs no host round trip per iteration.
+ * Enqueues on the handle's stream and returns; hc_graph_solve_info
+ * synchronises that stream and reports the solve.  The graph is built on the
+ * first call and reused while the arguments (pointers included) stay the same. */
+hc_status hc_solve_complex_graph(hcop_t* h, const hc_solve_params* prm, double omega, const double* br,
+                                 const double* bi, double* xr, double* xi);
+hc_status hc_graph_solve_info(hcop_t* h, hc_solve_info* info);
+/* n independent complex solves (config-4 style batches of uneven problems):
+ * every graph is enqueued first, then all are collected, so solves on
+ * handles with distinct streams (hc_set_stream) run concurrently.  info[i]
+ * gets each solve's report; returns the first non-OK status.               */
+hc_status hc_solve_complex_batch(int32_t n, hcop_t* const* hs, const hc_solve_params* prm, const double* omega,
+                                 const double* const* br, const double* const* bi, double* const* xr,
+                                 double* const* xi, hc_solve_info* info);
+
 /* ---- linear solve --------------------------------------------------------- */
 /* Solve J x = b for x (x holds the initial guess on entry).  Replaces the
  * HyprePCG solve of HCurlFormulation::ConstructJacobianSolver
