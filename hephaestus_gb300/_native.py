@@ -17,7 +17,7 @@ HC_OK, HC_EINVAL, HC_ENOMEM, HC_ECUDA, HC_NOT_CONVERGED, HC_BREAKDOWN, HC_TIMEOU
 STATUS_NAMES = ["OK", "EINVAL", "ENOMEM", "ECUDA", "NOT_CONVERGED", "BREAKDOWN", "TIMEOUT", "ENOTSUP"]
 HC_HEX, HC_TET = 0, 1
 HC_FP64, HC_FP32, HC_MIXED = 0, 1, 2
-HC_PRECOND_NONE, HC_PRECOND_JACOBI, HC_PRECOND_CHEBYSHEV = 0, 1, 2
+HC_PRECOND_NONE, HC_PRECOND_JACOBI, HC_PRECOND_CHEBYSHEV, HC_PRECOND_AUX = 0, 1, 2, 3
 
 
 class NativeUnavailable(RuntimeError):
@@ -96,6 +96,7 @@ _SIGS = {
     "hc_mult": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "hc_apply_form": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "hc_add_weak_curlcurl": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]),
+    "hc_add_weak_curlcurl_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]),
     "hc_diag": (C.c_int, [C.c_void_p, C.c_void_p]),
     "hc_mult_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "hc_mult_device_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),

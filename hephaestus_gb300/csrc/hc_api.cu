@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -125,7 +126,62 @@ void build_tab1d(int p, Tab1D<double>* t) {
 }
 }  // namespace hc
 
+namespace hc {
+cudaError_t dmalloc(const hcop* h, void** p, size_t bytes) {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    // keep freed blocks in the pool instead of returning them to the driver at
+    // every synchronisation (a process-local setting of this device's pool)
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t thr = ~0ull;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+  });
+  *p = nullptr;
+  if (bytes == 0) bytes = 16;
+  return cudaMallocAsync(p, bytes, h->stream);
+}
+void dfree(const hcop* h, void* p) {
+  if (p) cudaFreeAsync(p, h->stream);
+}
+namespace {
+std::mutex g_pin_mu;
+std::vector<void*> g_pin_free;
+}  // namespace
+void* pinned_get(size_t bytes) {
+  if (bytes > 4096) return nullptr;
+  std::lock_guard<std::mutex> lk(g_pin_mu);
+  if (!g_pin_free.empty()) {
+    void* p = g_pin_free.back();
+    g_pin_free.pop_back();
+    std::memset(p, 0, 4096);
+    return p;
+  }
+  void* p = nullptr;
+  if (cudaMallocHost(&p, 4096) != cudaSuccess) return nullptr;
+  std::memset(p, 0, 4096);
+  return p;
+}
+void pinned_put(void* p) {
+  if (!p) return;
+  std::lock_guard<std::mutex> lk(g_pin_mu);
+  g_pin_free.push_back(p);
+}
+}  // namespace hc
+
 using namespace hc;
+
+// The 1-D tables in constant memory are uploaded once per process (handles
+// may be created from several host threads).
+static bool tables_ready() {
+  static std::mutex mu;
+  static bool ok = false;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!ok) ok = upload_tables() == cudaSuccess;
+  return ok;
+}
 
 static hc_status fail_create(hcop* h, const std::string& msg, hc_status st) {
   g_create_err = msg;
@@ -136,10 +192,10 @@ static hc_status fail_create(hcop* h, const std::string& msg, hc_status st) {
 static bool alloc_common(hcop* h) {
   const int64_t N = h->ndof;
   auto ok = [](cudaError_t e) { return e == cudaSuccess; };
-  return ok(cudaMalloc((void**)&h->ess, N)) && ok(cudaMalloc((void**)&h->diag, N * 8)) &&
-         ok(cudaMalloc((void**)&h->dinv, N * 8)) && ok(cudaMalloc((void**)&h->dinvf, N * 4)) &&
-         ok(cudaMalloc((void**)&h->sdinv, N * 8)) && ok(cudaMalloc((void**)&h->sdinvf, N * 4)) &&
-         ok(cudaMalloc((void**)&h->xbuf, N * 8)) && ok(cudaMalloc((void**)&h->ybuf, N * 8));
+  return ok(dmalloc(h, (void**)&h->ess, N)) && ok(dmalloc(h, (void**)&h->diag, N * 8)) &&
+         ok(dmalloc(h, (void**)&h->dinv, N * 8)) && ok(dmalloc(h, (void**)&h->dinvf, N * 4)) &&
+         ok(dmalloc(h, (void**)&h->sdinv, N * 8)) && ok(dmalloc(h, (void**)&h->sdinvf, N * 4)) &&
+         ok(dmalloc(h, (void**)&h->xbuf, N * 8)) && ok(dmalloc(h, (void**)&h->ybuf, N * 8));
 }
 
 // Tetrahedral mesh: host topology + closed-form FP64 element matrices on the device.
@@ -169,23 +225,20 @@ static hc_status create_tet(const hc_problem_desc* desc, hcop_t** out) {
   if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return fail_create(h, "hc_create: no CUDA device available", HC_ECUDA);
   const size_t need = (size_t)h->ne * L * L * 12 + (size_t)h->ne * L * 4 + (size_t)N * (1 + 8 * 3 + 4 * 2 + 8 * 8);
   if (need > fr) return fail_create(h, "hc_create: problem exceeds free device memory", HC_ENOMEM);
-  static bool tables_ok = false;
-  if (!tables_ok) {
-    if (upload_tables() != cudaSuccess) return fail_create(h, "hc_create: constant table upload failed", HC_ECUDA);
-    tables_ok = true;
-  }
+  if (!tables_ready()) return fail_create(h, "hc_create: constant table upload failed", HC_ECUDA);
   if (!alloc_common(h)) return fail_create(h, "hc_create: device allocation failed", HC_ENOMEM);
-  cudaMemcpy(h->ess, h->ess_host.data(), N, cudaMemcpyHostToDevice);
+  cudaMemcpyAsync(h->ess, h->ess_host.data(), N, cudaMemcpyHostToDevice, h->stream);
   cudaError_t e = tet_setup_device(h, desc, edofs, sv);
   if (e == cudaErrorInvalidValue && h->err.empty())
     return fail_create(h, "hc_create: degenerate (zero-volume) tet", HC_EINVAL);
   if (e != cudaSuccess) return fail_create(h, "hc_create: " + h->err + " " + cudaGetErrorString(e), HC_ECUDA);
-  e = diag_finish(N, h->ess, h->diag, h->dinv, h->dinvf, h->sdinv, h->sdinvf, nullptr);
+  e = diag_finish(N, h->ess, h->diag, h->dinv, h->dinvf, h->sdinv, h->sdinvf, h->stream);
   if (e == cudaErrorInvalidValue)
     return fail_create(h, "hc_create: operator diagonal is not positive (nu = 0 and sigma = 0 somewhere?)",
                        HC_EINVAL);
   if (e != cudaSuccess) return fail_create(h, std::string("hc_create: ") + cudaGetErrorString(e), HC_ECUDA);
   if (ensure_scalars(h) != cudaSuccess) return fail_create(h, "hc_create: scalar allocation failed", HC_ENOMEM);
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) return fail_create(h, "hc_create: setup failed", HC_ECUDA);
   *out = h;
   return HC_OK;
 }
@@ -218,32 +271,25 @@ hc_status hc_get_ess_mask(const hcop_t* h, uint8_t* mask) {
 
 hc_status hc_set_stream(hcop_t* h, void* stream) {
   if (!h) return HC_EINVAL;
+  // everything queued on the old stream completes before the handle moves
+  HC_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   h->stream = (cudaStream_t)stream;
   return HC_OK;
 }
 
 void hc_destroy(hcop_t* h) {
   if (!h) return;
+  // work still queued on the handle's stream may read these buffers (and copy
+  // into the pinned scalars): let it finish, on this stream only
+  cudaStreamSynchronize(h->stream);
   complex_free(h);
-  cudaFree(h->fac);
-  cudaFree(h->facf);
-  cudaFree(h->ess);
-  cudaFree(h->diag);
-  cudaFree(h->dinv);
-  cudaFree(h->dinvf);
-  cudaFree(h->sdinv);
-  cudaFree(h->sdinvf);
-  cudaFree(h->scal);
-  cudaFreeHost(h->hscal);
-  cudaFree(h->partials);
-  cudaFree(h->work);
-  cudaFree(h->xbuf);
-  cudaFree(h->ybuf);
-  cudaFree(h->verts);
-  cudaFree(h->tet_edofs);
-  cudaFree(h->tetK64);
-  cudaFree(h->tetK32);
-  cudaFree(h->tab);
+  auxmg_free(h);
+  for (void* p : {(void*)h->fac, (void*)h->facf, (void*)h->ess, (void*)h->diag, (void*)h->dinv, (void*)h->dinvf,
+                  (void*)h->sdinv, (void*)h->sdinvf, (void*)h->scal, (void*)h->partials, h->work, (void*)h->xbuf,
+                  (void*)h->ybuf, (void*)h->verts, (void*)h->tet_edofs, (void*)h->tetK64, (void*)h->tetK32,
+                  (void*)h->tab})
+    dfree(h, p);
+  pinned_put(h->hscal);
   delete h;
 }
 
@@ -391,12 +437,8 @@ hc_status hc_create(const hc_problem_desc* desc, hcop_t** out) {
   }
 
   // ---- upload ----
-  static bool tables_ok = false;
-  if (!tables_ok) {
-    if (upload_tables() != cudaSuccess) return fail_create(h, "hc_create: constant table upload failed", HC_ECUDA);
-    tables_ok = true;
-  }
-  auto alloc = [&](void** p, size_t b) { return cudaMalloc(p, b) == cudaSuccess; };
+  if (!tables_ready()) return fail_create(h, "hc_create: constant table upload failed", HC_ECUDA);
+  auto alloc = [&](void** p, size_t b) { return dmalloc(h, p, b) == cudaSuccess; };
   if (!alloc((void**)&h->fac, fac.size() * 8) || !alloc((void**)&h->facf, facf.size() * 4) ||
       !alloc((void**)&h->ess, N) || !alloc((void**)&h->diag, N * 8) || !alloc((void**)&h->dinv, N * 8) ||
       !alloc((void**)&h->dinvf, N * 4) || !alloc((void**)&h->sdinv, N * 8) || !alloc((void**)&h->sdinvf, N * 4) ||
@@ -405,26 +447,29 @@ hc_status hc_create(const hc_problem_desc* desc, hcop_t** out) {
   {
     std::vector<int> tab;
     hex_tile_table(p, nx, ny, tab);
-    if (cudaMalloc((void**)&h->tab, tab.size() * sizeof(int)) != cudaSuccess)
+    if (dmalloc(h, (void**)&h->tab, tab.size() * sizeof(int)) != cudaSuccess)
       return fail_create(h, "hc_create: device allocation failed", HC_ENOMEM);
-    cudaMemcpy(h->tab, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice);
+    cudaMemcpyAsync(h->tab, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream);
+    // pageable sources: each copy is staged before the call returns
   }
-  if (cudaMalloc((void**)&h->verts, nv * 3 * sizeof(double)) != cudaSuccess)
+  if (dmalloc(h, (void**)&h->verts, nv * 3 * sizeof(double)) != cudaSuccess)
     return fail_create(h, "hc_create: device allocation failed", HC_ENOMEM);
-  cudaMemcpy(h->verts, V, nv * 3 * sizeof(double), cudaMemcpyHostToDevice);
-  cudaMemcpy(h->fac, fac.data(), fac.size() * 8, cudaMemcpyHostToDevice);
-  cudaMemcpy(h->facf, facf.data(), facf.size() * 4, cudaMemcpyHostToDevice);
-  cudaMemcpy(h->ess, h->ess_host.data(), N, cudaMemcpyHostToDevice);
-  cudaMemset(h->diag, 0, N * 8);
+  cudaStream_t cs = h->stream;
+  cudaMemcpyAsync(h->verts, V, nv * 3 * sizeof(double), cudaMemcpyHostToDevice, cs);
+  cudaMemcpyAsync(h->fac, fac.data(), fac.size() * 8, cudaMemcpyHostToDevice, cs);
+  cudaMemcpyAsync(h->facf, facf.data(), facf.size() * 4, cudaMemcpyHostToDevice, cs);
+  cudaMemcpyAsync(h->ess, h->ess_host.data(), N, cudaMemcpyHostToDevice, cs);
+  cudaMemsetAsync(h->diag, 0, N * 8, cs);
   const HexDev d = h->hexdev();
-  if (hex_diag(d, h->diag, nullptr) != cudaSuccess)
+  if (hex_diag(d, h->diag, cs) != cudaSuccess)
     return fail_create(h, "hc_create: diagonal kernel failed", HC_ECUDA);
-  cudaError_t e = diag_finish(N, h->ess, h->diag, h->dinv, h->dinvf, h->sdinv, h->sdinvf, nullptr);
+  cudaError_t e = diag_finish(N, h->ess, h->diag, h->dinv, h->dinvf, h->sdinv, h->sdinvf, cs);
   if (e == cudaErrorInvalidValue)
     return fail_create(h, "hc_create: operator diagonal is not positive (nu = 0 and sigma = 0 somewhere?)",
                        HC_EINVAL);
   if (e != cudaSuccess) return fail_create(h, std::string("hc_create: ") + cudaGetErrorString(e), HC_ECUDA);
   if (ensure_scalars(h) != cudaSuccess) return fail_create(h, "hc_create: scalar allocation failed", HC_ENOMEM);
+  if (cudaStreamSynchronize(cs) != cudaSuccess) return fail_create(h, "hc_create: setup failed", HC_ECUDA);
   *out = h;
   return HC_OK;
 }
@@ -516,6 +561,17 @@ hc_status hc_add_weak_curlcurl(hcop_t* h, const double* x, double* y, double sca
   HC_CUDA_TRY(h, hex_apply<double>(h->hexdev(), h->fac, h->xbuf, h->ybuf, 0.0, scale / h->dt, false, nullptr,
                                    nullptr, h->stream, false));
   return d2h_sync(h, y, h->ybuf);
+}
+
+hc_status hc_add_weak_curlcurl_device(hcop_t* h, const double* x, double* y, double scale) {
+  if (!h || !x || !y || !std::isfinite(scale)) return HC_EINVAL;
+  if (h->type != HC_HEX) {
+    h->err = "hc_add_weak_curlcurl: structured hex grids only in this build";
+    return HC_ENOTSUP;
+  }
+  HC_CUDA_TRY(h, hex_apply<double>(h->hexdev(), h->fac, x, y, 0.0, scale / h->dt, false, nullptr, nullptr,
+                                   h->stream, false));
+  return HC_OK;
 }
 
 hc_status hc_diag(hcop_t* h, double* d) {
@@ -652,7 +708,7 @@ static hc_status check_params(hcop* h, const hc_solve_params* p) {
     h->err = "precision must be HC_FP64 or HC_MIXED";
     return HC_EINVAL;
   }
-  if (p->precond < HC_PRECOND_NONE || p->precond > HC_PRECOND_CHEBYSHEV) {
+  if (p->precond < HC_PRECOND_NONE || p->precond > HC_PRECOND_AUX) {
     h->err = "unknown preconditioner";
     return HC_EINVAL;
   }
@@ -680,6 +736,10 @@ hc_status hc_solve_device(hcop_t* h, const hc_solve_params* prm, const double* b
   hc_solve_info loc{};
   if (!info) info = &loc;
   std::memset(info, 0, sizeof(*info));
+  if (prm->precond == HC_PRECOND_AUX) {
+    st = auxmg_setup(h);
+    if (st != HC_OK) return st;
+  }
   if (prm->precision == HC_MIXED) return mixed_device(h, prm, b, x, info);
   SolveCfg cfg;
   cfg.precond = prm->precond;

@@ -36,7 +36,7 @@ struct CScalars {
   double rtol2, atol2;
   int it, done, status, maxit;
   int trips;  // WHILE-loop trips of a graph-driven solve
-  unsigned int counter[4];
+  unsigned int counter[6];
 };
 
 // ---- complex operator -------------------------------------------------------------
@@ -251,6 +251,136 @@ __global__ void k_c_dir(int64_t n, const T* rr_, const T* ri_, const T* dr, cons
   }
 }
 
+// ---- COCG with a materialised preconditioned residual z = B r (HC_PRECOND_AUX) ------------
+// r = b - q (q == nullptr: x = 0); |b|^2, |r|^2; scalars reset
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+    k_ca_setup(int64_t n, const T* br, const T* bi, const T* qr, const T* qi, T* rr_, T* ri_, CScalars* S,
+               double* partials, const int* active) {
+  if (active && !*active) return;
+  double v[2] = {0, 0}, tot[2];
+  GS_LOOP(k, n) {
+    const double a = qr ? (double)br[k] - (double)qr[k] : (double)br[k];
+    const double b = qr ? (double)bi[k] - (double)qi[k] : (double)bi[k];
+    rr_[k] = (T)a;
+    ri_[k] = (T)b;
+    v[0] += a * a + b * b;
+    v[1] += (double)br[k] * (double)br[k] + (double)bi[k] * (double)bi[k];
+  }
+  block_sum_n<2>(v);
+  if (grid_sum_n<2>(v, partials, &S->counter[0], tot)) {
+    S->rr = tot[0];
+    S->bb = tot[1];
+    S->it = 0;
+    S->done = 0;
+    S->status = HC_NOT_CONVERGED;
+    S->tol2 = fmax(S->rtol2 * tot[1], S->atol2);
+    if (!isfinite(tot[0]) || !isfinite(tot[1])) {
+      S->done = 1;
+      S->status = HC_BREAKDOWN;
+    } else if (tot[0] <= S->tol2) {
+      S->done = 1;
+      S->status = HC_OK;
+    }
+  }
+}
+
+// x += alpha p; r -= alpha q; |r|^2; stopping tests
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+    k_ca_update(int64_t n, T* xr, T* xi, T* rr_, T* ri_, const T* pr, const T* pi, const T* qr, const T* qi,
+                CScalars* S, double* partials) {
+  if (S->done) return;
+  const T ar = (T)S->alpha_r, ai = (T)S->alpha_i;
+  double v[1] = {0}, tot[1];
+  GS_LOOP(k, n) {
+    const T p_r = pr[k], p_i = pi[k];
+    xr[k] += ar * p_r - ai * p_i;
+    xi[k] += ar * p_i + ai * p_r;
+    const T q_r = qr[k], q_i = qi[k];
+    const T a = rr_[k] - (ar * q_r - ai * q_i), b = ri_[k] - (ar * q_i + ai * q_r);
+    rr_[k] = a;
+    ri_[k] = b;
+    v[0] += (double)a * (double)a + (double)b * (double)b;
+  }
+  block_sum_n<1>(v);
+  if (grid_sum_n<1>(v, partials, &S->counter[2], tot)) {
+    S->it += 1;
+    S->rr = tot[0];
+    if (!isfinite(tot[0])) {
+      S->done = 1;
+      S->status = HC_BREAKDOWN;
+    } else if (tot[0] <= S->tol2) {
+      S->done = 1;
+      S->status = HC_OK;
+    } else if (S->it >= S->maxit) {
+      S->done = 1;
+      S->status = HC_NOT_CONVERGED;
+    }
+  }
+}
+
+// z = D^-1 r (complex Jacobi part)
+template <typename T>
+__global__ void k_ca_jz(int64_t n, const T* rr_, const T* ri_, const T* dr, const T* di, T* zr, T* zi,
+                        const CScalars* S) {
+  if (S->done) return;
+  GS_LOOP(k, n) {
+    const T a = rr_[k], b = ri_[k];
+    zr[k] = a * dr[k] - b * di[k];
+    zi[k] = a * di[k] + b * dr[k];
+  }
+}
+
+// rho' = r^T z; beta = rho'/rho (0 on the first call); rho = rho'
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+    k_ca_rho(int64_t n, const T* rr_, const T* ri_, const T* zr, const T* zi, int first, CScalars* S,
+             double* partials) {
+  if (S->done) return;
+  double v[2] = {0, 0}, tot[2];
+  GS_LOOP(k, n) {
+    const double a = rr_[k], b = ri_[k], c = zr[k], d = zi[k];
+    v[0] += a * c - b * d;
+    v[1] += a * d + b * c;
+  }
+  block_sum_n<2>(v);
+  if (grid_sum_n<2>(v, partials, &S->counter[4], tot)) {
+    if (first) {
+      S->beta_r = S->beta_i = 0.0;
+    } else {
+      const double den = S->rho_r * S->rho_r + S->rho_i * S->rho_i;
+      if (!(den > 0.0) || !isfinite(den) || !isfinite(tot[0]) || !isfinite(tot[1])) {
+        S->done = 1;
+        S->status = HC_BREAKDOWN;
+        S->beta_r = S->beta_i = 0.0;
+      } else {
+        S->beta_r = (tot[0] * S->rho_r + tot[1] * S->rho_i) / den;
+        S->beta_i = (tot[1] * S->rho_r - tot[0] * S->rho_i) / den;
+      }
+    }
+    S->rho_r = tot[0];
+    S->rho_i = tot[1];
+  }
+}
+
+// p = z + beta p (first: p = z)
+template <typename T>
+__global__ void k_ca_dir(int64_t n, const T* zr, const T* zi, T* pr, T* pi, int first, const CScalars* S) {
+  if (S->done) return;
+  const T br = (T)S->beta_r, bi = (T)S->beta_i;
+  GS_LOOP(k, n) {
+    if (first) {
+      pr[k] = zr[k];
+      pi[k] = zi[k];
+    } else {
+      const T p_r = pr[k], p_i = pi[k];
+      pr[k] = zr[k] + br * p_r - bi * p_i;
+      pi[k] = zi[k] + br * p_i + bi * p_r;
+    }
+  }
+}
+
 // ---- host drivers -----------------------------------------------------------------------
 struct ComplexWork {
   double *dC = nullptr, *dM = nullptr, *ir = nullptr, *ii = nullptr;
@@ -263,7 +393,7 @@ struct ComplexWork {
   void* graph = nullptr;  // ComplexGraph of the graph-driven solve
 };
 
-static void cgraph_free(ComplexWork* w);
+static void cgraph_free(hcop* h, ComplexWork* w);
 
 static ComplexWork* cwork(hcop* h) {
   if (!h->cwork) h->cwork = new ComplexWork();
@@ -273,16 +403,11 @@ static ComplexWork* cwork(hcop* h) {
 void complex_free(hcop* h) {
   if (!h->cwork) return;
   ComplexWork* w = static_cast<ComplexWork*>(h->cwork);
-  cgraph_free(w);
-  cudaFree(w->dC);
-  cudaFree(w->dM);
-  cudaFree(w->ir);
-  cudaFree(w->ii);
-  cudaFree(w->irf);
-  cudaFree(w->iif);
-  cudaFree(w->S);
-  cudaFreeHost(w->hS);
-  cudaFree(w->vec);
+  cgraph_free(h, w);
+  for (void* p : {(void*)w->dC, (void*)w->dM, (void*)w->ir, (void*)w->ii, (void*)w->irf, (void*)w->iif,
+                  (void*)w->S, w->vec})
+    dfree(h, p);
+  pinned_put(w->hS);
   delete w;
   h->cwork = nullptr;
 }
@@ -291,15 +416,15 @@ static hc_status complex_prepare(hcop* h, double omega) {
   ComplexWork* w = cwork(h);
   const int64_t n = h->ndof;
   if (!w->dC) {
-    if (cudaMalloc((void**)&w->dC, n * 8) != cudaSuccess || cudaMalloc((void**)&w->dM, n * 8) != cudaSuccess ||
-        cudaMalloc((void**)&w->ir, n * 8) != cudaSuccess || cudaMalloc((void**)&w->ii, n * 8) != cudaSuccess ||
-        cudaMalloc((void**)&w->irf, n * 4) != cudaSuccess || cudaMalloc((void**)&w->iif, n * 4) != cudaSuccess ||
-        cudaMalloc((void**)&w->S, sizeof(CScalars)) != cudaSuccess ||
-        cudaMallocHost((void**)&w->hS, sizeof(CScalars)) != cudaSuccess) {
+    if (dmalloc(h, (void**)&w->dC, n * 8) != cudaSuccess || dmalloc(h, (void**)&w->dM, n * 8) != cudaSuccess ||
+        dmalloc(h, (void**)&w->ir, n * 8) != cudaSuccess || dmalloc(h, (void**)&w->ii, n * 8) != cudaSuccess ||
+        dmalloc(h, (void**)&w->irf, n * 4) != cudaSuccess || dmalloc(h, (void**)&w->iif, n * 4) != cudaSuccess ||
+        dmalloc(h, (void**)&w->S, sizeof(CScalars)) != cudaSuccess ||
+        !(w->hS = static_cast<CScalars*>(pinned_get(sizeof(CScalars))))) {
       h->err = "complex work space allocation failed";
       return HC_ENOMEM;
     }
-    cudaMemset(w->S, 0, sizeof(CScalars));
+    cudaMemsetAsync(w->S, 0, sizeof(CScalars), h->stream);
     HexDev d = h->hexdev();
     HC_CUDA_TRY(h, cudaMemsetAsync(w->dC, 0, n * 8, h->stream));
     HC_CUDA_TRY(h, cudaMemsetAsync(w->dM, 0, n * 8, h->stream));
@@ -315,18 +440,20 @@ static hc_status complex_prepare(hcop* h, double omega) {
   return HC_OK;
 }
 
-// work vectors: FP64 path 6n doubles; mixed: 2n doubles (residual) + 2n
-// floats (rhs) + 2n floats (correction) + 6n floats (COCG)
+// work vectors: FP64 path 8n doubles; mixed: 2n doubles (residual) + 2n
+// floats (rhs) + 2n floats (correction) + 8n floats (COCG: r, p, q, z),
+// then 8n doubles for the FP64 polish that follows a stalled refinement
+static size_t polish_offset(int64_t n) { return (size_t)2 * n * sizeof(double) + (size_t)12 * n * 4; }
 static hc_status complex_vectors(hcop* h) {
   ComplexWork* w = cwork(h);
   const int64_t n = h->ndof;
-  const size_t need = std::max((size_t)6 * n * sizeof(double), (size_t)2 * n * sizeof(double) + (size_t)10 * n * 4);
+  const size_t need = polish_offset(n) + (size_t)8 * n * sizeof(double);
   if (w->vec_bytes >= need) return HC_OK;
-  if (w->graph) cgraph_free(w);  // built on the old vectors
-  cudaFree(w->vec);
+  if (w->graph) cgraph_free(h, w);  // built on the old vectors
+  dfree(h, w->vec);
   w->vec = nullptr;
   w->vec_bytes = 0;
-  if (cudaMalloc(&w->vec, need) != cudaSuccess) {
+  if (dmalloc(h, &w->vec, need) != cudaSuccess) {
     h->err = "complex work vectors allocation failed";
     return HC_ENOMEM;
   }
@@ -355,36 +482,93 @@ const float* cdi<float>(ComplexWork* w) {
   return w->iif;
 }
 
-// COCG on A x = b (planar).  wk: 6 n-vectors of T (r, p, q each re/im).
+// One COCG solve's kernels: setup and one iteration, Jacobi (z formed on the
+// fly) or auxiliary-space (z = D^-1 r + G V G^T r / (i omega), materialised).
+// wk: 8 n-vectors of T: r, p, q, z (each re, im).
 template <typename T>
-static hc_status cocg_run(hcop* h, double omega, double rtol, double atol, int maxit, const T* br, const T* bi, T* xr,
-                          T* xi, T* wk, int* iters) {
+struct CocgPlan {
+  hcop* h;
+  double omega;
+  bool aux;
+  T* wk;
+  CScalars* S;
+  int64_t n() const { return h->ndof; }
+  T* r(int c) const { return wk + (0 + c) * n(); }
+  T* p(int c) const { return wk + (2 + c) * n(); }
+  T* q(int c) const { return wk + (4 + c) * n(); }
+  T* z(int c) const { return wk + (6 + c) * n(); }
+  const T* dr() const { return cdr<T>(cwork(h)); }
+  const T* di() const { return cdi<T>(cwork(h)); }
+
+  cudaError_t precond(cudaStream_t s) const {
+    const int64_t nn = n();
+    k_ca_jz<T><<<cgrid(nn), kRedThreads, 0, s>>>(nn, r(0), r(1), dr(), di(), z(0), z(1), S);
+    const float io = (float)(1.0 / omega);
+    const float coef[4] = {0.0f, io, -io, 0.0f};  // (0 - i/omega) (v0 + i v1)
+    return auxmg_apply<T, 2>(h, r(0), r(1), z(0), z(1), coef, &S->done, s);
+  }
+  // r = b - A x (x_zero: r = b), first direction; skipped when active reads 0
+  cudaError_t setup(const T* br, const T* bi, const T* xr, const T* xi, bool x_zero, const int* active,
+                    cudaStream_t s, const int* apply_done = nullptr) const {
+    const int64_t nn = n();
+    if (!x_zero) {
+      cudaError_t e = complex_apply_done<T>(h, omega, xr, xi, q(0), q(1), apply_done, s);
+      if (e != cudaSuccess) return e;
+    }
+    const T* q0 = x_zero ? nullptr : q(0);
+    const T* q1 = x_zero ? nullptr : q(1);
+    if (!aux) {
+      k_c_setup<T><<<cgrid(nn), kRedThreads, 0, s>>>(nn, br, bi, q0, q1, r(0), r(1), p(0), p(1), dr(), di(), S,
+                                                      h->partials, active);
+      return cudaGetLastError();
+    }
+    k_ca_setup<T><<<cgrid(nn), kRedThreads, 0, s>>>(nn, br, bi, q0, q1, r(0), r(1), S, h->partials, active);
+    cudaError_t e = precond(s);
+    if (e != cudaSuccess) return e;
+    k_ca_rho<T><<<cgrid(nn), kRedThreads, 0, s>>>(nn, r(0), r(1), z(0), z(1), 1, S, h->partials);
+    k_ca_dir<T><<<cgrid(nn), kRedThreads, 0, s>>>(nn, z(0), z(1), p(0), p(1), 1, S);
+    return cudaGetLastError();
+  }
+  cudaError_t iterate(T* xr, T* xi, cudaStream_t s) const {
+    const int64_t nn = n();
+    cudaError_t e = complex_apply_done<T>(h, omega, p(0), p(1), q(0), q(1), &S->done, s);
+    if (e != cudaSuccess) return e;
+    k_c_alpha<T><<<cgrid(nn), kRedThreads, 0, s>>>(nn, p(0), p(1), q(0), q(1), S, h->partials);
+    if (!aux) {
+      k_c_update<T><<<cgrid(nn), kRedThreads, 0, s>>>(nn, xr, xi, r(0), r(1), p(0), p(1), q(0), q(1), dr(), di(), S,
+                                                      h->partials);
+      k_c_dir<T><<<cgrid(nn), kRedThreads, 0, s>>>(nn, r(0), r(1), dr(), di(), p(0), p(1), S);
+      return cudaGetLastError();
+    }
+    k_ca_update<T><<<cgrid(nn), kRedThreads, 0, s>>>(nn, xr, xi, r(0), r(1), p(0), p(1), q(0), q(1), S,
+                                                     h->partials);
+    e = precond(s);
+    if (e != cudaSuccess) return e;
+    k_ca_rho<T><<<cgrid(nn), kRedThreads, 0, s>>>(nn, r(0), r(1), z(0), z(1), 0, S, h->partials);
+    k_ca_dir<T><<<cgrid(nn), kRedThreads, 0, s>>>(nn, z(0), z(1), p(0), p(1), 0, S);
+    return cudaGetLastError();
+  }
+};
+
+// Host-driven COCG on A x = b (planar); wk: 8 n-vectors of T.
+template <typename T>
+static hc_status cocg_run(hcop* h, double omega, bool aux, double rtol, double atol, int maxit, const T* br,
+                          const T* bi, T* xr, T* xi, bool x_zero, T* wk, int* iters) {
   ComplexWork* w = cwork(h);
-  const int64_t n = h->ndof;
   cudaStream_t s = h->stream;
-  T *rr_ = wk, *ri_ = wk + n, *pr = wk + 2 * n, *pi = wk + 3 * n, *qr = wk + 4 * n, *qi = wk + 5 * n;
-  const T *dr = cdr<T>(w), *di = cdi<T>(w);
   CScalars* S = w->S;
   CScalars* hs = w->hS;
+  const CocgPlan<T> plan{h, omega, aux, wk, S};
   std::memset(hs, 0, sizeof(CScalars));
   hs->rtol2 = rtol * rtol;
   hs->atol2 = atol * atol;
   hs->maxit = maxit;
   HC_CUDA_TRY(h, cudaMemcpyAsync(S, hs, sizeof(CScalars), cudaMemcpyHostToDevice, s));
-  HC_CUDA_TRY(h, complex_apply<T>(h, omega, xr, xi, qr, qi, s));
-  k_c_setup<T><<<cgrid(n), kRedThreads, 0, s>>>(n, br, bi, qr, qi, rr_, ri_, pr, pi, dr, di, S, h->partials,
-                                                 nullptr);
-  HC_CUDA_TRY(h, cudaGetLastError());
+  HC_CUDA_TRY(h, plan.setup(br, bi, xr, xi, x_zero, nullptr, s));
   const int chunk = 20;
   int launched = 0;
   for (;;) {
-    for (int k = 0; k < chunk && launched < maxit; ++k, ++launched) {
-      HC_CUDA_TRY(h, complex_apply_done<T>(h, omega, pr, pi, qr, qi, &S->done, s));
-      k_c_alpha<T><<<cgrid(n), kRedThreads, 0, s>>>(n, pr, pi, qr, qi, S, h->partials);
-      k_c_update<T><<<cgrid(n), kRedThreads, 0, s>>>(n, xr, xi, rr_, ri_, pr, pi, qr, qi, dr, di, S, h->partials);
-      k_c_dir<T><<<cgrid(n), kRedThreads, 0, s>>>(n, rr_, ri_, dr, di, pr, pi, S);
-    }
-    HC_CUDA_TRY(h, cudaGetLastError());
+    for (int k = 0; k < chunk && launched < maxit; ++k, ++launched) HC_CUDA_TRY(h, plan.iterate(xr, xi, s));
     HC_CUDA_TRY(h, cudaMemcpyAsync(hs, S, sizeof(CScalars), cudaMemcpyDeviceToHost, s));
     HC_CUDA_TRY(h, cudaStreamSynchronize(s));
     if (hs->done || launched >= maxit) break;
@@ -432,13 +616,19 @@ hc_status complex_solve_device(hcop* h, const hc_solve_params* prm, double omega
   if (st != HC_OK) return st;
   st = complex_vectors(h);
   if (st != HC_OK) return st;
+  const bool aux = prm->precond == HC_PRECOND_AUX;
+  if (aux) {
+    st = auxmg_setup(h);
+    if (st != HC_OK) return st;
+  }
   ComplexWork* w = cwork(h);
   const int64_t n = h->ndof;
   std::memset(info, 0, sizeof(*info));
   cudaStream_t s = h->stream;
   if (prm->precision == HC_FP64) {
     int it = 0;
-    st = cocg_run<double>(h, omega, prm->rtol, prm->atol, prm->maxit, br, bi, xr, xi, (double*)w->vec, &it);
+    st = cocg_run<double>(h, omega, aux, prm->rtol, prm->atol, prm->maxit, br, bi, xr, xi, false, (double*)w->vec,
+                          &it);
     info->status = st;
     info->iterations = it;
     info->outer_iterations = 1;
@@ -471,6 +661,10 @@ hc_status complex_solve_device(hcop* h, const hc_solve_params* prm, double omega
   const double inner = prm->inner_rtol > 0 ? prm->inner_rtol : 1e-4;
   const int max_outer = prm->max_outer > 0 ? prm->max_outer : 50;
   hc_status result = HC_NOT_CONVERGED;
+  // stalled refinement (a step that does not cut the residual by 4x): finish in FP64
+  bool stalled = false;
+  double rn_prev = 0.0;
+  const int inner_cap = std::max(100, prm->maxit / 4);
   for (;;) {
     const double rn = std::sqrt(rn2);
     if (!std::isfinite(rn)) {
@@ -482,11 +676,17 @@ hc_status complex_solve_device(hcop* h, const hc_solve_params* prm, double omega
       break;
     }
     if (outer >= max_outer || total >= prm->maxit) break;
+    if (outer >= 2 && rn > 0.25 * rn_prev) {
+      stalled = true;
+      break;
+    }
+    rn_prev = rn;
     ++outer;
     k_c_d2f<<<g, kRedThreads, 0, s>>>(n, r64, i64, rf, if_, 1.0 / rn);
-    HC_CUDA_TRY(h, cudaMemsetAsync(cr, 0, 2 * n * sizeof(float), s));
+    HC_CUDA_TRY(h, cudaMemsetAsync(cr, 0, 2 * n * sizeof(float), s));  // x = 0 start
     int it = 0;
-    hc_status ist = cocg_run<float>(h, omega, inner, 0.0, prm->maxit - total, rf, if_, cr, ci, wk, &it);
+    hc_status ist = cocg_run<float>(h, omega, aux, inner, 0.0, std::min(prm->maxit - total, inner_cap), rf, if_, cr,
+                                    ci, true, wk, &it);
     total += it;
     if (ist == HC_ECUDA || ist == HC_ENOMEM) return ist;
     k_c_axpy<<<g, kRedThreads, 0, s>>>(n, cr, ci, xr, xi, rn);
@@ -497,6 +697,19 @@ hc_status complex_solve_device(hcop* h, const hc_solve_params* prm, double omega
       result = HC_BREAKDOWN;
       break;
     }
+  }
+  if (stalled && total < prm->maxit) {
+    int it = 0;
+    double* wk64 = (double*)((char*)w->vec + polish_offset(n));
+    const hc_status pst = cocg_run<double>(h, omega, aux, prm->rtol, prm->atol, prm->maxit - total, br, bi, xr, xi,
+                                           false, wk64, &it);
+    total += it;
+    ++outer;
+    if (pst == HC_ECUDA || pst == HC_ENOMEM) return pst;
+    st = residual(&rn2, &bn2);
+    if (st != HC_OK) return st;
+    // the FP64 Krylov's own verdict (recursive residual), as for a plain FP64 solve
+    result = std::isfinite(std::sqrt(rn2)) ? pst : HC_BREAKDOWN;
   }
   info->status = result;
   info->iterations = total;
@@ -578,8 +791,8 @@ static hc_status complex_params(hcop* h, const hc_solve_params* p) {
     h->err = "precision must be HC_FP64 or HC_MIXED";
     return HC_EINVAL;
   }
-  if (p->precond != HC_PRECOND_JACOBI) {
-    h->err = "complex solves take the (complex) Jacobi preconditioner only";
+  if (p->precond != HC_PRECOND_JACOBI && p->precond != HC_PRECOND_AUX) {
+    h->err = "complex solves take the complex Jacobi or the auxiliary-space (Jacobi + gradient) preconditioner";
     return HC_ENOTSUP;
   }
   if (!(p->rtol >= 0.0) || !(p->atol >= 0.0) || p->maxit < 1) {
@@ -671,8 +884,8 @@ namespace hc {
 // one CUDA graph whose loops are conditional WHILE nodes.  Stopping decisions
 // are taken on the device; every loop has a hard trip bound.
 struct CRefine {
-  double rn, bn, tol, rtol, atol;
-  int outer, total, max_outer, maxit, status, active, trips, pad;
+  double rn, bn, tol, rtol, atol, rn_prev;
+  int outer, total, max_outer, maxit, status, active, trips, polish;
 };
 
 __global__ void k_g_init(CScalars* S, double rtol2, double atol2, int maxit) {
@@ -700,7 +913,8 @@ __global__ void k_r_init(CRefine* R, double rtol, double atol, int maxit, int ma
   R->rn = R->bn = 0.0;
   R->maxit = maxit;
   R->max_outer = max_outer;
-  R->outer = R->total = R->trips = R->active = 0;
+  R->outer = R->total = R->trips = R->active = R->polish = 0;
+  R->rn_prev = 0.0;
   R->status = HC_NOT_CONVERGED;
 }
 
@@ -720,9 +934,14 @@ __global__ void k_r_check(CRefine* R, const CScalars* S, cudaGraphConditionalHan
     R->status = HC_OK;
   } else if (R->outer >= R->max_outer || R->total >= R->maxit || t >= max_trips) {
     R->status = HC_NOT_CONVERGED;
+  } else if (R->outer >= 2 && rn > 0.25 * R->rn_prev) {
+    // the FP32 inner solves stopped paying: finish in FP64
+    R->status = HC_NOT_CONVERGED;
+    R->polish = 1;
   } else {
     stop = 0;
   }
+  R->rn_prev = rn;
   R->rn = rn;
   R->active = !stop;
   if (!stop) R->outer += 1;
@@ -751,6 +970,25 @@ __global__ void k_r_inner_init(CScalars* S, const CRefine* R, double rtol2, cuda
   cudaGraphSetConditional(hnd, R->active ? 1u : 0u);
 }
 
+// FP64 polish after a stalled refinement: scalars for a COCG from the current x
+__global__ void k_polish_init(CScalars* S, CRefine* R, double rtol2, double atol2, cudaGraphConditionalHandle hnd) {
+  const int go = (R->polish && R->total < R->maxit) ? 1 : 0;
+  R->polish = go;
+  S->rtol2 = rtol2;
+  S->atol2 = atol2;
+  S->maxit = R->maxit - R->total;
+  S->trips = 0;
+  S->done = go ? 0 : 1;
+  cudaGraphSetConditional(hnd, (unsigned)go);
+}
+__global__ void k_polish_finish(CRefine* R, const CScalars* S) {
+  if (!R->polish) return;
+  R->total += S->it;
+  R->outer += 1;
+  R->status = S->status;
+  R->rn = sqrt(S->rr);
+}
+
 // x += |r| c
 __global__ void k_r_accum(int64_t n, CRefine* R, const CScalars* S, const float* cr, const float* ci, double* xr,
                           double* xi) {
@@ -772,7 +1010,7 @@ struct ComplexGraph {
   CRefine* R = nullptr;
   CRefine* hR = nullptr;
   // arguments the graph was built for
-  int precision = -1, maxit = 0, max_outer = 0, chunk = 0;
+  int precision = -1, precond = -1, maxit = 0, max_outer = 0, chunk = 0;
   double omega = 0, rtol = 0, atol = 0, inner = 0;
   const void* ptr[4] = {nullptr, nullptr, nullptr, nullptr};
 };
@@ -783,13 +1021,14 @@ static ComplexGraph* cgraph(hcop* h) {
   return static_cast<ComplexGraph*>(w->graph);
 }
 
-static void cgraph_free(ComplexWork* w) {
+static void cgraph_free(hcop* h, ComplexWork* w) {
   ComplexGraph* g = static_cast<ComplexGraph*>(w->graph);
   if (!g) return;
+  cudaStreamSynchronize(h->stream);  // no launch of this graph may still be pending
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->cap) cudaStreamDestroy(g->cap);
-  cudaFree(g->R);
-  cudaFreeHost(g->hR);
+  dfree(h, g->R);
+  pinned_put(g->hR);
   delete g;
   w->graph = nullptr;
 }
@@ -801,9 +1040,12 @@ static hc_status complex_graph_build(hcop* h, const hc_solve_params* prm, double
   const int64_t n = h->ndof;
   if (!G->cap) HC_CUDA_TRY(h, cudaStreamCreateWithFlags(&G->cap, cudaStreamNonBlocking));
   if (!G->R) {
-    HC_CUDA_TRY(h, cudaMalloc((void**)&G->R, sizeof(CRefine)));
-    HC_CUDA_TRY(h, cudaMallocHost((void**)&G->hR, sizeof(CRefine)));
-    std::memset(G->hR, 0, sizeof(CRefine));
+    HC_CUDA_TRY(h, dmalloc(h, (void**)&G->R, sizeof(CRefine)));
+    G->hR = static_cast<CRefine*>(pinned_get(sizeof(CRefine)));
+    if (!G->hR) {
+      h->err = "pinned scalar allocation failed";
+      return HC_ENOMEM;
+    }
   }
   if (G->exec) {
     cudaGraphExecDestroy(G->exec);
@@ -815,32 +1057,22 @@ static hc_status complex_graph_build(hcop* h, const hc_solve_params* prm, double
   HC_CUDA_TRY(h, cudaGraphCreate(&top, 0));
   GraphChain c{top, nullptr};
   cudaError_t e = cudaSuccess;
+  const bool aux = prm->precond == HC_PRECOND_AUX;
   if (prm->precision == HC_FP64) {
-    double* wk = (double*)w->vec;
+    const CocgPlan<double> plan{h, omega, aux, (double*)w->vec, S};
     e = chain_segment(c, G->cap, [&](cudaStream_t s) {
       k_g_init<<<1, 1, 0, s>>>(S, prm->rtol * prm->rtol, prm->atol * prm->atol, prm->maxit);
-      cudaError_t ee = complex_apply_done<double>(h, omega, xr, xi, wk + 4 * n, wk + 5 * n, nullptr, s);
-      if (ee != cudaSuccess) return ee;
-      k_c_setup<double><<<cgrid(n), kRedThreads, 0, s>>>(n, br, bi, wk + 4 * n, wk + 5 * n, wk, wk + n, wk + 2 * n,
-                                                          wk + 3 * n, w->ir, w->ii, S, h->partials, nullptr);
-      return cudaGetLastError();
+      return plan.setup(br, bi, xr, xi, false, nullptr, s);
     });
     cudaGraphConditionalHandle hl = 0;
     GraphChain body;
     if (e == cudaSuccess) e = chain_handle(c, &hl);
     if (e == cudaSuccess) e = chain_while(c, hl, &body);
-    // x is updated in place by k_c_update through the work layout below
     if (e == cudaSuccess)
       e = chain_segment(body, G->cap, [&](cudaStream_t s) {
-        const int64_t nn = n;
-        double *rr_ = wk, *ri_ = wk + nn, *pr = wk + 2 * nn, *pi = wk + 3 * nn, *qr = wk + 4 * nn, *qi = wk + 5 * nn;
         for (int k = 0; k < chunk; ++k) {
-          cudaError_t ee = complex_apply_done<double>(h, omega, pr, pi, qr, qi, &S->done, s);
+          cudaError_t ee = plan.iterate(xr, xi, s);
           if (ee != cudaSuccess) return ee;
-          k_c_alpha<double><<<cgrid(nn), kRedThreads, 0, s>>>(nn, pr, pi, qr, qi, S, h->partials);
-          k_c_update<double><<<cgrid(nn), kRedThreads, 0, s>>>(nn, xr, xi, rr_, ri_, pr, pi, qr, qi, w->ir, w->ii,
-                                                               S, h->partials);
-          k_c_dir<double><<<cgrid(nn), kRedThreads, 0, s>>>(nn, rr_, ri_, w->ir, w->ii, pr, pi, S);
         }
         k_c_cond<<<1, 1, 0, s>>>(S, hl, unit);
         return cudaGetLastError();
@@ -852,7 +1084,7 @@ static hc_status complex_graph_build(hcop* h, const hc_solve_params* prm, double
     float* if_ = rf + n;
     float* cr = if_ + n;
     float* ci = cr + n;
-    float* wk = ci + n;
+    const CocgPlan<float> plan{h, omega, aux, ci + n, S};
     CRefine* R = G->R;
     const double inner = prm->inner_rtol > 0 ? prm->inner_rtol : 1e-4;
     const int max_outer = prm->max_outer > 0 ? prm->max_outer : 50;
@@ -873,22 +1105,14 @@ static hc_status complex_graph_build(hcop* h, const hc_solve_params* prm, double
         k_r_check<<<1, 1, 0, s>>>(R, S, ho, max_outer + 2);
         k_r_d2f<<<cgrid(n), kRedThreads, 0, s>>>(n, R, r64, i64, rf, if_, cr, ci);
         k_r_inner_init<<<1, 1, 0, s>>>(S, R, inner * inner, hi);
-        k_c_setup<float><<<cgrid(n), kRedThreads, 0, s>>>(n, rf, if_, nullptr, nullptr, wk, wk + n, wk + 2 * n,
-                                                           wk + 3 * n, w->irf, w->iif, S, h->partials, &R->active);
-        return cudaGetLastError();
+        return plan.setup(rf, if_, nullptr, nullptr, true, &R->active, s);
       });
     if (e == cudaSuccess) e = chain_while(ob, hi, &ib);
     if (e == cudaSuccess)
       e = chain_segment(ib, G->cap, [&](cudaStream_t s) {
-        const int64_t nn = n;
-        float *rr_ = wk, *ri_ = wk + nn, *pr = wk + 2 * nn, *pi = wk + 3 * nn, *qr = wk + 4 * nn, *qi = wk + 5 * nn;
         for (int k = 0; k < chunk; ++k) {
-          cudaError_t ee = complex_apply_done<float>(h, omega, pr, pi, qr, qi, &S->done, s);
+          cudaError_t ee = plan.iterate(cr, ci, s);
           if (ee != cudaSuccess) return ee;
-          k_c_alpha<float><<<cgrid(nn), kRedThreads, 0, s>>>(nn, pr, pi, qr, qi, S, h->partials);
-          k_c_update<float><<<cgrid(nn), kRedThreads, 0, s>>>(nn, cr, ci, rr_, ri_, pr, pi, qr, qi, w->irf, w->iif,
-                                                              S, h->partials);
-          k_c_dir<float><<<cgrid(nn), kRedThreads, 0, s>>>(nn, rr_, ri_, w->irf, w->iif, pr, pi, S);
         }
         k_c_cond<<<1, 1, 0, s>>>(S, hi, unit);
         return cudaGetLastError();
@@ -898,8 +1122,29 @@ static hc_status complex_graph_build(hcop* h, const hc_solve_params* prm, double
         k_r_accum<<<cgrid(n), kRedThreads, 0, s>>>(n, R, S, cr, ci, xr, xi);
         return cudaGetLastError();
       });
+    // FP64 polish (runs only when the refinement stalled)
+    const CocgPlan<double> p64{h, omega, aux, (double*)((char*)w->vec + polish_offset(n)), S};
+    cudaGraphConditionalHandle hp = 0;
+    GraphChain pb;
+    if (e == cudaSuccess) e = chain_handle(c, &hp);
     if (e == cudaSuccess)
       e = chain_segment(c, G->cap, [&](cudaStream_t s) {
+        k_polish_init<<<1, 1, 0, s>>>(S, R, prm->rtol * prm->rtol, prm->atol * prm->atol, hp);
+        return p64.setup(br, bi, xr, xi, false, &R->polish, s, &S->done);
+      });
+    if (e == cudaSuccess) e = chain_while(c, hp, &pb);
+    if (e == cudaSuccess)
+      e = chain_segment(pb, G->cap, [&](cudaStream_t s) {
+        for (int k = 0; k < chunk; ++k) {
+          cudaError_t ee = p64.iterate(xr, xi, s);
+          if (ee != cudaSuccess) return ee;
+        }
+        k_c_cond<<<1, 1, 0, s>>>(S, hp, unit);
+        return cudaGetLastError();
+      });
+    if (e == cudaSuccess)
+      e = chain_segment(c, G->cap, [&](cudaStream_t s) {
+        k_polish_finish<<<1, 1, 0, s>>>(R, S);
         return cudaMemcpyAsync(G->hR, R, sizeof(CRefine), cudaMemcpyDeviceToHost, s);
       });
   }
@@ -915,6 +1160,7 @@ static hc_status complex_graph_build(hcop* h, const hc_solve_params* prm, double
     return HC_ECUDA;
   }
   G->precision = prm->precision;
+  G->precond = prm->precond;
   G->maxit = prm->maxit;
   G->max_outer = prm->max_outer;
   G->chunk = chunk;
@@ -941,9 +1187,14 @@ hc_status complex_graph_launch(hcop* h, const hc_solve_params* prm, double omega
   if (st != HC_OK) return st;
   st = complex_vectors(h);
   if (st != HC_OK) return st;
+  if (prm->precond == HC_PRECOND_AUX) {
+    st = auxmg_setup(h);
+    if (st != HC_OK) return st;
+  }
   if (chunk <= 0) chunk = default_chunk(h->ndof);
   ComplexGraph* G = cgraph(h);
-  const bool same = G->exec && G->precision == prm->precision && G->maxit == prm->maxit &&
+  const bool same = G->exec && G->precision == prm->precision && G->precond == prm->precond &&
+                    G->maxit == prm->maxit &&
                     G->max_outer == prm->max_outer && G->chunk == chunk && G->omega == omega && G->rtol == prm->rtol &&
                     G->atol == prm->atol && G->inner == prm->inner_rtol && G->ptr[0] == br && G->ptr[1] == bi &&
                     G->ptr[2] == xr && G->ptr[3] == xi;

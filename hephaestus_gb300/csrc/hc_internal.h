@@ -103,6 +103,7 @@ struct hcop {
   float* tetK32 = nullptr;             // FP32 copy
   int* tab = nullptr;                  // brick tile table of the apply kernel
   void* cwork = nullptr;               // complex (frequency-domain) work space, hc_complex.cu
+  void* aux = nullptr;                 // auxiliary-space preconditioner, hc_auxmg.cu
 
   hc::HexDev hexdev() const {
     hc::HexDev d;
@@ -125,6 +126,18 @@ struct hcop {
 };
 
 namespace hc {
+// ---- memory (hc_api.cu) ----
+// Device memory of a handle is stream-ordered on the handle's stream
+// (cudaMallocAsync / cudaFreeAsync from the device's default pool): creating,
+// growing or destroying a handle never synchronises the device, so requests
+// come and go while others compute.
+cudaError_t dmalloc(const hcop* h, void** p, size_t bytes);
+void dfree(const hcop* h, void* p);
+// Pinned host blocks (at most 4 KB) from a process-wide pool that is never
+// returned to the driver (cudaFreeHost would synchronise the device).
+void* pinned_get(size_t bytes);
+void pinned_put(void* p);
+
 // ---- hc_hex.cu ----
 cudaError_t upload_tables();
 int hex_apply_blocks(const HexDev& d);
@@ -167,6 +180,16 @@ cudaError_t dot_alpha(int64_t n, const T* p, const T* q, KrylovScalars* S, doubl
 template <typename T, int P>
 cudaError_t hex_launch_cplx_p(const HexDev& d, const T* fac, const T* xr, const T* xi, T* yr, T* yi, T omega,
                               T cs, bool masked, const int* done, cudaStream_t s);
+// ---- hc_auxmg.cu ----
+// gradient-space (auxiliary) preconditioner: setup once per handle (FP32)
+hc_status auxmg_setup(hcop* h);
+void auxmg_free(hcop* h);
+// z += C G V G^T r; NV = 1: z0 += coef[0] (G V G^T r0); NV = 2 (planar complex):
+// z0 += coef[0] v0 + coef[1] v1, z1 += coef[2] v0 + coef[3] v1
+template <typename T, int NV>
+cudaError_t auxmg_apply(const hcop* h, const T* r0, const T* r1, T* z0, T* z1, const float coef[4], const int* done,
+                        cudaStream_t s);
+
 // ---- hc_complex.cu ----
 // y = (I-P) x + P (C_nu + i omega M_sigma) P x on planar (re, im) vectors
 template <typename T>

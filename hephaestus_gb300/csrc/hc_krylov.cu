@@ -285,6 +285,14 @@ __global__ void __launch_bounds__(kRedThreads)
   }
 }
 
+// z = D^-1 r (the Jacobi part of the auxiliary-space preconditioner)
+template <typename T>
+__global__ void k_jz(int64_t n, const T* __restrict__ r, const T* __restrict__ dinv, T* __restrict__ z,
+                     const KrylovScalars* S) {
+  if (S->done) return;
+  GS_LOOP(i, n) z[i] = dinv[i] * r[i];
+}
+
 // Chebyshev iteration (Saad, Iterative Methods for Sparse Linear Systems,
 // Alg. 12.1) on D^-1 J z = D^-1 r, zero start, fixed degree: a fixed SPD
 // polynomial preconditioner when lmax bounds the spectrum of D^-1 J.
@@ -412,25 +420,26 @@ __global__ void k_axpy_f2d(int64_t n, const float* __restrict__ c, double* __res
 // ---------------------------------------------------------------------------
 // host drivers
 // ---------------------------------------------------------------------------
+static_assert(sizeof(KrylovScalars) <= 4096, "pinned scalar blocks are 4 KB");
 cudaError_t ensure_scalars(hcop* h) {
   if (h->scal) return cudaSuccess;
-  cudaError_t e = cudaMalloc(&h->scal, sizeof(KrylovScalars));
+  cudaError_t e = dmalloc(h, (void**)&h->scal, sizeof(KrylovScalars));
   if (e != cudaSuccess) return e;
-  e = cudaMemset(h->scal, 0, sizeof(KrylovScalars));
+  e = cudaMemsetAsync(h->scal, 0, sizeof(KrylovScalars), h->stream);
   if (e != cudaSuccess) return e;
-  e = cudaMallocHost(&h->hscal, sizeof(KrylovScalars));
-  if (e != cudaSuccess) return e;
+  h->hscal = static_cast<KrylovScalars*>(pinned_get(sizeof(KrylovScalars)));
+  if (!h->hscal) return cudaErrorMemoryAllocation;
   const HexDev d = h->hexdev();
   const size_t np = (size_t)std::max(kRedBlocks, hex_apply_blocks(d)) * 4;
-  return cudaMalloc(&h->partials, np * sizeof(double));
+  return dmalloc(h, (void**)&h->partials, np * sizeof(double));
 }
 
 hc_status ensure_work(hcop* h, size_t bytes) {
   if (h->work_bytes >= bytes) return HC_OK;
-  if (h->work) cudaFree(h->work);
+  dfree(h, h->work);  // stream-ordered: queued work on the handle's stream finishes first
   h->work = nullptr;
   h->work_bytes = 0;
-  cudaError_t e = cudaMalloc(&h->work, bytes);
+  cudaError_t e = dmalloc(h, &h->work, bytes);
   if (e != cudaSuccess) {
     h->err = std::string("work space allocation failed: ") + cudaGetErrorString(e);
     return HC_ENOMEM;
@@ -568,12 +577,13 @@ static hc_status pcg_run(hcop* h, const SolveCfg& cfg, const T* b, T* x, T* wk, 
   HC_CUDA_TRY(h, cudaMemcpyAsync(S, hs, sizeof(KrylovScalars), cudaMemcpyHostToDevice, s));
   HC_CUDA_TRY(h, cudaMemsetAsync(p, 0, n * sizeof(T), s));
 
-  const bool jac = cfg.precond != HC_PRECOND_CHEBYSHEV;
+  const bool jac = cfg.precond == HC_PRECOND_JACOBI || cfg.precond == HC_PRECOND_NONE;
   const bool none = cfg.precond == HC_PRECOND_NONE;
+  const bool aux = cfg.precond == HC_PRECOND_AUX;
   // z = C(r) for the Chebyshev preconditioner
   double theta = 0, delta = 0, sigma1 = 0;
   std::vector<double> c1s, c2s;
-  if (!jac) {
+  if (cfg.precond == HC_PRECOND_CHEBYSHEV) {
     const double lmin = cfg.lmax / cfg.cheb_ratio;
     theta = 0.5 * (cfg.lmax + lmin);
     delta = 0.5 * (cfg.lmax - lmin);
@@ -598,6 +608,15 @@ static hc_status pcg_run(hcop* h, const SolveCfg& cfg, const T* b, T* x, T* wk, 
     }
     return cudaGetLastError();
   };
+  // z = B r for the non-Jacobi preconditioners
+  auto precond = [&]() -> cudaError_t {
+    if (aux) {
+      k_jz<T><<<g, kRedThreads, 0, s>>>(n, r, dinv, z, S);
+      const float coef[4] = {1.0f, 0.0f, 0.0f, 0.0f};
+      return auxmg_apply<T, 1>(h, r, nullptr, z, nullptr, coef, &S->done, s);
+    }
+    return cheb();
+  };
 
   // r = b - J x
   HC_CUDA_TRY(h, init_masked<T>(n, h->ess, x, q, s));
@@ -610,7 +629,7 @@ static hc_status pcg_run(hcop* h, const SolveCfg& cfg, const T* b, T* x, T* wk, 
     k_pcg_dir<T, true><<<g, kRedThreads, 0, s>>>(n, r, dj, p, q, h->ess, S, part);
   } else {
     k_pcg_setup<T, false><<<g, kRedThreads, 0, s>>>(n, b, q, r, dinv, S, part);
-    HC_CUDA_TRY(h, cheb());
+    HC_CUDA_TRY(h, precond());
     k_rz_beta<T><<<g, kRedThreads, 0, s>>>(n, r, z, 1, S, part);
     k_pcg_dir<T, false><<<g, kRedThreads, 0, s>>>(n, z, dinv, p, q, h->ess, S, part);
   }
@@ -627,7 +646,7 @@ static hc_status pcg_run(hcop* h, const SolveCfg& cfg, const T* b, T* x, T* wk, 
         k_pcg_dir<T, true><<<g, kRedThreads, 0, s>>>(n, r, dj, p, q, h->ess, S, part);
       } else {
         k_pcg_update<T, false><<<g, kRedThreads, 0, s>>>(n, x, r, p, q, dinv, S, part);
-        HC_CUDA_TRY(h, cheb());
+        HC_CUDA_TRY(h, precond());
         k_rz_beta<T><<<g, kRedThreads, 0, s>>>(n, r, z, 0, S, part);
         k_pcg_dir<T, false><<<g, kRedThreads, 0, s>>>(n, z, dinv, p, q, h->ess, S, part);
       }
@@ -708,6 +727,12 @@ hc_status mixed_device(hcop* h, const hc_solve_params* prm, const double* b, dou
   const double bn = std::sqrt(bn2);
   const double tol = std::max(prm->rtol * bn, prm->atol);
   hc_status result = HC_NOT_CONVERGED;
+  // A refinement step that no longer cuts the FP64 residual by 4x has hit the
+  // FP32 accuracy floor of this operator (kappa eps_32 ~ 1 on its smooth
+  // modes): stop refining and finish with FP64 PCG from the current x.
+  bool stalled = false;
+  double rn_prev = 0.0;
+  const int inner_cap = std::max(100, prm->maxit / 4);
   while (true) {
     const double rn = std::sqrt(rn2);
     if (!std::isfinite(rn)) {
@@ -719,10 +744,15 @@ hc_status mixed_device(hcop* h, const hc_solve_params* prm, const double* b, dou
       break;
     }
     if (outer >= max_outer || iters >= prm->maxit) break;
+    if (outer >= 2 && rn > 0.25 * rn_prev) {
+      stalled = true;
+      break;
+    }
+    rn_prev = rn;
     ++outer;
     k_d2f_scaled<<<g, kRedThreads, 0, s>>>(n, r64, rf, 1.0 / rn);
     HC_CUDA_TRY(h, cudaMemsetAsync(cf, 0, n * sizeof(float), s));
-    in.maxit = prm->maxit - iters;
+    in.maxit = std::min(prm->maxit - iters, inner_cap);
     int it = 0, ap = 0;
     hc_status ist = pcg_run<float>(h, in, rf, cf, wk, &it, &ap);
     iters += it;
@@ -735,6 +765,41 @@ hc_status mixed_device(hcop* h, const hc_solve_params* prm, const double* b, dou
     HC_CUDA_TRY(h, cudaGetLastError());
     st = residual(&rn2, &bn2);
     if (st != HC_OK) return st;
+  }
+  if (stalled && iters < prm->maxit) {
+    // FP64 polish: PCG on J x = b from the refined x.  Work layout grows to
+    // r64 | 8n floats | 6n doubles (the FP64 PCG vectors, also Lanczos space).
+    st = ensure_work(h, (size_t)n * sizeof(double) + (size_t)8 * n * sizeof(float) + (size_t)6 * n * sizeof(double));
+    if (st != HC_OK) return st;
+    r64 = (double*)h->work;
+    double* wk64 = (double*)((char*)h->work + (size_t)n * sizeof(double) + (size_t)8 * n * sizeof(float));
+    SolveCfg c64;
+    c64.precond = prm->precond;
+    c64.cheb_degree = in.cheb_degree;
+    c64.cheb_ratio = in.cheb_ratio;
+    c64.lmax = prm->cheb_lmax;
+    if (c64.precond == HC_PRECOND_CHEBYSHEV && c64.lmax <= 0) {
+      if (h->lmax64 <= 0) {
+        double lm = 0;
+        st = lanczos_device<double>(h, 20, &lm, wk64);
+        if (st != HC_OK) return st;
+        h->lmax64 = 1.1 * lm;
+      }
+      c64.lmax = h->lmax64;
+    }
+    c64.rtol = prm->rtol;
+    c64.atol = prm->atol;
+    c64.maxit = prm->maxit - iters;
+    int it = 0, ap = 0;
+    const hc_status pst = pcg_run<double>(h, c64, b, x, wk64, &it, &ap);
+    iters += it;
+    applies += ap;
+    ++outer;
+    if (pst == HC_ECUDA || pst == HC_ENOMEM) return pst;
+    st = residual(&rn2, &bn2);
+    if (st != HC_OK) return st;
+    // the FP64 Krylov's own verdict (recursive residual), as for a plain FP64 solve
+    result = std::isfinite(std::sqrt(rn2)) ? pst : HC_BREAKDOWN;
   }
   if (info) {
     info->status = result;

@@ -76,7 +76,9 @@ cudaError_t hex_curl(const HexDev& d, const double* A, double* B, cudaStream_t s
 }
 
 // ---- coil load vector -------------------------------------------------------------
-// Gauss-Legendre points per direction (<= 8) and the 1-D basis values there.
+// Gauss-Legendre points per direction (<= 8) and the 1-D basis values there;
+// passed to the kernel by value, so concurrent loads on different streams
+// never share it.
 struct LoadTab {
   int q;
   double w[8];
@@ -84,14 +86,13 @@ struct LoadTab {
   double bc[8][kMaxP + 1];  // closed basis at the points
   double bo[8][kMaxP];      // open basis at the points
 };
-static __constant__ LoadTab c_load;
-
 struct CoilDev {
   double I0, xc, yc, r0, r1, z0, z1;
 };
 
 template <int P>
-__global__ void hex_load_coil_kernel(HexDev d, const double* __restrict__ V, CoilDev coil, double* __restrict__ b) {
+__global__ void hex_load_coil_kernel(HexDev d, const double* __restrict__ V, CoilDev coil, LoadTab c_load,
+                                     double* __restrict__ b) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= d.ne) return;
   constexpr int C = P + 1, O = P, NDC = O * C * C;
@@ -165,16 +166,14 @@ cudaError_t hex_load_coil(const HexDev& d, const double* V, const double coil[7]
     for (int j = 0; j <= d.p; ++j) t.bc[k][j] = bc[k * (d.p + 1) + j];
     for (int j = 0; j < d.p; ++j) t.bo[k][j] = bo[k * d.p + j];
   }
-  cudaError_t e = cudaMemcpyToSymbolAsync(c_load, &t, sizeof(t), 0, cudaMemcpyHostToDevice, s);
-  if (e != cudaSuccess) return e;
-  e = cudaMemsetAsync(b, 0, d.ndof * sizeof(double), s);
+  cudaError_t e = cudaMemsetAsync(b, 0, d.ndof * sizeof(double), s);
   if (e != cudaSuccess) return e;
   const CoilDev cd{coil[0], coil[1], coil[2], coil[3], coil[4], coil[5], coil[6]};
   const int blocks = (int)((d.ne + 127) / 128);
   switch (d.p) {
-    case 1: hex_load_coil_kernel<1><<<blocks, 128, 0, s>>>(d, V, cd, b); break;
-    case 2: hex_load_coil_kernel<2><<<blocks, 128, 0, s>>>(d, V, cd, b); break;
-    case 3: hex_load_coil_kernel<3><<<blocks, 128, 0, s>>>(d, V, cd, b); break;
+    case 1: hex_load_coil_kernel<1><<<blocks, 128, 0, s>>>(d, V, cd, t, b); break;
+    case 2: hex_load_coil_kernel<2><<<blocks, 128, 0, s>>>(d, V, cd, t, b); break;
+    case 3: hex_load_coil_kernel<3><<<blocks, 128, 0, s>>>(d, V, cd, t, b); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

@@ -363,46 +363,49 @@ cudaError_t tet_setup_device(hcop* h, const hc_problem_desc* desc, const std::ve
   int32_t* dsv = nullptr;
   double *dnu = nullptr, *dsig = nullptr;
   int* bad = nullptr;
-  cudaError_t e = cudaMalloc((void**)&h->tet_edofs, edofs.size() * sizeof(int32_t));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&h->tetK64, (size_t)ne * L * L * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&h->tetK32, (size_t)ne * L * L * sizeof(float));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&V, desc->n_vert * 3 * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&dsv, sv.size() * sizeof(int32_t));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&dnu, ne * sizeof(double));
-  if (e == cudaSuccess && desc->sigma) e = cudaMalloc((void**)&dsig, ne * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&bad, sizeof(int));
+  cudaStream_t cs = h->stream;
+  cudaError_t e = dmalloc(h, (void**)&h->tet_edofs, edofs.size() * sizeof(int32_t));
+  if (e == cudaSuccess) e = dmalloc(h, (void**)&h->tetK64, (size_t)ne * L * L * sizeof(double));
+  if (e == cudaSuccess) e = dmalloc(h, (void**)&h->tetK32, (size_t)ne * L * L * sizeof(float));
+  if (e == cudaSuccess) e = dmalloc(h, (void**)&V, desc->n_vert * 3 * sizeof(double));
+  if (e == cudaSuccess) e = dmalloc(h, (void**)&dsv, sv.size() * sizeof(int32_t));
+  if (e == cudaSuccess) e = dmalloc(h, (void**)&dnu, ne * sizeof(double));
+  if (e == cudaSuccess && desc->sigma) e = dmalloc(h, (void**)&dsig, ne * sizeof(double));
+  if (e == cudaSuccess) e = dmalloc(h, (void**)&bad, sizeof(int));
   if (e == cudaSuccess) {
-    cudaMemcpy(h->tet_edofs, edofs.data(), edofs.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
-    cudaMemcpy(V, desc->vertices, desc->n_vert * 3 * sizeof(double), cudaMemcpyHostToDevice);
-    cudaMemcpy(dsv, sv.data(), sv.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
-    cudaMemcpy(dnu, desc->nu, ne * sizeof(double), cudaMemcpyHostToDevice);
-    if (dsig) cudaMemcpy(dsig, desc->sigma, ne * sizeof(double), cudaMemcpyHostToDevice);
-    cudaMemset(bad, 0, sizeof(int));
-    tet_elem_matrix_kernel<<<(unsigned)((ne + 127) / 128), 128>>>(ne, h->p, V, dsv, dnu, dsig, h->dt, h->tetK64,
-                                                                  h->tetK32, bad);
+    cudaMemcpyAsync(h->tet_edofs, edofs.data(), edofs.size() * sizeof(int32_t), cudaMemcpyHostToDevice, cs);
+    cudaMemcpyAsync(V, desc->vertices, desc->n_vert * 3 * sizeof(double), cudaMemcpyHostToDevice, cs);
+    cudaMemcpyAsync(dsv, sv.data(), sv.size() * sizeof(int32_t), cudaMemcpyHostToDevice, cs);
+    cudaMemcpyAsync(dnu, desc->nu, ne * sizeof(double), cudaMemcpyHostToDevice, cs);
+    if (dsig) cudaMemcpyAsync(dsig, desc->sigma, ne * sizeof(double), cudaMemcpyHostToDevice, cs);
+    cudaMemsetAsync(bad, 0, sizeof(int), cs);
+    tet_elem_matrix_kernel<<<(unsigned)((ne + 127) / 128), 128, 0, cs>>>(ne, h->p, V, dsv, dnu, dsig, h->dt,
+                                                                         h->tetK64, h->tetK32, bad);
     e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
     if (e != cudaSuccess) {
       h->err = std::string("tet element-matrix kernel: ") + cudaGetErrorString(e);
     } else {
-      cudaMemset(h->diag, 0, h->ndof * sizeof(double));
+      cudaMemsetAsync(h->diag, 0, h->ndof * sizeof(double), cs);
       if (L == 6)
-        tet_diag_kernel<6><<<(unsigned)((ne + 127) / 128), 128>>>(ne, h->tet_edofs, h->tetK64, h->diag);
+        tet_diag_kernel<6><<<(unsigned)((ne + 127) / 128), 128, 0, cs>>>(ne, h->tet_edofs, h->tetK64, h->diag);
       else
-        tet_diag_kernel<20><<<(unsigned)((ne + 127) / 128), 128>>>(ne, h->tet_edofs, h->tetK64, h->diag);
+        tet_diag_kernel<20><<<(unsigned)((ne + 127) / 128), 128, 0, cs>>>(ne, h->tet_edofs, h->tetK64, h->diag);
       e = cudaGetLastError();
-      if (e == cudaSuccess) e = cudaDeviceSynchronize();
+      if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
       if (e != cudaSuccess) h->err = std::string("tet diagonal kernel: ") + cudaGetErrorString(e);
       int hb = 0;
-      cudaMemcpy(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost);
+      cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, cs);
+      cudaStreamSynchronize(cs);
       if (e == cudaSuccess && hb) e = cudaErrorInvalidValue;
     }
   }
-  cudaFree(V);
-  cudaFree(dsv);
-  cudaFree(dnu);
-  cudaFree(dsig);
-  cudaFree(bad);
+  cudaStreamSynchronize(cs);
+  dfree(h, V);
+  dfree(h, dsv);
+  dfree(h, dnu);
+  dfree(h, dsig);
+  dfree(h, bad);
   return e;
 }
 

@@ -238,6 +238,12 @@ class HCurlOperator:
         N.check(N.lib().hc_add_weak_curlcurl(self.h, _ptr(u), _ptr(lf), scale), self.h)
         return lf
 
+    def AddWeakCurlCurlDevice(self, u, lf, scale=-1.0):
+        """lf += scale * C_nu u on float64 device tensors (WeakCurlCurlKernel::Apply)."""
+        N.check(N.lib().hc_add_weak_curlcurl_device(self.h, _dev_ptr(u, "float64"), _dev_ptr(lf, "float64"),
+                                                    float(scale)), self.h)
+        return lf
+
     def Diagonal(self):
         d = np.empty(self.ndof)
         N.check(N.lib().hc_diag(self.h, _ptr(d)), self.h)
@@ -340,7 +346,8 @@ class HCurlOperator:
         return v.value
 
 
-_PRECOND = {"none": N.HC_PRECOND_NONE, "jacobi": N.HC_PRECOND_JACOBI, "chebyshev": N.HC_PRECOND_CHEBYSHEV}
+_PRECOND = {"none": N.HC_PRECOND_NONE, "jacobi": N.HC_PRECOND_JACOBI, "chebyshev": N.HC_PRECOND_CHEBYSHEV,
+            "aux": N.HC_PRECOND_AUX}
 _PREC = {"fp64": N.HC_FP64, "mixed": N.HC_MIXED}
 
 
@@ -350,7 +357,8 @@ class GpuHCurlPCGSolver:
     Options (defaults as DefaultJacobiPCGSolver, hephaestus_solvers.hpp:34-57):
       Tolerance (1e-9), AbsTolerance (1e-16), MaxIter (1000), PrintLevel (ignored),
     plus: Precision ('fp64' | 'mixed'), Preconditioner ('jacobi' |
-    'chebyshev' | 'none'), ChebyshevDegree (2), ChebyshevRatio (30),
+    'chebyshev' | 'aux' | 'none'; 'aux' = Jacobi + the auxiliary-space
+    gradient correction, the gradient part of AMS), ChebyshevDegree (2), ChebyshevRatio (30),
     ChebyshevLmax (0 = estimate), InnerTolerance (1e-4), MaxOuter (50).
     """
 
@@ -412,12 +420,12 @@ class GpuComplexCOCGSolver(GpuHCurlPCGSolver):
     Jacobi preconditioner: the solve of ComplexMaxwellOperator::Solve
     (src/formulations/ComplexMaxwell/complex_maxwell_formulation.cpp:171-222)
     with an iterative solver in place of SuperLU.  Options as
-    GpuHCurlPCGSolver (Precision 'fp64' | 'mixed'); the preconditioner is
-    always Jacobi."""
+    GpuHCurlPCGSolver (Precision 'fp64' | 'mixed'); Preconditioner 'jacobi'
+    (default) or 'aux' (Jacobi + G V G^T / (i omega))."""
 
     def __init__(self, params=None, op=None, omega=0.0):
         params = dict(params or {})
-        params["Preconditioner"] = "jacobi"
+        params.setdefault("Preconditioner", "jacobi")
         super().__init__(params, op)
         self.omega = float(omega)
 

@@ -66,7 +66,11 @@ enum {
   HC_MIXED = 2   /* FP32 inner PCG inside FP64 iterative refinement       */
 };
 
-enum { HC_PRECOND_NONE = 0, HC_PRECOND_JACOBI = 1, HC_PRECOND_CHEBYSHEV = 2 };
+/* HC_PRECOND_AUX: Jacobi plus the auxiliary-space gradient correction
+ * G V G^T (V one multigrid V-cycle for G^T M_sigma G on the H1 nodes), the
+ * gradient part of the AMS preconditioner the reference uses
+ * (hcurl_formulation.cpp:69-79).  Structured hex grids with sigma.        */
+enum { HC_PRECOND_NONE = 0, HC_PRECOND_JACOBI = 1, HC_PRECOND_CHEBYSHEV = 2, HC_PRECOND_AUX = 3 };
 
 typedef struct {
   int32_t elem_type;        /* HC_HEX (structured grid) or HC_TET                 */
@@ -144,6 +148,7 @@ hc_status hc_apply_form(hcop_t* h, const double* x, double* y);
  * WeakCurlCurlKernel::Apply's _curl_curl->AddMultTranspose(u, lf, -1)
  * (src/kernels/weak_curl_curl_kernel.cpp:27-31) with scale = -1.            */
 hc_status hc_add_weak_curlcurl(hcop_t* h, const double* x, double* y, double scale);
+hc_status hc_add_weak_curlcurl_device(hcop_t* h, const double* x, double* y, double scale);
 /* Diagonal of J (HypreDiagScale's diagonal, hephaestus_solvers.hpp:34-57).  */
 hc_status hc_diag(hcop_t* h, double* d);
 
