@@ -16,7 +16,7 @@ HEADER = os.path.join(os.path.dirname(_HERE), "include", "hcurl_op.h")
 HC_OK, HC_EINVAL, HC_ENOMEM, HC_ECUDA, HC_NOT_CONVERGED, HC_BREAKDOWN, HC_TIMEOUT, HC_ENOTSUP = range(8)
 STATUS_NAMES = ["OK", "EINVAL", "ENOMEM", "ECUDA", "NOT_CONVERGED", "BREAKDOWN", "TIMEOUT", "ENOTSUP"]
 HC_HEX, HC_TET = 0, 1
-HC_FP64, HC_FP32, HC_MIXED = 0, 1, 2
+HC_FP64, HC_FP32, HC_MIXED, HC_BF16 = 0, 1, 2, 3
 HC_PRECOND_NONE, HC_PRECOND_JACOBI, HC_PRECOND_CHEBYSHEV, HC_PRECOND_AUX = 0, 1, 2, 3
 
 

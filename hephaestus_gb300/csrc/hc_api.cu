@@ -287,7 +287,7 @@ void hc_destroy(hcop_t* h) {
   for (void* p : {(void*)h->fac, (void*)h->facf, (void*)h->ess, (void*)h->diag, (void*)h->dinv, (void*)h->dinvf,
                   (void*)h->sdinv, (void*)h->sdinvf, (void*)h->scal, (void*)h->partials, h->work, (void*)h->xbuf,
                   (void*)h->ybuf, (void*)h->verts, (void*)h->tet_edofs, (void*)h->tetK64, (void*)h->tetK32,
-                  (void*)h->tab})
+                  h->tetK16, (void*)h->tab})
     dfree(h, p);
   pinned_put(h->hscal);
   delete h;
@@ -586,9 +586,13 @@ hc_status hc_mult_multi_device(hcop_t* h, int precision, int nrhs, const void* X
     h->err = "hc_mult_multi_device: nrhs must be 1, 2, 4, 8, 16 or 32";
     return HC_EINVAL;
   }
-  if (precision != HC_FP64 && precision != HC_FP32) {
-    h->err = "hc_mult_multi_device: precision must be HC_FP64 or HC_FP32";
+  if (precision != HC_FP64 && precision != HC_FP32 && precision != HC_BF16) {
+    h->err = "hc_mult_multi_device: precision must be HC_FP64, HC_FP32 or HC_BF16";
     return HC_EINVAL;
+  }
+  if (precision == HC_BF16 && h->type != HC_TET) {
+    h->err = "hc_mult_multi_device: HC_BF16 element matrices exist for tet meshes only";
+    return HC_ENOTSUP;
   }
   if (h->type != HC_TET) {
     if (nrhs != 1) {
@@ -602,10 +606,14 @@ hc_status hc_mult_multi_device(hcop_t* h, int precision, int nrhs, const void* X
     HC_CUDA_TRY(h, init_masked_multi<double>(h->ndof, nrhs, h->ess, (const double*)X, (double*)Y, h->stream));
     HC_CUDA_TRY(h, tet_apply_launch<double>(h, h->tetK64, (const double*)X, (double*)Y, nrhs, true, 1.0, nullptr,
                                             h->stream));
-  } else {
+  } else if (precision == HC_FP32) {
     HC_CUDA_TRY(h, init_masked_multi<float>(h->ndof, nrhs, h->ess, (const float*)X, (float*)Y, h->stream));
     HC_CUDA_TRY(h, tet_apply_launch<float>(h, h->tetK32, (const float*)X, (float*)Y, nrhs, true, 1.0, nullptr,
                                            h->stream));
+  } else {
+    HC_CUDA_TRY(h, tet_ensure_bf16(h));
+    HC_CUDA_TRY(h, init_masked_multi<float>(h->ndof, nrhs, h->ess, (const float*)X, (float*)Y, h->stream));
+    HC_CUDA_TRY(h, tet_apply_launch_bf16(h, (const float*)X, (float*)Y, nrhs, true, h->stream));
   }
   return HC_OK;
 }

@@ -37,9 +37,10 @@ namespace hc {
 
 constexpr int kAuxMaxLevels = 10;
 constexpr int kAuxCoarseNodes = 1000;
-constexpr int kAuxDegree = 3;
-constexpr int kAuxCoarseDegree = 8;
+constexpr int kAuxDegree = 2;        // Chebyshev degree of the pre- and post-smoothers
+constexpr int kAuxCoarseDegree = 4;  // Chebyshev degree on the coarsest grid
 constexpr double kAuxRatio = 30.0;
+constexpr int kAuxGraphs = 8;
 
 static inline unsigned agrid(int64_t n, int threads = 256) {
   const int64_t b = (n + threads - 1) / threads;
@@ -72,8 +73,19 @@ struct AuxLevel {
   double lmax = 2.0;
 };
 
+// A replayable capture of one preconditioner application (fixed buffers).
+struct AuxGraph {
+  cudaGraphExec_t exec = nullptr;
+  const void* key[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  int nv = 0, tsize = 0;
+  float coef[4] = {0, 0, 0, 0};
+};
+
 struct AuxMG {
   int p = 1, nlev = 0;
+  std::vector<AuxGraph> graphs;   // at most kAuxGraphs, oldest replaced first
+  int next_graph = 0;
+  cudaStream_t cap = nullptr;     // private stream the captures are made on
   AuxLevel lev[kAuxMaxLevels];
   Dims q{0, 0, 0};         // Gauss-Lobatto node grid as "elements" (nodes = (n p + 1)^3), p > 1
   int64_t nq = 0;
@@ -301,20 +313,6 @@ __global__ void k_finish_dinv(int64_t n, const float* __restrict__ diag, const u
   GS_LOOP(i, n) dinv[i] = (fixed[i] || !(diag[i] > 0.0f)) ? 0.0f : 1.0f / diag[i];
 }
 
-// ---- Chebyshev smoothing (Saad Alg. 12.1 on D^-1 L) for NV vectors ----------------
-template <int NV>
-__global__ void k_ch_zero_start(int64_t nn, const float* __restrict__ b, const float* __restrict__ dinv,
-                                float* __restrict__ r, float* __restrict__ d, float* __restrict__ x, float inv_theta,
-                                const int* __restrict__ done) {
-  if (done && *done) return;
-  GS_LOOP(i, NV * nn) {
-    const float ri = b[i];
-    const float di = dinv[i % nn] * ri * inv_theta;
-    r[i] = ri;
-    d[i] = di;
-    x[i] = di;
-  }
-}
 // ---- grid transfers between Q1 levels ------------------------------------------------
 // 1-D transfer weights between a fine grid of nf cells and its 2:1 coarsening
 // (coarse node I sits at fine node min(2 I, nf)).
@@ -326,9 +324,28 @@ __device__ __forceinline__ float w1d(int f, int I, int nf) {
   return (I == (f - 1) / 2 || I == (f + 1) / 2) ? 0.5f : 0.0f;
 }
 // b_c = R r_f (r_f is zero at fixed fine nodes), zero at fixed coarse nodes
+// The producer of a level's right-hand side also starts its Chebyshev
+// smoother from x = 0: r = b, d = D^-1 b / theta, x = d.
+struct ChebStart {
+  float* r;
+  float* d;
+  float* x;
+  float inv_theta;
+};
+template <int NV>
+__device__ __forceinline__ void cheb_start_at(const ChebStart& cs, int nn, int n, float dinv, const float (&b)[NV]) {
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    const float dv = dinv * b[v] * cs.inv_theta;
+    cs.r[v * nn + n] = b[v];
+    cs.d[v * nn + n] = dv;
+    cs.x[v * nn + n] = dv;
+  }
+}
+
 template <int NV>
 __global__ void k_restrict(Dims fd, Dims cd, const float* __restrict__ rf, const float* __restrict__ dinvc,
-                           float* __restrict__ bc, const int* __restrict__ done) {
+                           float* __restrict__ bc, ChebStart cs, const int* __restrict__ done) {
   if (done && *done) return;
   NODE_IJK(cd, I, J, K, n);
   const int nc = (int)cd.nodes(), nf = (int)fd.nodes();
@@ -347,6 +364,7 @@ __global__ void k_restrict(Dims fd, Dims cd, const float* __restrict__ rf, const
   }
 #pragma unroll
   for (int v = 0; v < NV; ++v) bc[v * nc + n] = acc[v];
+  cheb_start_at<NV>(cs, nc, n, dinvc[n], acc);
 }
 // x_f += P x_c at free fine nodes
 __device__ __forceinline__ void coarse_pair(int f, int nf, int& c0, int& c1, float& w0, float& w1) {
@@ -399,7 +417,8 @@ __global__ void k_prolong_add(Dims fd, Dims cd, const float* __restrict__ xc, co
 // g = G^T r on the Gauss-Lobatto grid (mx+1, my+1, mz+1), zero where qdinv = 0
 template <typename T, int NV, int P>
 __global__ void k_gt(HexDev h, AuxTab tab, const T* __restrict__ r0, const T* __restrict__ r1,
-                     const float* __restrict__ qdinv, float* __restrict__ g, const int* __restrict__ done) {
+                     const float* __restrict__ qdinv, float* __restrict__ g, ChebStart cs,
+                     const int* __restrict__ done) {
   if (done && *done) return;
   const Dims qd{h.nx * P, h.ny * P, h.nz * P};
   NODE_IJK(qd, I, J, K, n);
@@ -444,6 +463,7 @@ __global__ void k_gt(HexDev h, AuxTab tab, const T* __restrict__ r0, const T* __
   }
 #pragma unroll
   for (int v = 0; v < NV; ++v) g[v * nq + n] = acc[v];
+  if (cs.r) cheb_start_at<NV>(cs, nq, n, qdinv[n], acc);
 }
 
 // z += C G phi for the dofs of component c (grid n0 x n1 x n2, open along c);
@@ -492,7 +512,7 @@ __device__ __forceinline__ float wq1d(int I, int i, int p, const AuxTab& tab) {
 // Gauss-Lobatto grid -> element vertices: b1 = P0^T g (zero at fixed vertices)
 template <int NV, int P>
 __global__ void k_rq(Dims vd, AuxTab tab, const float* __restrict__ g, const float* __restrict__ dinv1,
-                     float* __restrict__ b1, const int* __restrict__ done) {
+                     float* __restrict__ b1, ChebStart cs, const int* __restrict__ done) {
   if (done && *done) return;
   NODE_IJK(vd, i, j, k, n);
   const int mx = vd.nx * P, my = vd.ny * P, mz = vd.nz * P;
@@ -524,6 +544,7 @@ __global__ void k_rq(Dims vd, AuxTab tab, const float* __restrict__ g, const flo
   }
 #pragma unroll
   for (int v = 0; v < NV; ++v) b1[v * n1 + n] = acc[v];
+  cheb_start_at<NV>(cs, n1, n, dinv1[n], acc);
 }
 
 // phi = D_L^-1 g + P0 x1 on the Gauss-Lobatto grid (zero at fixed nodes)
@@ -635,6 +656,9 @@ void auxmg_free(hcop* h) {
     dfree(h, L.dv);
     dfree(h, L.t);
   }
+  for (AuxGraph& g : M->graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  if (M->cap) cudaStreamDestroy(M->cap);
   dfree(h, M->qdinv);
   dfree(h, M->g);
   dfree(h, M->phi);
@@ -842,9 +866,8 @@ static void smooth(const hcop* h, AuxLevel& L, int degree, bool from_zero, const
   const ChebCoef c = cheb_coef(L.lmax, degree);
   const unsigned gv = agrid(NV * nn);
   const NodeGrid gn = node_grid(L.d.nx, L.d.ny, L.d.nz);
-  if (from_zero)
-    k_ch_zero_start<NV><<<gv, 256, 0, s>>>(nn, L.b, L.dinv, L.r, L.dv, L.x, c.inv_theta, done);
-  else
+  // from zero: the kernel that produced L.b already set r, d and x (ChebStart)
+  if (!from_zero)
     k_cheb_resid<NV><<<gn.grid, gn.block, 0, s>>>(L.d, L.St, L.dinv, L.b, L.x, L.r, L.dv, c.inv_theta, done);
   float* din = L.dv;
   float* dout = L.t;
@@ -854,6 +877,10 @@ static void smooth(const hcop* h, AuxLevel& L, int degree, bool from_zero, const
     std::swap(din, dout);
   }
   if (!from_zero && degree == 1) k_add<NV><<<gv, 256, 0, s>>>((int)nn, L.dv, L.x, done);
+}
+
+static ChebStart start_of(AuxLevel& L) {
+  return ChebStart{L.r, L.dv, L.x, cheb_coef(L.lmax, 1).inv_theta};
 }
 
 template <int NV>
@@ -868,7 +895,7 @@ static void vcycle(const hcop* h, AuxMG* M, int l, const int* done, cudaStream_t
   // r = b - L x (masked), restricted
   const NodeGrid gl = node_grid(L.d.nx, L.d.ny, L.d.nz), gc = node_grid(C.d.nx, C.d.ny, C.d.nz);
   k_cheb_resid<NV><<<gl.grid, gl.block, 0, s>>>(L.d, L.St, L.dinv, L.b, L.x, L.r, L.dv, 1.0f, done);
-  k_restrict<NV><<<gc.grid, gc.block, 0, s>>>(L.d, C.d, L.r, C.dinv, C.b, done);
+  k_restrict<NV><<<gc.grid, gc.block, 0, s>>>(L.d, C.d, L.r, C.dinv, C.b, start_of(C), done);
   vcycle<NV>(h, M, l + 1, done, s);
   k_prolong_add<NV><<<gl.grid, gl.block, 0, s>>>(L.d, C.d, C.x, L.dinv, L.x, done);
   smooth<NV>(h, L, kAuxDegree, false, done, s);
@@ -885,8 +912,9 @@ static void aux_apply_p(const hcop* h, AuxMG* M, const T* r0, const T* r1, T* z0
   float* g = P > 1 ? M->g : L0.b;
   const float* qd = P > 1 ? M->qdinv : L0.dinv;
   const NodeGrid gq = node_grid(mx, my, mz), g1 = node_grid(L0.d.nx, L0.d.ny, L0.d.nz);
-  k_gt<T, NV, P><<<gq.grid, gq.block, 0, s>>>(hd, M->tab, r0, r1, qd, g, done);
-  if (P > 1) k_rq<NV, P><<<g1.grid, g1.block, 0, s>>>(L0.d, M->tab, g, L0.dinv, L0.b, done);
+  const ChebStart none{nullptr, nullptr, nullptr, 0.0f};
+  k_gt<T, NV, P><<<gq.grid, gq.block, 0, s>>>(hd, M->tab, r0, r1, qd, g, P > 1 ? none : start_of(L0), done);
+  if (P > 1) k_rq<NV, P><<<g1.grid, g1.block, 0, s>>>(L0.d, M->tab, g, L0.dinv, L0.b, start_of(L0), done);
   vcycle<NV>(h, M, 0, done, s);
   const float* phi = L0.x;
   if (P > 1) {
@@ -906,17 +934,72 @@ static void aux_apply_p(const hcop* h, AuxMG* M, const T* r0, const T* r1, T* z0
 // z += C G V G^T r   (NV = 1: real r, coefficient c00; NV = 2: planar complex,
 // z_0 += c00 v_0 + c01 v_1, z_1 += c10 v_0 + c11 v_1)
 template <typename T, int NV>
-cudaError_t auxmg_apply(const hcop* h, const T* r0, const T* r1, T* z0, T* z1, const float coef[4], const int* done,
-                        cudaStream_t s) {
-  AuxMG* M = static_cast<AuxMG*>(h->aux);
-  if (!M) return cudaErrorInvalidValue;
+static void aux_apply_any(const hcop* h, AuxMG* M, const T* r0, const T* r1, T* z0, T* z1, const float coef[4],
+                          const int* done, cudaStream_t s) {
   switch (M->p) {
     case 1: aux_apply_p<T, NV, 1>(h, M, r0, r1, z0, z1, coef, done, s); break;
     case 2: aux_apply_p<T, NV, 2>(h, M, r0, r1, z0, z1, coef, done, s); break;
-    case 3: aux_apply_p<T, NV, 3>(h, M, r0, r1, z0, z1, coef, done, s); break;
-    default: return cudaErrorInvalidValue;
+    default: aux_apply_p<T, NV, 3>(h, M, r0, r1, z0, z1, coef, done, s); break;
   }
-  return cudaGetLastError();
+}
+
+// The ~40 small kernels of one application are captured once per argument
+// set into a CUDA graph and replayed with one launch (host-driven Krylov
+// loops would otherwise be bound by launch overhead).  Inside a stream that
+// is itself being captured (a graph-driven solve) the kernels are issued
+// directly and become part of that graph.
+template <typename T, int NV>
+cudaError_t auxmg_apply(const hcop* h, const T* r0, const T* r1, T* z0, T* z1, const float coef[4], const int* done,
+                        cudaStream_t s) {
+  AuxMG* M = static_cast<AuxMG*>(h->aux);
+  if (!M || M->p < 1 || M->p > 3) return cudaErrorInvalidValue;
+  cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(s, &cst);
+  if (e != cudaSuccess) return e;
+  if (cst != cudaStreamCaptureStatusNone) {
+    aux_apply_any<T, NV>(h, M, r0, r1, z0, z1, coef, done, s);
+    return cudaGetLastError();
+  }
+  const void* key[5] = {r0, r1, z0, z1, done};
+  for (AuxGraph& g : M->graphs) {
+    if (g.exec && g.nv == NV && g.tsize == (int)sizeof(T) && std::memcmp(g.key, key, sizeof(key)) == 0 &&
+        std::memcmp(g.coef, coef, sizeof(g.coef)) == 0)
+      return cudaGraphLaunch(g.exec, s);
+  }
+  if (!M->cap) {
+    e = cudaStreamCreateWithFlags(&M->cap, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return e;
+  }
+  e = cudaStreamBeginCapture(M->cap, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) return e;
+  aux_apply_any<T, NV>(h, M, r0, r1, z0, z1, coef, done, M->cap);
+  const cudaError_t le = cudaGetLastError();
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(M->cap, &graph);
+  if (le != cudaSuccess || e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return le != cudaSuccess ? le : e;
+  }
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return e;
+  AuxGraph* slot = nullptr;
+  if ((int)M->graphs.size() < kAuxGraphs) {
+    M->graphs.emplace_back();
+    slot = &M->graphs.back();
+  } else {
+    // the replaced graph may still have a launch in flight
+    cudaDeviceSynchronize();
+    slot = &M->graphs[M->next_graph++ % kAuxGraphs];
+    cudaGraphExecDestroy(slot->exec);
+  }
+  slot->exec = exec;
+  std::memcpy(slot->key, key, sizeof(key));
+  std::memcpy(slot->coef, coef, sizeof(slot->coef));
+  slot->nv = NV;
+  slot->tsize = (int)sizeof(T);
+  return cudaGraphLaunch(exec, s);
 }
 
 template cudaError_t auxmg_apply<double, 1>(const hcop*, const double*, const double*, double*, double*,

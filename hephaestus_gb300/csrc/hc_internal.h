@@ -101,6 +101,7 @@ struct hcop {
   int32_t* tet_edofs = nullptr;        // ne * L element dofs
   double* tetK64 = nullptr;            // ne * L * L element matrices (FP64)
   float* tetK32 = nullptr;             // FP32 copy
+  void* tetK16 = nullptr;              // BF16 copy (made on first use)
   int* tab = nullptr;                  // brick tile table of the apply kernel
   void* cwork = nullptr;               // complex (frequency-domain) work space, hc_complex.cu
   void* aux = nullptr;                 // auxiliary-space preconditioner, hc_auxmg.cu
@@ -170,6 +171,8 @@ cudaError_t tet_setup_device(hcop* h, const hc_problem_desc* desc, const std::ve
 template <typename T>
 cudaError_t tet_apply_launch(const hcop* h, const T* K, const T* x, T* y, int nrhs, bool masked, double scale,
                              const int* done, cudaStream_t s);
+cudaError_t tet_ensure_bf16(hcop* h);
+cudaError_t tet_apply_launch_bf16(const hcop* h, const float* x, float* y, int nrhs, bool masked, cudaStream_t s);
 // pq = p.q over all dofs, then alpha = rz / pq (PCG mode of operators without a fused energy)
 template <typename T>
 cudaError_t dot_alpha(int64_t n, const T* p, const T* q, KrylovScalars* S, double* partials, cudaStream_t s);

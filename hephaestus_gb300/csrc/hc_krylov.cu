@@ -190,11 +190,13 @@ __global__ void __launch_bounds__(kRedThreads)
   }
 }
 
-// x += alpha p; r -= alpha q; rr (and Jacobi rz = r.D^-1 r); stopping test; beta
+// x += alpha p; r -= alpha q; rr (and Jacobi rz = r.D^-1 r); stopping test; beta.
+// zout != nullptr: also z = D^-1 r (the Jacobi part of the auxiliary-space preconditioner)
 template <typename T, bool JAC>
 __global__ void __launch_bounds__(kRedThreads)
     k_pcg_update(int64_t n, T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
-                 const T* __restrict__ q, const T* __restrict__ dinv, KrylovScalars* S, double* partials) {
+                 const T* __restrict__ q, const T* __restrict__ dinv, KrylovScalars* S, double* partials,
+                 T* __restrict__ zout = nullptr) {
   if (S->done) return;
   const T a = (T)S->alpha;
   double v[2] = {0.0, 0.0}, tot[2];
@@ -204,6 +206,7 @@ __global__ void __launch_bounds__(kRedThreads)
     x[i] += a * p[i];
     const T ri = r[i] - a * q[i];
     r[i] = ri;
+    if (zout) zout[i] = dinv[i] * ri;
     rrt += ri * ri;
     if (JAC) rzt += ri * ri * (dinv ? dinv[i] : T(1));
     if (++c == 8) {
@@ -609,9 +612,9 @@ static hc_status pcg_run(hcop* h, const SolveCfg& cfg, const T* b, T* x, T* wk, 
     return cudaGetLastError();
   };
   // z = B r for the non-Jacobi preconditioners
-  auto precond = [&]() -> cudaError_t {
+  auto precond = [&](bool z_ready) -> cudaError_t {
     if (aux) {
-      k_jz<T><<<g, kRedThreads, 0, s>>>(n, r, dinv, z, S);
+      if (!z_ready) k_jz<T><<<g, kRedThreads, 0, s>>>(n, r, dinv, z, S);
       const float coef[4] = {1.0f, 0.0f, 0.0f, 0.0f};
       return auxmg_apply<T, 1>(h, r, nullptr, z, nullptr, coef, &S->done, s);
     }
@@ -629,7 +632,7 @@ static hc_status pcg_run(hcop* h, const SolveCfg& cfg, const T* b, T* x, T* wk, 
     k_pcg_dir<T, true><<<g, kRedThreads, 0, s>>>(n, r, dj, p, q, h->ess, S, part);
   } else {
     k_pcg_setup<T, false><<<g, kRedThreads, 0, s>>>(n, b, q, r, dinv, S, part);
-    HC_CUDA_TRY(h, precond());
+    HC_CUDA_TRY(h, precond(false));
     k_rz_beta<T><<<g, kRedThreads, 0, s>>>(n, r, z, 1, S, part);
     k_pcg_dir<T, false><<<g, kRedThreads, 0, s>>>(n, z, dinv, p, q, h->ess, S, part);
   }
@@ -645,8 +648,8 @@ static hc_status pcg_run(hcop* h, const SolveCfg& cfg, const T* b, T* x, T* wk, 
         k_pcg_update<T, true><<<g, kRedThreads, 0, s>>>(n, x, r, p, q, dj, S, part);
         k_pcg_dir<T, true><<<g, kRedThreads, 0, s>>>(n, r, dj, p, q, h->ess, S, part);
       } else {
-        k_pcg_update<T, false><<<g, kRedThreads, 0, s>>>(n, x, r, p, q, dinv, S, part);
-        HC_CUDA_TRY(h, precond());
+        k_pcg_update<T, false><<<g, kRedThreads, 0, s>>>(n, x, r, p, q, dinv, S, part, aux ? z : nullptr);
+        HC_CUDA_TRY(h, precond(aux));
         k_rz_beta<T><<<g, kRedThreads, 0, s>>>(n, r, z, 0, S, part);
         k_pcg_dir<T, false><<<g, kRedThreads, 0, s>>>(n, z, dinv, p, q, h->ess, S, part);
       }

@@ -24,6 +24,8 @@
 #include <cstring>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "hc_internal.h"
 #include "hc_reduce.cuh"
 
@@ -293,9 +295,14 @@ __global__ void tet_elem_matrix_kernel(int64_t ne, int p, const double* __restri
 // ---- apply -----------------------------------------------------------------------
 // y (+)= P K P x for nrhs right-hand sides stored row-major ([dof][rhs]).
 // One warp per element: lane = rhs + nrhs * part, rows split between parts.
-template <typename T, int L>
+__device__ __forceinline__ float kval(float v) { return v; }
+__device__ __forceinline__ double kval(double v) { return v; }
+__device__ __forceinline__ float kval(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+// K holds the element matrices in TK (double, float, or bf16 with FP32 vectors)
+template <typename T, int L, typename TK = T>
 __global__ void __launch_bounds__(256) tet_apply_kernel(int64_t ne, const int32_t* __restrict__ edofs,
-                                                        const T* __restrict__ K, const uint8_t* __restrict__ ess,
+                                                        const TK* __restrict__ K, const uint8_t* __restrict__ ess,
                                                         int masked, int nrhs, T scale, const T* __restrict__ x,
                                                         T* __restrict__ y, const int* done) {
   if (done && *done) return;
@@ -313,12 +320,12 @@ __global__ void __launch_bounds__(256) tet_apply_kernel(int64_t ne, const int32_
       if (masked && ess[dof[j]]) v = T(0);
       xe[j] = v;
     }
-    const T* Ke = K + e * L * L;
+    const TK* Ke = K + e * L * L;
     for (int i = part; i < L; i += nparts) {
       if (masked && ess[dof[i]]) continue;
       T acc = T(0);
 #pragma unroll
-      for (int j = 0; j < L; ++j) acc += __ldg(Ke + i * L + j) * xe[j];
+      for (int j = 0; j < L; ++j) acc += (T)kval(Ke[i * L + j]) * xe[j];
       atomicAdd(y + (int64_t)dof[i] * nrhs + r, scale * acc);
     }
   }
@@ -346,6 +353,36 @@ template cudaError_t tet_apply_launch<double>(const hcop*, const double*, const 
                                               const int*, cudaStream_t);
 template cudaError_t tet_apply_launch<float>(const hcop*, const float*, const float*, float*, int, bool, double,
                                              const int*, cudaStream_t);
+
+// FP32 vectors with BF16 element matrices (FP32 accumulation)
+cudaError_t tet_apply_launch_bf16(const hcop* h, const float* x, float* y, int nrhs, bool masked, cudaStream_t s) {
+  const int warps_per_block = 8;
+  int64_t blocks = (h->ne + warps_per_block - 1) / warps_per_block;
+  blocks = std::min<int64_t>(blocks, 152 * 16);
+  const __nv_bfloat16* K = static_cast<const __nv_bfloat16*>(h->tetK16);
+  if (h->p == 1)
+    tet_apply_kernel<float, 6, __nv_bfloat16><<<(unsigned)blocks, 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess,
+                                                                             masked ? 1 : 0, nrhs, 1.0f, x, y, nullptr);
+  else
+    tet_apply_kernel<float, 20, __nv_bfloat16><<<(unsigned)blocks, 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess,
+                                                                              masked ? 1 : 0, nrhs, 1.0f, x, y, nullptr);
+  return cudaGetLastError();
+}
+
+__global__ void k_to_bf16(int64_t n, const double* __restrict__ a, __nv_bfloat16* __restrict__ b) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = __double2bfloat16(a[i]);
+}
+// BF16 copy of the element matrices, made on first use (rounded from FP64)
+cudaError_t tet_ensure_bf16(hcop* h) {
+  if (h->tetK16) return cudaSuccess;
+  const int L = h->p == 1 ? 6 : 20;
+  const int64_t n = h->ne * L * L;
+  cudaError_t e = dmalloc(h, &h->tetK16, (size_t)n * sizeof(__nv_bfloat16));
+  if (e != cudaSuccess) return e;
+  k_to_bf16<<<2048, 256, 0, h->stream>>>(n, h->tetK64, static_cast<__nv_bfloat16*>(h->tetK16));
+  return cudaGetLastError();
+}
 
 template <int L>
 __global__ void tet_diag_kernel(int64_t ne, const int32_t* __restrict__ edofs, const double* __restrict__ K,

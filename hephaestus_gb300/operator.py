@@ -282,10 +282,13 @@ class HCurlOperator:
         N.check(N.lib().hc_tet_element_matrix(self.h, e, _ptr(out)), self.h)
         return out
 
-    def MultMultiDevice(self, X, Y):
-        """Y = J X for a (ndof, nrhs) row-major CUDA tensor (float32 or float64)."""
+    def MultMultiDevice(self, X, Y, bf16_matrices=False):
+        """Y = J X for a (ndof, nrhs) row-major CUDA tensor (float32 or float64);
+        bf16_matrices (float32 tensors, tets): element matrices read as BF16."""
         prec = N.HC_FP32 if str(X.dtype) == "torch.float32" else N.HC_FP64
-        name = "float32" if prec == N.HC_FP32 else "float64"
+        if bf16_matrices:
+            prec = N.HC_BF16
+        name = "float64" if prec == N.HC_FP64 else "float32"
         nrhs = 1 if X.dim() == 1 else X.shape[1]
         N.check(N.lib().hc_mult_multi_device(self.h, prec, nrhs, _dev_ptr(X, name), _dev_ptr(Y, name)), self.h)
         return Y

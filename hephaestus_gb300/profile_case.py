@@ -1,12 +1,15 @@
 """Small, self-contained operator-apply case for profiling (ncu) runs.
 
-    python -m hephaestus_gb300.profile_case N P [mult|add|fp64]
+    python -m hephaestus_gb300.profile_case N P [mult|add|fp64|solve|complex]
 
 Builds an N^3-hex, order-P operator with nu = 10^U(0,3), sigma = 10^U(-2,6),
 dt = 0.01 (the benchmark's coefficient distributions) and applies it:
   mult  - y = J x in FP32 (masked init + apply), 5 times
   add   - y += P K P x in FP32 (the accumulate-form apply kernel alone), 5 times
   fp64  - y = J x in FP64, 3 times
+  solve - one mixed-precision PCG solve (auxiliary-space preconditioner) of
+          the coil load, capped at 8 inner iterations and 1 refinement step
+  complex - y = (C + i omega M) x in FP32 (fused complex kernel), 5 times
 """
 import sys
 
@@ -25,7 +28,21 @@ def main(argv):
     nu = meshes.loguniform(n ** 3, 1, 1e3, rng)
     sg = meshes.loguniform(n ** 3, 1e-2, 1e6, rng)
     op = HCurlOperator(n, n, n, p, nu, sg, dt=0.01)
-    if mode == "fp64":
+    if mode == "solve":
+        from hephaestus_gb300 import GpuHCurlPCGSolver
+
+        b = torch.tensor(np.where(op.ess_mask() != 0, 0.0, op.LoadCoil()), device="cuda")
+        x = torch.zeros_like(b)
+        s = GpuHCurlPCGSolver({"Tolerance": 1e-10, "MaxIter": 8, "MaxOuter": 1, "Precision": "mixed",
+                               "Preconditioner": "aux"}, op)
+        s.MultDevice(b, x)
+    elif mode == "complex":
+        xr = torch.randn(op.ndof, device="cuda")
+        xi = torch.randn_like(xr)
+        yr, yi = torch.empty_like(xr), torch.empty_like(xr)
+        for _ in range(5):
+            op.MultComplexDevice(1e3, xr, xi, yr, yi)
+    elif mode == "fp64":
         x = torch.randn(op.ndof, device="cuda", dtype=torch.float64)
         y = torch.empty_like(x)
         for _ in range(3):

@@ -63,7 +63,9 @@ enum { HC_HEX = 0, HC_TET = 1 };
 enum {
   HC_FP64 = 0,   /* plain FP64 operator and PCG (the drop-in path)        */
   HC_FP32 = 1,   /* FP32 operator and vectors, FP64 dots and alpha/beta   */
-  HC_MIXED = 2   /* FP32 inner PCG inside FP64 iterative refinement       */
+  HC_MIXED = 2,  /* FP32 inner PCG inside FP64 iterative refinement       */
+  HC_BF16 = 3    /* tet multi-RHS apply: BF16 element matrices, FP32
+                    vectors and accumulation                               */
 };
 
 /* HC_PRECOND_AUX: Jacobi plus the auxiliary-space gradient correction
@@ -192,7 +194,8 @@ hc_status hc_load_coil(hcop_t* h, const hc_coil* coil, int q, double* b);
 hc_status hc_load_coil_device(hcop_t* h, const hc_coil* coil, int q, double* b);
 
 /* Y = J X for nrhs right-hand sides stored row-major ([dof][rhs]), device
- * pointers of the given precision (HC_FP64: double, HC_FP32: float);
+ * pointers of the given precision (HC_FP64: double, HC_FP32 and HC_BF16:
+ * float; HC_BF16 reads element matrices rounded to BF16, tets only);
  * nrhs in {1, 2, 4, 8, 16, 32}.  Tet meshes apply each element matrix to all
  * right-hand sides at once (config 3's batched element-matrix apply).      */
 hc_status hc_mult_multi_device(hcop_t* h, int precision, int nrhs, const void* X, void* Y);

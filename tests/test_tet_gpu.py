@@ -72,6 +72,26 @@ def test_tet_multi_rhs_parity(prec):
         assert np.linalg.norm(Y[:, r] - yr) / np.linalg.norm(yr) < tol
 
 
+def test_tet_multi_rhs_bf16_matrices():
+    """BF16 element matrices, FP32 vectors and accumulation: within BF16 rounding
+    of the FP64 operator (8-bit significand: tolerance 1e-2, relative 2-norm)."""
+    import torch
+
+    op, ref, rng = _pair(4, 2)
+    nrhs = 16
+    X = rng.standard_normal((op.ndof, nrhs))
+    Xd = torch.tensor(X, dtype=torch.float32, device="cuda")
+    Yd = torch.empty_like(Xd)
+    op.MultMultiDevice(Xd, Yd, bf16_matrices=True)
+    torch.cuda.synchronize()
+    Y = Yd.double().cpu().numpy()
+    Xr = Xd.double().cpu().numpy()
+    for r in range(nrhs):
+        yr = ref.apply_masked(Xr[:, r])
+        err = np.linalg.norm(Y[:, r] - yr) / np.linalg.norm(yr)
+        assert 1e-7 < err < 1e-2, (r, err)  # really rounded, and only by BF16
+
+
 def test_tet_beam_mesh_matches_oracle():
     d = np.load(os.path.join(GOLD, "beam_tet.npz"))
     v, t, bt, ba = meshes.refine_tets(d["verts"], d["tets"], d["btris"], d["battr"])
