@@ -1,6 +1,6 @@
 """Small, self-contained operator-apply case for profiling (ncu) runs.
 
-    python -m hephaestus_gb300.profile_case N P [mult|add|fp64|solve|complex]
+    python -m hephaestus_gb300.profile_case N P [mult|add|fp64|solve|complex|tets]
 
 Builds an N^3-hex, order-P operator with nu = 10^U(0,3), sigma = 10^U(-2,6),
 dt = 0.01 (the benchmark's coefficient distributions) and applies it:
@@ -10,6 +10,7 @@ dt = 0.01 (the benchmark's coefficient distributions) and applies it:
   solve - one mixed-precision PCG solve (auxiliary-space preconditioner) of
           the coil load, capped at 8 inner iterations and 1 refinement step
   complex - y = (C + i omega M) x in FP32 (fused complex kernel), 5 times
+  tets  - Kuhn N^3 tet mesh (jitter 0.15 h), order P: 16-RHS FP32 apply, 3 times
 """
 import sys
 
@@ -25,6 +26,18 @@ def main(argv):
     p = int(argv[1]) if len(argv) > 1 else 2
     mode = argv[2] if len(argv) > 2 else "mult"
     rng = np.random.default_rng(0)
+    if mode == "tets":
+        v, t, bt, ba = meshes.kuhn_mesh(n, jitter=0.15, seed=0)
+        ne = len(t)
+        op = HCurlOperator.from_tets(v, t, p, meshes.loguniform(ne, 1, 1e3, rng), meshes.loguniform(ne, 1e-2, 1e6, rng),
+                                     dt=0.01, btris=bt, battr=ba, ess_attr_bits=0x3F)
+        X = torch.randn(op.ndof, 16, device="cuda")
+        Y = torch.empty_like(X)
+        for _ in range(3):
+            op.MultMultiDevice(X, Y)
+        torch.cuda.synchronize()
+        print("ok", mode, op.ndof)
+        return
     nu = meshes.loguniform(n ** 3, 1, 1e3, rng)
     sg = meshes.loguniform(n ** 3, 1e-2, 1e6, rng)
     op = HCurlOperator(n, n, n, p, nu, sg, dt=0.01)
