@@ -300,7 +300,7 @@ def run_ours(args):
     # ---- converged solves on the same problem: FP64 vs mixed (auxiliary-space PCG) ----
     solves = None
     if args.solves > 0:
-        solves = measure_solves(op, args.solves, args.solve_rtol)
+        solves = measure_solves(op, args.solves, args.solve_rtol, args.inner_rtol)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -338,7 +338,7 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def measure_solves(op, k, rtol):
+def measure_solves(op, k, rtol, inner=3e-4):
     """Coil right-hand side, both precisions, auxiliary-space preconditioner:
     time per converged solve (CUDA events around each solve on the handle's
     stream), iterations, and the mixed solution's relative difference from
@@ -352,7 +352,7 @@ def measure_solves(op, k, rtol):
     out, xs = {}, {}
     for prec in ("fp64", "mixed"):
         s = GpuHCurlPCGSolver({"Tolerance": rtol, "AbsTolerance": 0.0, "MaxIter": 5000, "Precision": prec,
-                               "Preconditioner": "aux"}, op)
+                               "Preconditioner": "aux", "InnerTolerance": inner}, op)
         x = torch.zeros_like(b)
         s.MultDevice(b, x)  # setup (hierarchy) + warm-up
         ts = []
@@ -377,6 +377,7 @@ def measure_solves(op, k, rtol):
     out["rhs"] = "loop-coil load vector, A x n = 0"
     out["preconditioner"] = "Jacobi + auxiliary-space gradient correction (HC_PRECOND_AUX)"
     out["rtol"] = rtol
+    out["inner_rtol"] = inner
     return out
 
 
@@ -388,7 +389,8 @@ def run_batch(args):
 
     dist_init()
     probs = B.make_batch(args.batch, seed=0)
-    base = {"Tolerance": args.solve_rtol, "AbsTolerance": 0.0, "MaxIter": 20000, "Preconditioner": "aux"}
+    base = {"Tolerance": args.solve_rtol, "AbsTolerance": 0.0, "MaxIter": 20000, "Preconditioner": "aux",
+            "InnerTolerance": args.inner_rtol}
     t0 = time.perf_counter()
     db = B.DeviceBatch(probs, dict(base, Precision="fp64"))
     setup_s = time.perf_counter() - t0
@@ -445,7 +447,7 @@ def run_serve(args):
     out = {}
     # service-time calibration: a few requests alone, then the rate that loads the GPU to ~80 %
     cal = SV.make_stream(8, rate=1.0, seed=99)
-    ex = SV.GpuExecutor(1, precision="mixed", rtol=args.solve_rtol)
+    ex = SV.GpuExecutor(1, precision="mixed", rtol=args.solve_rtol, inner_rtol=args.inner_rtol)
     t0 = time.perf_counter()
     for r in cal:
         ex(r, 0)
@@ -453,7 +455,7 @@ def run_serve(args):
     rate = 0.8 / mean_service
     for prec in ("fp64", "mixed"):
         reqs = SV.make_stream(args.requests, rate=rate, seed=7)
-        ex = SV.GpuExecutor(args.slots, precision=prec, rtol=args.solve_rtol, keep=False)
+        ex = SV.GpuExecutor(args.slots, precision=prec, rtol=args.solve_rtol, keep=False, inner_rtol=args.inner_rtol)
         done, wall = SV.run_stream(reqs, ex, budget_bytes=budget, slots=args.slots)
         steps = sum(r.steps for r in done)
         st = SV.latency_stats(done)
@@ -540,7 +542,9 @@ def main():
     ap.add_argument("--cpu-step-seconds", type=float, default=1.0)
     ap.add_argument("--workload", default="apply", choices=["apply", "batch", "serve", "tets"])
     ap.add_argument("--solves", type=int, default=2, help="timed converged solves per precision (0: skip)")
-    ap.add_argument("--solve-rtol", type=float, default=1e-12)
+    ap.add_argument("--solve-rtol", type=float, default=1e-10,
+                    help="relative residual of every solve; the mixed result is checked against FP64 (<= 1e-10)")
+    ap.add_argument("--inner-rtol", type=float, default=3e-4, help="FP32 inner solve tolerance of the mixed path")
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--requests", type=int, default=2000)
     ap.add_argument("--slots", type=int, default=8)

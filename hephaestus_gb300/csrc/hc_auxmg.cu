@@ -180,9 +180,15 @@ __global__ void k_stencil(Dims d, const float* __restrict__ Ke, float* __restric
 struct NodeGrid {
   dim3 grid, block;
 };
+// rows of w nodes split into equal blocks of at most 256 threads (a row of
+// 129 becomes one block of 160, not 128 + 1)
+static inline int row_block(int w) {
+  const int nb = (w + 255) / 256;
+  return ((w + nb - 1) / nb + 31) / 32 * 32;
+}
 static inline NodeGrid node_grid(int nx, int ny, int nz) {
   const int w = nx + 1;
-  const int bx = w >= 128 ? 128 : ((w + 31) / 32) * 32;
+  const int bx = row_block(w);
   return NodeGrid{dim3((unsigned)((w + bx - 1) / bx), (unsigned)(ny + 1), (unsigned)(nz + 1)), dim3((unsigned)bx)};
 }
 #define NODE_IJK(d, i, j, k, n)                                              \
@@ -916,12 +922,12 @@ static void aux_apply_p(const hcop* h, AuxMG* M, const T* r0, const T* r1, T* z0
   k_gt<T, NV, P><<<gq.grid, gq.block, 0, s>>>(hd, M->tab, r0, r1, qd, g, P > 1 ? none : start_of(L0), done);
   if (P > 1) k_rq<NV, P><<<g1.grid, g1.block, 0, s>>>(L0.d, M->tab, g, L0.dinv, L0.b, start_of(L0), done);
   vcycle<NV>(h, M, 0, done, s);
-  const float* phi = L0.x;
+  const float* phi = L0.x;  // order 1: phi is the finest Q1 level's x
   if (P > 1) {
     k_pq<NV, P><<<gq.grid, gq.block, 0, s>>>(L0.d, M->tab, g, M->qdinv, L0.x, M->phi, done);
     phi = M->phi;
   }
-  // one launch per Nedelec component (grid open along c)
+  // z += C G phi, one launch per Nedelec component (grid open along c)
   const NodeGrid c0 = node_grid(mx - 1, my, mz), c1 = node_grid(mx, my - 1, mz), c2 = node_grid(mx, my, mz - 1);
   k_g<T, NV, P, 0><<<c0.grid, c0.block, 0, s>>>(hd, M->tab, phi, h->ess, z0, z1, coef[0], coef[1], coef[2], coef[3],
                                                 done);

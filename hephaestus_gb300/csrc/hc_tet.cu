@@ -299,12 +299,96 @@ __device__ __forceinline__ float kval(float v) { return v; }
 __device__ __forceinline__ double kval(double v) { return v; }
 __device__ __forceinline__ float kval(__nv_bfloat16 v) { return __bfloat162float(v); }
 
-// K holds the element matrices in TK (double, float, or bf16 with FP32 vectors)
-template <typename T, int L, typename TK = T>
-__global__ void __launch_bounds__(256) tet_apply_kernel(int64_t ne, const int32_t* __restrict__ edofs,
-                                                        const TK* __restrict__ K, const uint8_t* __restrict__ ess,
-                                                        int masked, int nrhs, T scale, const T* __restrict__ x,
-                                                        T* __restrict__ y, const int* done) {
+// Y (+)= scale * P K P X for R right-hand sides ([dof][rhs] row-major).  One
+// warp per element: the element's X block (L x R) is staged once in shared
+// memory, lane i < L owns row i of the element matrix (read once, in TK =
+// double, float or bf16), accumulates its R outputs in registers and adds them
+// with R/4 128-bit atomics (FP32) or R scalar atomics (FP64).
+template <typename T, int L, int R, typename TK>
+__global__ void __launch_bounds__(256) tet_apply_rows(int64_t ne, const int32_t* __restrict__ edofs,
+                                                      const TK* __restrict__ K, const uint8_t* __restrict__ ess,
+                                                      int masked, T scale, const T* __restrict__ x,
+                                                      T* __restrict__ y, int vec_ok, const int* done) {
+  if (done && *done) return;
+  constexpr int W = 8;  // warps per block
+  __shared__ T xs_all[W][L * R];
+  __shared__ int sdof_all[W][L];
+  __shared__ unsigned char sess_all[W][L];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* xs = xs_all[wid];
+  int* sdof = sdof_all[wid];
+  unsigned char* sess = sess_all[wid];
+  for (int64_t e = (int64_t)blockIdx.x * W + wid; e < ne; e += (int64_t)gridDim.x * W) {
+    if (lane < L) {
+      const int d = __ldg(edofs + e * L + lane);
+      sdof[lane] = d;
+      sess[lane] = (masked && ess[d]) ? 1 : 0;
+    }
+    __syncwarp();
+    for (int idx = lane; idx < L * R; idx += 32) {
+      const int j = idx / R, r = idx - j * R;
+      T v = __ldg(x + (int64_t)sdof[j] * R + r);
+      if (sess[j]) v = T(0);
+      xs[idx] = v;
+    }
+    __syncwarp();
+    if (lane < L && !sess[lane]) {
+      T kr[L];
+      const TK* Krow = K + (e * L + lane) * L;
+      if constexpr (sizeof(TK) == 2 && L % 4 == 0) {
+        // 8-byte loads of 4 bf16
+#pragma unroll
+        for (int j = 0; j < L; j += 4) {
+          const uint2 v = __ldg(reinterpret_cast<const uint2*>(Krow) + j / 4);
+          const __nv_bfloat162 a = *reinterpret_cast<const __nv_bfloat162*>(&v.x);
+          const __nv_bfloat162 b = *reinterpret_cast<const __nv_bfloat162*>(&v.y);
+          const float2 fa = __bfloat1622float2(a), fb = __bfloat1622float2(b);
+          kr[j] = fa.x;
+          kr[j + 1] = fa.y;
+          kr[j + 2] = fb.x;
+          kr[j + 3] = fb.y;
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < L; ++j) kr[j] = (T)kval(Krow[j]);
+      }
+      T acc[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) acc[r] = T(0);
+#pragma unroll
+      for (int j = 0; j < L; ++j)
+#pragma unroll
+        for (int r = 0; r < R; ++r) acc[r] += kr[j] * xs[j * R + r];
+      T* yr = y + (int64_t)sdof[lane] * R;
+      if constexpr (sizeof(T) == 4 && R % 4 == 0) {
+        if (vec_ok) {
+#pragma unroll
+          for (int q = 0; q < R / 4; ++q)
+            atomicAdd(reinterpret_cast<float4*>(yr) + q,
+                      make_float4(scale * acc[4 * q], scale * acc[4 * q + 1], scale * acc[4 * q + 2],
+                                  scale * acc[4 * q + 3]));
+        } else {
+#pragma unroll
+          for (int r = 0; r < R; ++r) atomicAdd(yr + r, scale * acc[r]);
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r) atomicAdd(yr + r, scale * acc[r]);
+      }
+    }
+    __syncwarp();  // xs is rewritten for the next element
+  }
+}
+
+// FP64: all 32 lanes stay busy (the FP64 apply is bound by FP64 throughput):
+// lanes split into (right-hand side, row subset), element matrix rows read
+// by every lane of a subset.
+template <int L>
+__global__ void __launch_bounds__(256) tet_apply_lanes64(int64_t ne, const int32_t* __restrict__ edofs,
+                                                         const double* __restrict__ K,
+                                                         const uint8_t* __restrict__ ess, int masked, int nrhs,
+                                                         double scale, const double* __restrict__ x,
+                                                         double* __restrict__ y, const int* done) {
   if (done && *done) return;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -312,23 +396,44 @@ __global__ void __launch_bounds__(256) tet_apply_kernel(int64_t ne, const int32_
   const int r = lane % nrhs, part = lane / nrhs;
   for (int64_t e = warp; e < ne; e += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     int dof[L];
-    T xe[L];
+    double xe[L];
 #pragma unroll
     for (int j = 0; j < L; ++j) {
       dof[j] = __ldg(edofs + e * L + j);
-      T v = __ldg(x + (int64_t)dof[j] * nrhs + r);
-      if (masked && ess[dof[j]]) v = T(0);
+      double v = __ldg(x + (int64_t)dof[j] * nrhs + r);
+      if (masked && ess[dof[j]]) v = 0.0;
       xe[j] = v;
     }
-    const TK* Ke = K + e * L * L;
+    const double* Ke = K + e * L * L;
     for (int i = part; i < L; i += nparts) {
       if (masked && ess[dof[i]]) continue;
-      T acc = T(0);
+      double acc = 0.0;
 #pragma unroll
-      for (int j = 0; j < L; ++j) acc += (T)kval(Ke[i * L + j]) * xe[j];
+      for (int j = 0; j < L; ++j) acc += __ldg(Ke + i * L + j) * xe[j];
       atomicAdd(y + (int64_t)dof[i] * nrhs + r, scale * acc);
     }
   }
+}
+
+template <typename T, int L, typename TK>
+static cudaError_t tet_rows_launch(const hcop* h, const TK* K, const T* x, T* y, int nrhs, bool masked, T scale,
+                                   const int* done, cudaStream_t s) {
+  const int W = 8;
+  int64_t blocks = (h->ne + W - 1) / W;
+  blocks = std::min<int64_t>(blocks, 152 * 16);
+  const int vec_ok = ((uintptr_t)y % 16) == 0 ? 1 : 0;
+  const int m = masked ? 1 : 0;
+  const unsigned b = (unsigned)blocks;
+  switch (nrhs) {
+    case 1: tet_apply_rows<T, L, 1, TK><<<b, 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess, m, scale, x, y, vec_ok, done); break;
+    case 2: tet_apply_rows<T, L, 2, TK><<<b, 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess, m, scale, x, y, vec_ok, done); break;
+    case 4: tet_apply_rows<T, L, 4, TK><<<b, 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess, m, scale, x, y, vec_ok, done); break;
+    case 8: tet_apply_rows<T, L, 8, TK><<<b, 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess, m, scale, x, y, vec_ok, done); break;
+    case 16: tet_apply_rows<T, L, 16, TK><<<b, 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess, m, scale, x, y, vec_ok, done); break;
+    case 32: tet_apply_rows<T, L, 32, TK><<<b, 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess, m, scale, x, y, vec_ok, done); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
 }
 
 template <typename T>
@@ -338,16 +443,20 @@ cudaError_t tet_apply_launch(const hcop* h, const T* K, const T* x, T* y, int nr
     const cudaError_t prior = cudaGetLastError();  // report a failure of an earlier call
     if (prior != cudaSuccess) return prior;
   }
-  const int warps_per_block = 8;
-  int64_t blocks = (h->ne + warps_per_block - 1) / warps_per_block;
-  blocks = std::min<int64_t>(blocks, 152 * 16);
-  if (h->p == 1)
-    tet_apply_kernel<T, 6><<<(unsigned)blocks, 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess, masked ? 1 : 0,
-                                                            nrhs, (T)scale, x, y, done);
-  else
-    tet_apply_kernel<T, 20><<<(unsigned)blocks, 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess, masked ? 1 : 0,
-                                                             nrhs, (T)scale, x, y, done);
-  return cudaGetLastError();
+  if constexpr (sizeof(T) == 8) {
+    int64_t blocks = (h->ne + 7) / 8;
+    blocks = std::min<int64_t>(blocks, 152 * 16);
+    if (h->p == 1)
+      tet_apply_lanes64<6><<<(unsigned)blocks, 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess, masked ? 1 : 0, nrhs,
+                                                            scale, x, y, done);
+    else
+      tet_apply_lanes64<20><<<(unsigned)blocks, 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess, masked ? 1 : 0, nrhs,
+                                                             scale, x, y, done);
+    return cudaGetLastError();
+  } else {
+    if (h->p == 1) return tet_rows_launch<T, 6, T>(h, K, x, y, nrhs, masked, (T)scale, done, s);
+    return tet_rows_launch<T, 20, T>(h, K, x, y, nrhs, masked, (T)scale, done, s);
+  }
 }
 template cudaError_t tet_apply_launch<double>(const hcop*, const double*, const double*, double*, int, bool, double,
                                               const int*, cudaStream_t);
@@ -356,17 +465,9 @@ template cudaError_t tet_apply_launch<float>(const hcop*, const float*, const fl
 
 // FP32 vectors with BF16 element matrices (FP32 accumulation)
 cudaError_t tet_apply_launch_bf16(const hcop* h, const float* x, float* y, int nrhs, bool masked, cudaStream_t s) {
-  const int warps_per_block = 8;
-  int64_t blocks = (h->ne + warps_per_block - 1) / warps_per_block;
-  blocks = std::min<int64_t>(blocks, 152 * 16);
   const __nv_bfloat16* K = static_cast<const __nv_bfloat16*>(h->tetK16);
-  if (h->p == 1)
-    tet_apply_kernel<float, 6, __nv_bfloat16><<<(unsigned)blocks, 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess,
-                                                                             masked ? 1 : 0, nrhs, 1.0f, x, y, nullptr);
-  else
-    tet_apply_kernel<float, 20, __nv_bfloat16><<<(unsigned)blocks, 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess,
-                                                                              masked ? 1 : 0, nrhs, 1.0f, x, y, nullptr);
-  return cudaGetLastError();
+  if (h->p == 1) return tet_rows_launch<float, 6, __nv_bfloat16>(h, K, x, y, nrhs, masked, 1.0f, nullptr, s);
+  return tet_rows_launch<float, 20, __nv_bfloat16>(h, K, x, y, nrhs, masked, 1.0f, nullptr, s);
 }
 
 __global__ void k_to_bf16(int64_t n, const double* __restrict__ a, __nv_bfloat16* __restrict__ b) {

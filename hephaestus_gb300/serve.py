@@ -209,7 +209,7 @@ class GpuExecutor:
     then takes its time steps with device-resident A, b, dA on a dedicated
     stream (one per worker)."""
 
-    def __init__(self, slots, precision="mixed", precond="aux", rtol=1e-12, dt=0.01, keep=False):
+    def __init__(self, slots, precision="mixed", precond="aux", rtol=1e-12, dt=0.01, keep=False, inner_rtol=3e-4):
         import torch
 
         self.torch = torch
@@ -220,6 +220,7 @@ class GpuExecutor:
         self.dt = dt
         self.keep = keep
         self.kept = {}
+        self.inner_rtol = inner_rtol
 
     def fields(self, req):
         from . import meshes
@@ -248,7 +249,8 @@ class GpuExecutor:
                 free = torch.tensor(op.ess_mask() == 0, device="cuda")
                 op.LoadCoilDevice(J, I0=I0)
                 s = GpuHCurlPCGSolver({"Tolerance": self.rtol, "AbsTolerance": 0.0, "MaxIter": 5000,
-                                       "Precision": self.precision, "Preconditioner": self.precond}, op)
+                                       "Precision": self.precision, "Preconditioner": self.precond,
+                                       "InnerTolerance": self.inner_rtol}, op)
                 its = []
                 for _ in range(req.steps):
                     b.copy_(J)
