@@ -382,7 +382,7 @@ def measure_solves(op, k, rtol, inner=3e-4):
 
 
 def run_batch(args):
-    """Config-4 style batch: uneven complex eddy-current solves, all in flight at once."""
+    """Batch of uneven complex eddy-current solves, all in flight at once."""
     import torch
 
     from hephaestus_gb300 import batch as B
@@ -436,7 +436,7 @@ def run_batch(args):
 
 
 def run_serve(args):
-    """Config-5 style serving: Poisson arrivals of transient A-formulation steps."""
+    """Serving: Poisson arrivals of transient A-formulation steps."""
     import torch
 
     from hephaestus_gb300 import serve as SV
@@ -474,10 +474,11 @@ def run_serve(args):
 
 
 def run_tets(args):
-    """Config-3 style tets: 48^3 Kuhn subdivision (6 tets per cube), interior
-    vertices jittered by U(-0.15h, 0.15h), Nedelec order 2; the eliminated
-    operator applied to 16 right-hand sides at once (element matrices stored
-    in FP32 and FP64)."""
+    """Tets: 48^3 Kuhn subdivision (6 tets per cube), interior vertices
+    jittered by U(-0.15h, 0.15h), Nedelec order 2; the eliminated operator
+    applied to 16 right-hand sides at once (element matrices stored in FP32,
+    FP64 and BF16), then 16 right-hand sides solved together (block PCG,
+    FP64 and FP32-inner/FP64-refinement) to the requested relative residual."""
     import torch
 
     from hephaestus_gb300 import HCurlOperator, meshes
@@ -516,13 +517,58 @@ def run_tets(args):
         alg = ne * 400 * kb + ne * 20 * 4 + 2 * op.ndof * nrhs * vb  # K, element dofs, X and Y
         out[name] = {"ms_per_apply": ms, "gdof_rhs_per_s": op.ndof * nrhs / (ms * 1e-3) / 1e9,
                      "alg_bytes": alg, "achieved_gbs": alg / (ms * 1e-3) / 1e9}
+    solves = tet_solves(args, op, nrhs) if args.solves > 0 else None
     line = {"metric": "GDoF/s x RHS, tet Nedelec p=2 element-matrix apply, 16 RHS",
             "value": out["fp32"]["gdof_rhs_per_s"], "unit": "GDoF*RHS/s", "n_gpus": 1, "higher_is_better": True,
             "config": {"workload": "tets48: Kuhn 48^3 (%d tets), jitter 0.15h, ND p=2, %d dofs, 16 RHS" % (ne, op.ndof),
                        "l2": "flushed between steps"},
             "fp32": out["fp32"], "fp64": out["fp64"], "bf16_matrices": out["bf16_matrices"],
-            "setup_seconds": setup_s}
+            "setup_seconds": setup_s, "solves": solves}
     print(json.dumps(line))
+
+
+def tet_solves(args, op, nrhs):
+    """16 seeded right-hand sides (standard normal, zero on essential rows)
+    solved together in FP64 and in mixed precision to args.solve_rtol; the
+    mixed solutions are checked against the FP64 ones column by column."""
+    import torch
+
+    from hephaestus_gb300 import GpuHCurlPCGSolver
+
+    g = torch.Generator(device="cuda")
+    g.manual_seed(1)
+    B = torch.randn(op.ndof, nrhs, dtype=torch.float64, device="cuda", generator=g)
+    B.mul_(torch.tensor(op.ess_mask() == 0, device="cuda")[:, None])
+    X = torch.zeros_like(B)
+    out, sols = {}, {}
+    for prec in ("fp64", "mixed"):
+        s = GpuHCurlPCGSolver({"Tolerance": args.solve_rtol, "AbsTolerance": 0.0, "MaxIter": 40000,
+                               "Precision": prec, "InnerTolerance": args.inner_rtol}, op)
+        ts = []
+        for k in range(max(1, args.solves)):
+            X.zero_()
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            res = s.MultMultiDevice(B, X)
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        sols[prec] = X.clone()
+        ms = float(np.mean(ts))
+        out[prec] = {"solves_per_s": nrhs / (ms * 1e-3), "ms_per_block_solve": ms,
+                     "iterations_max": max(r["iterations"] for r in res),
+                     "outer_iterations_max": max(r["outer_iterations"] for r in res),
+                     "status": sorted({r["status"] for r in res}),
+                     "rel_residual_max": max(r["rel_residual"] for r in res)}
+    err = torch.linalg.vector_norm(sols["mixed"] - sols["fp64"], dim=0) / torch.linalg.vector_norm(sols["fp64"], dim=0)
+    out["rel_err_mixed_vs_fp64_max"] = float(err.max())
+    out["speedup_mixed_over_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+    out["rhs"] = "%d seeded N(0,1) columns, zero on essential rows" % nrhs
+    out["preconditioner"] = "Jacobi (block PCG, one batched apply per iteration)"
+    out["rtol"] = args.solve_rtol
+    return out
 
 
 def op_full(op):

@@ -284,6 +284,7 @@ void hc_destroy(hcop_t* h) {
   cudaStreamSynchronize(h->stream);
   complex_free(h);
   auxmg_free(h);
+  multi_free(h);
   for (void* p : {(void*)h->fac, (void*)h->facf, (void*)h->ess, (void*)h->diag, (void*)h->dinv, (void*)h->dinvf,
                   (void*)h->sdinv, (void*)h->sdinvf, (void*)h->scal, (void*)h->partials, h->work, (void*)h->xbuf,
                   (void*)h->ybuf, (void*)h->verts, (void*)h->tet_edofs, (void*)h->tetK64, (void*)h->tetK32,

@@ -105,6 +105,7 @@ struct hcop {
   int* tab = nullptr;                  // brick tile table of the apply kernel
   void* cwork = nullptr;               // complex (frequency-domain) work space, hc_complex.cu
   void* aux = nullptr;                 // auxiliary-space preconditioner, hc_auxmg.cu
+  void* mwork = nullptr;               // multi-RHS block PCG work space, hc_multi.cu
 
   hc::HexDev hexdev() const {
     hc::HexDev d;
@@ -201,6 +202,12 @@ cudaError_t complex_apply(hcop* h, double omega, const T* xr, const T* xi, T* yr
 hc_status complex_solve_device(hcop* h, const hc_solve_params* prm, double omega, const double* br,
                                const double* bi, double* xr, double* xi, hc_solve_info* info);
 void complex_free(hcop* h);
+
+// ---- hc_multi.cu ----
+// block PCG (Jacobi) for R right-hand sides in [dof][rhs] layout (tet meshes)
+hc_status multi_solve_device(hcop* h, const hc_solve_params* prm, int R, const double* B, double* X,
+                             hc_solve_info* info);
+void multi_free(hcop* h);
 
 // ---- hc_krylov.cu ----
 cudaError_t diag_finish(int64_t n, const uint8_t* ess, double* d, double* dinv, float* dinvf, double* sd,

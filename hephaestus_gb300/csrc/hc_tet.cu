@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(256) tet_apply_rows(int64_t ne, const int32_t*
                                                       T* __restrict__ y, int vec_ok, const int* done) {
   if (done && *done) return;
   constexpr int W = 8;  // warps per block
-  __shared__ T xs_all[W][L * R];
+  __shared__ __align__(16) T xs_all[W][L * R];
   __shared__ int sdof_all[W][L];
   __shared__ unsigned char sess_all[W][L];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -355,10 +355,24 @@ __global__ void __launch_bounds__(256) tet_apply_rows(int64_t ne, const int32_t*
       T acc[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) acc[r] = T(0);
+      if constexpr (sizeof(T) == 4 && R % 4 == 0) {
+        // 128-bit shared-memory reads of the staged block (broadcast to all rows)
 #pragma unroll
-      for (int j = 0; j < L; ++j)
+        for (int j = 0; j < L; ++j)
 #pragma unroll
-        for (int r = 0; r < R; ++r) acc[r] += kr[j] * xs[j * R + r];
+          for (int r = 0; r < R; r += 4) {
+            const float4 xv = *reinterpret_cast<const float4*>(xs + j * R + r);
+            acc[r] += kr[j] * xv.x;
+            acc[r + 1] += kr[j] * xv.y;
+            acc[r + 2] += kr[j] * xv.z;
+            acc[r + 3] += kr[j] * xv.w;
+          }
+      } else {
+#pragma unroll
+        for (int j = 0; j < L; ++j)
+#pragma unroll
+          for (int r = 0; r < R; ++r) acc[r] += kr[j] * xs[j * R + r];
+      }
       T* yr = y + (int64_t)sdof[lane] * R;
       if constexpr (sizeof(T) == 4 && R % 4 == 0) {
         if (vec_ok) {

@@ -403,6 +403,25 @@ class GpuHCurlPCGSolver:
         self._check(st)
         return x
 
+    def MultMultiDevice(self, B, X):
+        """Solve J X = B for the columns of (ndof, nrhs) row-major float64 CUDA
+        tensors together (hc_solve_multi_device: block PCG, one batched
+        apply per iteration; tet meshes).  X holds the initial guesses and is
+        updated in place; returns the list of per-column result dicts."""
+        op = self.op
+        nrhs = 1 if B.dim() == 1 else int(B.shape[1])
+        if tuple(X.shape) != tuple(B.shape):
+            raise ValueError("B and X must have the same shape")
+        infos = (N.SolveInfo * nrhs)()
+        st = N.lib().hc_solve_multi_device(op.h, C.byref(self.p), nrhs, _dev_ptr(B, "float64"),
+                                           _dev_ptr(X, "float64"), infos)
+        self._check(st)
+        out = []
+        for i in infos:
+            self.info = i
+            out.append(self.result)
+        return out
+
     def _check(self, st):
         if st in (N.HC_OK,):
             return

@@ -197,13 +197,27 @@ hc_status hc_load_coil_device(hcop_t* h, const hc_coil* coil, int q, double* b);
  * pointers of the given precision (HC_FP64: double, HC_FP32 and HC_BF16:
  * float; HC_BF16 reads element matrices rounded to BF16, tets only);
  * nrhs in {1, 2, 4, 8, 16, 32}.  Tet meshes apply each element matrix to all
- * right-hand sides at once (config 3's batched element-matrix apply).      */
+ * right-hand sides at once (one element-matrix read serves every column). */
 hc_status hc_mult_multi_device(hcop_t* h, int precision, int nrhs, const void* X, void* Y);
 /* HC_HEX or HC_TET */
 int32_t hc_elem_type(const hcop_t* h);
 /* Tet meshes: the FP64 element matrix (L x L, L = 6 or 20) of element e,
  * rows/columns in the local dof order of the basis.                        */
 hc_status hc_tet_element_matrix(hcop_t* h, int64_t e, double* out);
+/* Solve J X = B for nrhs right-hand sides together (block PCG with Jacobi,
+ * one batched element-matrix apply per iteration for all columns), device
+ * pointers in the [dof][rhs] layout of hc_mult_multi_device; X holds the
+ * initial guesses.  Each column keeps its own alpha, beta and stopping test
+ * (max(rtol ||b_k||, atol)); a converged column is frozen while the others
+ * continue.  HC_FP64, or HC_MIXED: FP32 inner block PCG on column-normalised
+ * residuals inside FP64 iterative refinement, with an FP64 block PCG from
+ * the refined X when a refinement step stops cutting the residuals.  info
+ * holds nrhs reports; returns the first non-OK column status.  Tet meshes;
+ * nrhs in {1, 2, 4, 8, 16, 32}; precond HC_PRECOND_JACOBI.  Replaces R
+ * separate HyprePCG solves of the same operator
+ * (hcurl_formulation.cpp:81-85, problem_builder_base.cpp:221-253).        */
+hc_status hc_solve_multi_device(hcop_t* h, const hc_solve_params* prm, int32_t nrhs, const double* B, double* X,
+                                hc_solve_info* info);
 
 /* ---- frequency domain: A = C_nu + i omega M_sigma ------------------------------
  * The complex operator of ComplexMaxwellOperator::Solve
@@ -239,7 +253,7 @@ hc_status hc_solve_complex_device(hcop_t* h, const hc_solve_params* prm, double 
 hc_status hc_solve_complex_graph(hcop_t* h, const hc_solve_params* prm, double omega, const double* br,
                                  const double* bi, double* xr, double* xi);
 hc_status hc_graph_solve_info(hcop_t* h, hc_solve_info* info);
-/* n independent complex solves (config-4 style batches of uneven problems):
+/* n independent complex solves (batches of uneven problems):
  * every graph is enqueued first, then all are collected, so solves on
  * handles with distinct streams (hc_set_stream) run concurrently.  info[i]
  * gets each solve's report; returns the first non-OK status.               */
