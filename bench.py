@@ -527,18 +527,33 @@ def run_tets(args):
     print(json.dumps(line))
 
 
+def tet_coil_rhs(op, nrhs, seed):
+    """(ndof, nrhs) device matrix of coil loads (zero on essential rows)."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    B = torch.empty(op.ndof, nrhs, dtype=torch.float64, device="cuda")
+    col = torch.empty(op.ndof, dtype=torch.float64, device="cuda")
+    free = torch.tensor(op.ess_mask() == 0, device="cuda")
+    for k in range(nrhs):
+        I0 = float(rng.uniform(0.5, 2.0))
+        xc, yc = 0.5 + rng.uniform(-0.1, 0.1, size=2)
+        op.LoadCoilDevice(col, I0=I0, xc=float(xc), yc=float(yc), q=4)
+        B[:, k] = col * free
+    torch.cuda.synchronize()
+    return B
+
+
 def tet_solves(args, op, nrhs):
-    """16 seeded right-hand sides (standard normal, zero on essential rows)
-    solved together in FP64 and in mixed precision to args.solve_rtol; the
-    mixed solutions are checked against the FP64 ones column by column."""
+    """16 loop-coil right-hand sides (I0 uniform in [0.5, 2], coil centre
+    shifted uniformly by up to +-0.1 in x and y, seeded; zero on essential
+    rows) solved together in FP64 and in mixed precision to args.solve_rtol;
+    the mixed solutions are checked against the FP64 ones column by column."""
     import torch
 
     from hephaestus_gb300 import GpuHCurlPCGSolver
 
-    g = torch.Generator(device="cuda")
-    g.manual_seed(1)
-    B = torch.randn(op.ndof, nrhs, dtype=torch.float64, device="cuda", generator=g)
-    B.mul_(torch.tensor(op.ess_mask() == 0, device="cuda")[:, None])
+    B = tet_coil_rhs(op, nrhs, seed=1)
     X = torch.zeros_like(B)
     out, sols = {}, {}
     for prec in ("fp64", "mixed"):
@@ -565,7 +580,7 @@ def tet_solves(args, op, nrhs):
     err = torch.linalg.vector_norm(sols["mixed"] - sols["fp64"], dim=0) / torch.linalg.vector_norm(sols["fp64"], dim=0)
     out["rel_err_mixed_vs_fp64_max"] = float(err.max())
     out["speedup_mixed_over_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
-    out["rhs"] = "%d seeded N(0,1) columns, zero on essential rows" % nrhs
+    out["rhs"] = "%d loop coils, I0 ~ U[0.5, 2], centre (0.5, 0.5) + U[-0.1, 0.1]^2, seeded" % nrhs
     out["preconditioner"] = "Jacobi (block PCG, one batched apply per iteration)"
     out["rtol"] = args.solve_rtol
     return out

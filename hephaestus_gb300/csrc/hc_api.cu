@@ -287,7 +287,7 @@ void hc_destroy(hcop_t* h) {
   multi_free(h);
   for (void* p : {(void*)h->fac, (void*)h->facf, (void*)h->ess, (void*)h->diag, (void*)h->dinv, (void*)h->dinvf,
                   (void*)h->sdinv, (void*)h->sdinvf, (void*)h->scal, (void*)h->partials, h->work, (void*)h->xbuf,
-                  (void*)h->ybuf, (void*)h->verts, (void*)h->tet_edofs, (void*)h->tetK64, (void*)h->tetK32,
+                  (void*)h->ybuf, (void*)h->verts, (void*)h->tet_edofs, (void*)h->tet_sv, (void*)h->tetK64, (void*)h->tetK32,
                   h->tetK16, (void*)h->tab})
     dfree(h, p);
   pinned_put(h->hscal);
@@ -677,13 +677,16 @@ hc_status hc_curl(hcop_t* h, const double* A, double* B) {
 }
 
 hc_status hc_load_coil_device(hcop_t* h, const hc_coil* coil, int q, double* b) {
-  if (h && h->type != HC_HEX) {
-    h->err = "hc_load_coil: structured hex grids only in this build";
-    return HC_ENOTSUP;
-  }
   if (!h || !coil || !b || q < 1 || q > 8) {
     if (h) h->err = "hc_load_coil: need a coil and 1 <= q <= 8";
     return HC_EINVAL;
+  }
+  if (h->type == HC_TET) {
+    std::vector<double> xq(q), wq(q);
+    gl01(q, xq.data(), wq.data());
+    const double cv[7] = {coil->I0, coil->xc, coil->yc, coil->r0, coil->r1, coil->z0, coil->z1};
+    HC_CUDA_TRY(h, tet_load_coil(h, cv, q, xq.data(), wq.data(), b, h->stream));
+    return HC_OK;
   }
   std::vector<double> xq(q), wq(q), bc(q * (h->p + 1)), bo(q * h->p);
   gl01(q, xq.data(), wq.data());

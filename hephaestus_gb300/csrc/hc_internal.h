@@ -99,6 +99,7 @@ struct hcop {
   // tetrahedral meshes
   int64_t n_edges = 0, n_faces = 0;
   int32_t* tet_edofs = nullptr;        // ne * L element dofs
+  int32_t* tet_sv = nullptr;           // ne * 4 element vertices, sorted by global index
   double* tetK64 = nullptr;            // ne * L * L element matrices (FP64)
   float* tetK32 = nullptr;             // FP32 copy
   void* tetK16 = nullptr;              // BF16 copy (made on first use)
@@ -174,6 +175,9 @@ cudaError_t tet_apply_launch(const hcop* h, const T* K, const T* x, T* y, int nr
                              const int* done, cudaStream_t s);
 cudaError_t tet_ensure_bf16(hcop* h);
 cudaError_t tet_apply_launch_bf16(const hcop* h, const float* x, float* y, int nrhs, bool masked, cudaStream_t s);
+// b = coil load (I0, xc, yc, r0, r1, z0, z1) with a q^3 collapsed Gauss-Legendre rule per tet (1 <= q <= 8)
+cudaError_t tet_load_coil(const hcop* h, const double coil[7], int q, const double* xq, const double* wq, double* b,
+                          cudaStream_t s);
 // pq = p.q over all dofs, then alpha = rz / pq (PCG mode of operators without a fused energy)
 template <typename T>
 cudaError_t dot_alpha(int64_t n, const T* p, const T* q, KrylovScalars* S, double* partials, cudaStream_t s);

@@ -553,12 +553,113 @@ cudaError_t tet_setup_device(hcop* h, const hc_problem_desc* desc, const std::ve
     }
   }
   cudaStreamSynchronize(cs);
-  dfree(h, V);
-  dfree(h, dsv);
+  // vertices and sorted element vertices stay resident (load vectors)
+  h->verts = V;
+  h->tet_sv = dsv;
   dfree(h, dnu);
   dfree(h, dsig);
   dfree(h, bad);
   return e;
+}
+
+// ---- coil load b_i = (J, W_i) -------------------------------------------------------
+// Collapsed (Duffy) Gauss-Legendre rule with q^3 points per tet: lambda_1 = u,
+// lambda_2 = v (1 - u), lambda_3 = t (1 - u)(1 - v), weight w_u w_v w_t (1 - u)^2 (1 - v)
+// (weights sum to 1/6), times |det J|.  One thread per element; the element
+// vector is scattered with atomic adds.
+struct TetQuad {
+  int q;
+  double x[8], w[8];
+  double coil[7];  // I0, xc, yc, r0, r1, z0, z1
+};
+
+template <int L>
+__global__ void __launch_bounds__(128) tet_load_coil_kernel(int64_t ne, int p, const double* __restrict__ V,
+                                                            const int32_t* __restrict__ sv,
+                                                            const int32_t* __restrict__ edofs, TetQuad Q,
+                                                            double* __restrict__ b) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  double vx[4][3];
+  for (int k = 0; k < 4; ++k)
+    for (int r = 0; r < 3; ++r) vx[k][r] = V[3 * (int64_t)sv[4 * e + k] + r];
+  double J[9];
+  for (int c = 0; c < 3; ++c)
+    for (int r = 0; r < 3; ++r) J[3 * r + c] = vx[c + 1][r] - vx[0][r];
+  const double det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) +
+                     J[2] * (J[3] * J[7] - J[4] * J[6]);
+  double gl[4][3];
+  gl[1][0] = (J[4] * J[8] - J[5] * J[7]) / det;
+  gl[1][1] = (J[2] * J[7] - J[1] * J[8]) / det;
+  gl[1][2] = (J[1] * J[5] - J[2] * J[4]) / det;
+  gl[2][0] = (J[5] * J[6] - J[3] * J[8]) / det;
+  gl[2][1] = (J[0] * J[8] - J[2] * J[6]) / det;
+  gl[2][2] = (J[2] * J[3] - J[0] * J[5]) / det;
+  gl[3][0] = (J[3] * J[7] - J[4] * J[6]) / det;
+  gl[3][1] = (J[1] * J[6] - J[0] * J[7]) / det;
+  gl[3][2] = (J[0] * J[4] - J[1] * J[3]) / det;
+  for (int r = 0; r < 3; ++r) gl[0][r] = -(gl[1][r] + gl[2][r] + gl[3][r]);
+  const double adet = fabs(det);
+  const double I0 = Q.coil[0], xc = Q.coil[1], yc = Q.coil[2], r0 = Q.coil[3], r1 = Q.coil[4], z0 = Q.coil[5],
+               z1 = Q.coil[6];
+  double be[L];
+#pragma unroll
+  for (int i = 0; i < L; ++i) be[i] = 0.0;
+  for (int ia = 0; ia < Q.q; ++ia)
+    for (int ib = 0; ib < Q.q; ++ib)
+      for (int ic = 0; ic < Q.q; ++ic) {
+        const double u = Q.x[ia], v = Q.x[ib], t = Q.x[ic];
+        double lam[4];
+        lam[1] = u;
+        lam[2] = v * (1 - u);
+        lam[3] = t * (1 - u) * (1 - v);
+        lam[0] = 1.0 - lam[1] - lam[2] - lam[3];
+        double x[3];
+        for (int r = 0; r < 3; ++r)
+          x[r] = vx[0][r] + lam[1] * (vx[1][r] - vx[0][r]) + lam[2] * (vx[2][r] - vx[0][r]) +
+                 lam[3] * (vx[3][r] - vx[0][r]);
+        const double dx = x[0] - xc, dy = x[1] - yc;
+        const double rr = sqrt(dx * dx + dy * dy);
+        if (!(rr >= r0 && rr <= r1 && x[2] >= z0 && x[2] <= z1)) continue;
+        const double wq = Q.w[ia] * Q.w[ib] * Q.w[ic] * (1 - u) * (1 - u) * (1 - v) * adet;
+        const double f0 = -I0 * dy * wq, f1 = I0 * dx * wq;
+#pragma unroll
+        for (int I = 0; I < L; ++I) {
+          VTerm vt[2];
+          CTerm ct[3];
+          int nv, nc;
+          basis_terms(p, I, vt, &nv, ct, &nc);
+          double acc = 0.0;
+          for (int k = 0; k < nv; ++k) {
+            const double m = vt[k].c * (vt[k].l0 >= 0 ? lam[vt[k].l0] : 1.0) * lam[vt[k].l1];
+            acc += m * (f0 * gl[vt[k].g][0] + f1 * gl[vt[k].g][1]);
+          }
+          be[I] += acc;
+        }
+      }
+#pragma unroll
+  for (int i = 0; i < L; ++i)
+    if (be[i] != 0.0) atomicAdd(b + edofs[e * L + i], be[i]);
+}
+
+cudaError_t tet_load_coil(const hcop* h, const double coil[7], int q, const double* xq, const double* wq, double* b,
+                          cudaStream_t s) {
+  if (!h->verts || !h->tet_sv || q < 1 || q > 8) return cudaErrorInvalidValue;
+  TetQuad Q;
+  Q.q = q;
+  for (int k = 0; k < 8; ++k) {
+    Q.x[k] = k < q ? xq[k] : 0.0;
+    Q.w[k] = k < q ? wq[k] : 0.0;
+  }
+  for (int k = 0; k < 7; ++k) Q.coil[k] = coil[k];
+  cudaError_t e = cudaMemsetAsync(b, 0, h->ndof * sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  const unsigned blocks = (unsigned)((h->ne + 127) / 128);
+  if (h->p == 1)
+    tet_load_coil_kernel<6><<<blocks, 128, 0, s>>>(h->ne, 1, h->verts, h->tet_sv, h->tet_edofs, Q, b);
+  else
+    tet_load_coil_kernel<20><<<blocks, 128, 0, s>>>(h->ne, 2, h->verts, h->tet_sv, h->tet_edofs, Q, b);
+  return cudaGetLastError();
 }
 
 }  // namespace hc

@@ -184,8 +184,9 @@ hc_status hc_curl_device(hcop_t* h, const double* A, double* B);
 hc_status hc_curl_static(hcop_t* h, const double* A, double* B);
 
 /* Loop coil J = I0 (-(y-yc), x-xc, 0) for r0 <= r <= r1, z0 <= z <= z1 (r about
- * (xc, yc)), else 0.  b_i = (J, w_i) with a q^3 Gauss-Legendre rule per hex
- * (1 <= q <= 8): the right-hand side DivFreeSource adds
+ * (xc, yc)), else 0.  b_i = (J, w_i) with a q^3 Gauss-Legendre rule per hex,
+ * or the q^3 collapsed (Duffy) Gauss-Legendre rule per tet (1 <= q <= 8):
+ * the right-hand side DivFreeSource adds
  * (src/sources/div_free_source.cpp:72-114).                                  */
 typedef struct {
   double I0, xc, yc, r0, r1, z0, z1;

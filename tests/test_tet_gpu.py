@@ -178,3 +178,15 @@ def test_tet_multi_rhs_solve_initial_guess_and_single_column_agree():
         assert res[r]["status"] == "OK" and s1.result["status"] == "OK"
         assert np.linalg.norm(X[:, r] - x1) / np.linalg.norm(x1) < 1e-10, r
         assert np.array_equal(X[m, r], X0[m, r])
+
+
+@pytest.mark.parametrize("p", [1, 2])
+def test_tet_coil_load_matches_oracle(p):
+    """Device coil load on tets (collapsed Gauss-Legendre rule) = the oracle's
+    load with the same rule, for a shifted coil and two rule sizes."""
+    op, ref, _ = _pair(4, p)
+    for q in (3, 5):
+        b = op.LoadCoil(I0=1.3, xc=0.56, yc=0.45, q=q)
+        br = ref.load_coil(I0=1.3, xc=0.56, yc=0.45, q=q)
+        assert np.count_nonzero(br) > 0
+        assert np.linalg.norm(b - br) <= 1e-13 * np.linalg.norm(br), q
