@@ -558,7 +558,7 @@ def tet_solves(args, op, nrhs):
     out, sols = {}, {}
     for prec in ("fp64", "mixed"):
         s = GpuHCurlPCGSolver({"Tolerance": args.solve_rtol, "AbsTolerance": 0.0, "MaxIter": 40000,
-                               "Precision": prec, "InnerTolerance": args.inner_rtol}, op)
+                               "Precision": prec, "InnerTolerance": args.inner_rtol, "Preconditioner": "aux"}, op)
         ts = []
         for k in range(max(1, args.solves)):
             X.zero_()
@@ -581,7 +581,8 @@ def tet_solves(args, op, nrhs):
     out["rel_err_mixed_vs_fp64_max"] = float(err.max())
     out["speedup_mixed_over_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
     out["rhs"] = "%d loop coils, I0 ~ U[0.5, 2], centre (0.5, 0.5) + U[-0.1, 0.1]^2, seeded" % nrhs
-    out["preconditioner"] = "Jacobi (block PCG, one batched apply per iteration)"
+    out["preconditioner"] = ("Jacobi + gradient-space correction (PG) V (PG)^T, V = one smoothed-aggregation AMG "
+                             "V-cycle on the P1 nodal operator, all columns at once (block PCG)")
     out["rtol"] = args.solve_rtol
     return out
 

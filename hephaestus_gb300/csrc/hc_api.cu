@@ -214,6 +214,7 @@ static hc_status create_tet(const hc_problem_desc* desc, hcop_t** out) {
   h->type = HC_TET;
   h->p = desc->order;
   h->ne = desc->n_elem;
+  h->n_vert = desc->n_vert;
   h->dt = desc->dt;
   h->has_mass = desc->sigma != nullptr;
   std::vector<int32_t> edofs, sv;
@@ -285,6 +286,7 @@ void hc_destroy(hcop_t* h) {
   complex_free(h);
   auxmg_free(h);
   multi_free(h);
+  tetaux_free(h);
   for (void* p : {(void*)h->fac, (void*)h->facf, (void*)h->ess, (void*)h->diag, (void*)h->dinv, (void*)h->dinvf,
                   (void*)h->sdinv, (void*)h->sdinvf, (void*)h->scal, (void*)h->partials, h->work, (void*)h->xbuf,
                   (void*)h->ybuf, (void*)h->verts, (void*)h->tet_edofs, (void*)h->tet_sv, (void*)h->tetK64, (void*)h->tetK32,
@@ -703,6 +705,16 @@ hc_status hc_load_coil_device(hcop_t* h, const hc_coil* coil, int q, double* b) 
   return HC_OK;
 }
 
+hc_status hc_tet_gradient_device(hcop_t* h, const double* u, double* y) {
+  if (!h || !u || !y) return HC_EINVAL;
+  if (h->type != HC_TET) {
+    h->err = "hc_tet_gradient_device: tet meshes only";
+    return HC_ENOTSUP;
+  }
+  HC_CUDA_TRY(h, tet_gradient(h, u, y, h->stream));
+  return HC_OK;
+}
+
 hc_status hc_load_coil(hcop_t* h, const hc_coil* coil, int q, double* b) {
   if (!h || !b) return HC_EINVAL;
   hc_status st = hc_load_coil_device(h, coil, q, h->ybuf);
@@ -748,6 +760,8 @@ hc_status hc_solve_device(hcop_t* h, const hc_solve_params* prm, const double* b
   hc_solve_info loc{};
   if (!info) info = &loc;
   std::memset(info, 0, sizeof(*info));
+  if (prm->precond == HC_PRECOND_AUX && h->type == HC_TET)  // one-column block PCG with the tet AMG
+    return multi_solve_device(h, prm, 1, b, x, info);
   if (prm->precond == HC_PRECOND_AUX) {
     st = auxmg_setup(h);
     if (st != HC_OK) return st;

@@ -107,6 +107,8 @@ struct hcop {
   void* cwork = nullptr;               // complex (frequency-domain) work space, hc_complex.cu
   void* aux = nullptr;                 // auxiliary-space preconditioner, hc_auxmg.cu
   void* mwork = nullptr;               // multi-RHS block PCG work space, hc_multi.cu
+  void* taux = nullptr;                // tet auxiliary-space preconditioner, hc_tetaux.cu
+  int64_t n_vert = 0;                  // tet meshes: vertices
 
   hc::HexDev hexdev() const {
     hc::HexDev d;
@@ -212,6 +214,18 @@ void complex_free(hcop* h);
 hc_status multi_solve_device(hcop* h, const hc_solve_params* prm, int R, const double* B, double* X,
                              hc_solve_info* info);
 void multi_free(hcop* h);
+
+// ---- hc_tetaux.cu ----
+// gradient-space (auxiliary) preconditioner of tet meshes: AMG setup once per handle
+hc_status tetaux_setup(hcop* h);
+void tetaux_free(hcop* h);
+// work vectors for R right-hand sides (call before applying with R columns)
+hc_status tetaux_reserve(hcop* h, int R);
+// z = D^-1 r + (PG) V (PG)^T r for R columns in [dof][rhs] layout; skipped when *done
+template <typename T>
+cudaError_t tetaux_apply(const hcop* h, int R, const T* r, T* z, const T* dinv, const int* done, cudaStream_t s);
+// y = G u: discrete gradient of vertex values u (P1) into the Nedelec space
+cudaError_t tet_gradient(const hcop* h, const double* u, double* y, cudaStream_t s);
 
 // ---- hc_krylov.cu ----
 cudaError_t diag_finish(int64_t n, const uint8_t* ess, double* d, double* dinv, float* dinvf, double* sd,

@@ -7,8 +7,10 @@
 // segmented by right-hand side and deterministic: with a grid stride that is a
 // multiple of R every thread touches a single right-hand side (tid % R); warp
 // shuffles over lane offsets >= R, fixed-order block and last-block grid sums.
-// Preconditioner: Jacobi (the operator diagonal).  A converged right-hand side
-// is frozen (alpha = 0, direction zeroed) while the others continue.
+// Preconditioner: Jacobi (the operator diagonal), or Jacobi plus the
+// gradient-space AMG correction of hc_tetaux.cu applied to all columns at once.
+// A converged right-hand side is frozen (alpha = 0, direction zeroed) while the
+// others continue.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -121,15 +123,16 @@ __global__ void __launch_bounds__(kMThreads)
   }
 }
 
-// p = D^-1 r + beta p (p = 0 for a stopped rhs); q = (I - P) p
+// p = z + beta p with z = B r (z == nullptr: z = D^-1 r; p = 0 for a stopped rhs); q = (I - P) p
 template <typename T>
-__global__ void k_m_dir(int64_t n, int R, const T* __restrict__ r, const T* __restrict__ dinv, T* __restrict__ p,
-                        T* __restrict__ q, const uint8_t* __restrict__ ess, const MScalars* S) {
+__global__ void k_m_dir(int64_t n, int R, const T* __restrict__ r, const T* __restrict__ z, const T* __restrict__ dinv,
+                        T* __restrict__ p, T* __restrict__ q, const uint8_t* __restrict__ ess, const MScalars* S) {
   if (S->all_done) return;
   M_LOOP(i, n, R) {
     const int k = (int)(i % R);
     const int64_t d = i / R;
-    const T pi = S->done[k] ? T(0) : dinv[d] * r[i] + (T)S->beta[k] * p[i];
+    const T zi = z ? z[i] : dinv[d] * r[i];
+    const T pi = S->done[k] ? T(0) : zi + (T)S->beta[k] * p[i];
     p[i] = pi;
     q[i] = ess[d] ? pi : T(0);
   }
@@ -160,11 +163,11 @@ __global__ void __launch_bounds__(kMThreads)
   }
 }
 
-// x += alpha p; r -= alpha q; rr, rz per rhs; stopping tests; beta
+// x += alpha p; r -= alpha q; rr per rhs and stopping tests; jac: rz = r.D^-1 r and beta
 template <typename T>
 __global__ void __launch_bounds__(kMThreads)
     k_m_update(int64_t n, int R, T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
-               const T* __restrict__ q, const T* __restrict__ dinv, MScalars* S, double* partials) {
+               const T* __restrict__ q, const T* __restrict__ dinv, int jac, MScalars* S, double* partials) {
   if (S->all_done) return;
   double v[2] = {0, 0};
   M_LOOP(i, n, R) {
@@ -174,7 +177,7 @@ __global__ void __launch_bounds__(kMThreads)
     const T ri = r[i] - a * q[i];
     r[i] = ri;
     v[0] += (double)ri * (double)ri;
-    v[1] += (double)ri * (double)ri * (double)dinv[i / R];
+    if (jac) v[1] += (double)ri * (double)ri * (double)dinv[i / R];
   }
   if (const double* tot = mgrid_sum<2>(v, R, partials, &S->counter[2])) {
     S->iter += 1;
@@ -183,8 +186,10 @@ __global__ void __launch_bounds__(kMThreads)
       if (!S->done[k]) {
         S->it[k] += 1;
         S->rr[k] = tot[k];
-        S->beta[k] = tot[kMaxRhs + k] / S->rz[k];
-        S->rz[k] = tot[kMaxRhs + k];
+        if (jac) {
+          S->beta[k] = tot[kMaxRhs + k] / S->rz[k];
+          S->rz[k] = tot[kMaxRhs + k];
+        }
         if (!isfinite(tot[k])) {
           S->done[k] = 1;
           S->status[k] = HC_BREAKDOWN;
@@ -199,6 +204,27 @@ __global__ void __launch_bounds__(kMThreads)
       all &= S->done[k];
     }
     S->all_done = all;
+  }
+}
+
+// rz = r.z per rhs; first: beta = 0, else beta = rz_new / rz_old (columns still running)
+template <typename T>
+__global__ void __launch_bounds__(kMThreads)
+    k_m_rz(int64_t n, int R, const T* __restrict__ r, const T* __restrict__ z, int first, MScalars* S,
+           double* partials) {
+  if (S->all_done) return;
+  double v[1] = {0};
+  M_LOOP(i, n, R) v[0] += (double)r[i] * (double)z[i];
+  if (const double* tot = mgrid_sum<1>(v, R, partials, &S->counter[1])) {
+    for (int k = 0; k < R; ++k) {
+      if (first) {
+        S->rz[k] = tot[k];
+        S->beta[k] = 0.0;
+      } else if (!S->done[k]) {
+        S->beta[k] = tot[k] / S->rz[k];
+        S->rz[k] = tot[k];
+      }
+    }
   }
 }
 
@@ -307,14 +333,22 @@ static hc_status multi_prepare(hcop* h, size_t vec_bytes) {
   return HC_OK;
 }
 
-// Block PCG on J X = B (X: initial guess); wk holds r, p, q (3 n R of T).
+// Block PCG on J X = B (X: initial guess); wk holds r, p, q (and z with aux): 3 (4) n R of T.
 template <typename T>
 static hc_status mpcg_run(hcop* h, int R, double rtol, double atol, int maxit, const T* B, T* X, T* wk,
-                          const T* dinv) {
+                          const T* dinv, bool aux) {
   MultiWork* w = mwork(h);
   cudaStream_t s = h->stream;
   const int64_t n = h->ndof;
   T *r = wk, *p = wk + n * R, *q = wk + 2 * n * R;
+  T* z = aux ? wk + 3 * n * R : nullptr;
+  const int* all_done = &w->S->all_done;
+  auto precond = [&](int first) -> hc_status {
+    if (!aux) return HC_OK;
+    HC_CUDA_TRY(h, tetaux_apply<T>(h, R, r, z, dinv, all_done, s));
+    k_m_rz<T><<<mgrid(n, R), kMThreads, 0, s>>>(n, R, r, z, first, w->S, w->partials);
+    return HC_OK;
+  };
   MScalars* hs = w->hS;
   std::memset(hs, 0, sizeof(MScalars));
   hs->rtol2 = rtol * rtol;
@@ -325,7 +359,9 @@ static hc_status mpcg_run(hcop* h, int R, double rtol, double atol, int maxit, c
   HC_CUDA_TRY(h, multi_apply<T>(h, R, X, q, s));
   k_m_setup<T><<<g, kMThreads, 0, s>>>(n, R, B, q, r, dinv, w->S, w->partials);
   HC_CUDA_TRY(h, cudaMemsetAsync(p, 0, n * R * sizeof(T), s));
-  k_m_dir<T><<<g, kMThreads, 0, s>>>(n, R, r, dinv, p, q, h->ess, w->S);
+  hc_status pst = precond(1);
+  if (pst != HC_OK) return pst;
+  k_m_dir<T><<<g, kMThreads, 0, s>>>(n, R, r, z, dinv, p, q, h->ess, w->S);
   HC_CUDA_TRY(h, cudaGetLastError());
   const int chunk = 25;
   for (int launched = 0;;) {
@@ -334,8 +370,10 @@ static hc_status mpcg_run(hcop* h, int R, double rtol, double atol, int maxit, c
       HC_CUDA_TRY(h, tet_apply_launch<T>(h, sizeof(T) == 8 ? (const T*)h->tetK64 : (const T*)h->tetK32, p, q, R,
                                          true, 1.0, &w->S->all_done, s));
       k_m_alpha<T><<<g, kMThreads, 0, s>>>(n, R, p, q, w->S, w->partials);
-      k_m_update<T><<<g, kMThreads, 0, s>>>(n, R, X, r, p, q, dinv, w->S, w->partials);
-      k_m_dir<T><<<g, kMThreads, 0, s>>>(n, R, r, dinv, p, q, h->ess, w->S);
+      k_m_update<T><<<g, kMThreads, 0, s>>>(n, R, X, r, p, q, dinv, aux ? 0 : 1, w->S, w->partials);
+      pst = precond(0);
+      if (pst != HC_OK) return pst;
+      k_m_dir<T><<<g, kMThreads, 0, s>>>(n, R, r, z, dinv, p, q, h->ess, w->S);
     }
     HC_CUDA_TRY(h, cudaGetLastError());
     HC_CUDA_TRY(h, cudaMemcpyAsync(hs, w->S, sizeof(MScalars), cudaMemcpyDeviceToHost, s));
@@ -355,11 +393,18 @@ hc_status multi_solve_device(hcop* h, const hc_solve_params* prm, int R, const d
   const size_t nr = (size_t)n * R;
   MultiWork* w = nullptr;
   for (int k = 0; k < R; ++k) std::memset(&info[k], 0, sizeof(hc_solve_info));
+  const bool aux = prm->precond == HC_PRECOND_AUX;
+  const size_t nk = aux ? 4 : 3;  // Krylov vectors: r, p, q (, z)
+  if (aux) {
+    hc_status st = tetaux_setup(h);
+    if (st == HC_OK) st = tetaux_reserve(h, R);
+    if (st != HC_OK) return st;
+  }
   if (prm->precision == HC_FP64) {
-    hc_status st = multi_prepare(h, 3 * nr * sizeof(double));
+    hc_status st = multi_prepare(h, nk * nr * sizeof(double));
     if (st != HC_OK) return st;
     w = mwork(h);
-    st = mpcg_run<double>(h, R, prm->rtol, prm->atol, prm->maxit, B, X, (double*)w->vec, h->dinv);
+    st = mpcg_run<double>(h, R, prm->rtol, prm->atol, prm->maxit, B, X, (double*)w->vec, h->dinv, aux);
     if (st != HC_OK) return st;
     hc_status worst = HC_OK;
     for (int k = 0; k < R; ++k) {
@@ -371,8 +416,8 @@ hc_status multi_solve_device(hcop* h, const hc_solve_params* prm, int R, const d
     }
     return worst;
   }
-  // mixed: r64 (n R doubles) | rf, c (2 n R floats) | r, p, q (3 n R floats)
-  hc_status st = multi_prepare(h, nr * sizeof(double) + 5 * nr * sizeof(float));
+  // mixed: r64 (n R doubles) | rf, c (2 n R floats) | r, p, q (, z) (nk n R floats)
+  hc_status st = multi_prepare(h, nr * sizeof(double) + (2 + nk) * nr * sizeof(float));
   if (st != HC_OK) return st;
   w = mwork(h);
   double* r64 = (double*)w->vec;
@@ -429,7 +474,7 @@ hc_status multi_solve_device(hcop* h, const hc_solve_params* prm, int R, const d
     HC_CUDA_TRY(h, cudaMemcpyAsync(w->col, inv.data(), 2 * kMaxRhs * sizeof(double), cudaMemcpyHostToDevice, s));
     k_m_d2f<<<g, kMThreads, 0, s>>>(n, R, r64, w->col, rf, c);
     st = mpcg_run<float>(h, R, inner, 0.0, std::min(prm->maxit - used, std::max(100, prm->maxit / 4)), rf, c, wk,
-                         h->dinvf);
+                         h->dinvf, aux);
     if (st != HC_OK) return st;
     for (int k = 0; k < R; ++k) total[k] += w->hS->it[k];
     k_m_axpy<<<g, kMThreads, 0, s>>>(n, R, c, w->col + kMaxRhs, X);
@@ -439,14 +484,15 @@ hc_status multi_solve_device(hcop* h, const hc_solve_params* prm, int R, const d
   }
   if (stalled) {
     // FP64 block PCG from the refined X
-    st = multi_prepare(h, nr * sizeof(double) + 5 * nr * sizeof(float) + 3 * nr * sizeof(double));
+    const size_t off = nr * sizeof(double) + (2 + nk) * nr * sizeof(float);
+    st = multi_prepare(h, off + nk * nr * sizeof(double));
     if (st != HC_OK) return st;
     w = mwork(h);
     r64 = (double*)w->vec;
-    double* wk64 = (double*)((char*)w->vec + nr * sizeof(double) + 5 * nr * sizeof(float));
+    double* wk64 = (double*)((char*)w->vec + off);
     int used = 0;
     for (int k = 0; k < R; ++k) used = std::max(used, total[k]);
-    st = mpcg_run<double>(h, R, prm->rtol, prm->atol, std::max(1, prm->maxit - used), B, X, wk64, h->dinv);
+    st = mpcg_run<double>(h, R, prm->rtol, prm->atol, std::max(1, prm->maxit - used), B, X, wk64, h->dinv, aux);
     if (st != HC_OK) return st;
     for (int k = 0; k < R; ++k) {
       total[k] += w->hS->it[k];
@@ -482,8 +528,8 @@ extern "C" hc_status hc_solve_multi_device(hcop_t* h, const hc_solve_params* prm
     h->err = "precision must be HC_FP64 or HC_MIXED";
     return HC_EINVAL;
   }
-  if (prm->precond != HC_PRECOND_JACOBI) {
-    h->err = "multi-RHS solves take the Jacobi preconditioner";
+  if (prm->precond != HC_PRECOND_JACOBI && prm->precond != HC_PRECOND_AUX) {
+    h->err = "multi-RHS solves take the Jacobi or the auxiliary-space preconditioner";
     return HC_ENOTSUP;
   }
   if (!(prm->rtol >= 0.0) || !(prm->atol >= 0.0) || prm->maxit < 1) {

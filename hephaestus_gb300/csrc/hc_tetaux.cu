@@ -1,0 +1,959 @@
+// hc_tetaux.cu -- auxiliary-space gradient correction for Nedelec tets:
+//
+//   B = D^-1 + (PG) V (PG)^T,   V ~ ((PG)^T J (PG))^-1,
+//
+// the gradient part of the AMS preconditioner HypreAMS builds for the H(curl)
+// solve (the Hiptmair-Xu splitting; hcurl_formulation.cpp:81-85 installs
+// HypreAMS).  G is the exact discrete gradient from nodal functions (P1
+// vertex hats; for order 2 also the quadratic edge bubbles) into this Nedelec
+// space (P masks essential dofs), and V applies one V-cycle of a
+// smoothed-aggregation algebraic multigrid to the P1 nodal operator
+// A_n = (PG)^T K (PG), assembled from the element matrices.
+//
+// Discrete gradient, in the basis of hc_tet.cu (vertices sorted by global
+// index, W_ab = l_a grad l_b - l_b grad l_a):
+//   grad l_v = sum_{j != v} W_jv, so G u has W_ab-coefficient u_b - u_a;
+//   W_ab = l_a W_ab + l_b W_ab + sum_{c != a,b} l_c W_ab, and on a face i<j<k
+//   (functions F0 = l_k W_ij, F1 = l_j W_ik) l_i W_jk = F1 - F0, so
+//   order 1: edge ab: u_b - u_a;
+//   order 2: both dofs of edge ab: u_b - u_a; face ijk: F0 = -u_i + 2u_j - u_k,
+//            F1 = -u_i - u_j + 2u_k.
+// Order 2 adds the gradients of the quadratic edge bubbles l_a l_b (a < b), the
+// slow modes of Jacobi on order-2 meshes with coefficient jumps:
+//   grad(l_a l_b) = l_a W_ab - l_b W_ab + sum over faces containing ab of
+//   (F0, F1) x (1, -2) for the face's edge ij, (-2, 1) for ik, (1, 1) for jk,
+// so on the P2 nodal space (vertices + edge bubbles) V = D_L^-1 + P0 V1 P0^T
+// with V1 the AMG V-cycle on the vertex block and D_L the diagonal of the P2
+// nodal operator (P0 injects P1 into the vertex functions of the hierarchical
+// P2 basis).
+//
+// AMG (setup on the host in FP64, V-cycle on the device in FP32, all right-hand
+// sides at once in the [node][rhs] layout): strength |a_ij| > 0.08 sqrt(a_ii a_jj),
+// three-pass greedy aggregation, tentative prolongator normalised per
+// aggregate, one damped-Jacobi smoothing step (omega = 4/3 / lambda_max(D^-1 A)),
+// Galerkin coarse operators R A P with R = P^T, Chebyshev-Jacobi degree 2
+// smoothing on the interval [lambda_max / 30, lambda_max], and a dense inverse
+// of the diagonally scaled coarsest operator (<= 1500 nodes).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "hc_internal.h"
+
+namespace hc {
+
+namespace {
+constexpr int kTaMaxLevels = 10;
+constexpr int kTaCoarse = 600;
+constexpr int kTaDenseMax = 1500;
+constexpr double kTaTheta = 0.08;
+constexpr double kTaRatio = 30.0;
+constexpr int kTaThreads = 256;
+constexpr int kTaMaxBlocks = 152 * 8;
+
+__constant__ int c_ta_edges[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+__constant__ int c_ta_faces[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
+const int kHEdges[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+const int kHFaces[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
+
+// local vertices (up to 3) and coefficients of local dof I in G
+__host__ __device__ inline int ta_local(int p, int I, const int (*E)[2], const int (*F)[3], int v[3], float c[3]) {
+  if (p == 1 || I < 12) {
+    const int k = p == 1 ? I : I / 2;
+    v[0] = E[k][0];
+    v[1] = E[k][1];
+    c[0] = -1.f;
+    c[1] = 1.f;
+    return 2;
+  }
+  const int f = (I - 12) / 2, s = (I - 12) % 2;
+  v[0] = F[f][0];
+  v[1] = F[f][1];
+  v[2] = F[f][2];
+  c[0] = -1.f;
+  c[1] = s == 0 ? 2.f : -1.f;
+  c[2] = s == 0 ? -1.f : 2.f;
+  return 3;
+}
+
+// coefficient of local order-2 dof I in grad of the bubble of local edge ke
+__host__ __device__ inline float ta_bubble(int I, int ke, const int (*E)[2], const int (*F)[3]) {
+  if (I < 12) return (I / 2 == ke) ? ((I % 2 == 0) ? 1.f : -1.f) : 0.f;
+  const int f = (I - 12) / 2, s = (I - 12) % 2;
+  const int i = F[f][0], j = F[f][1], k = F[f][2], a = E[ke][0], b = E[ke][1];
+  if (a == i && b == j) return s == 0 ? 1.f : -2.f;
+  if (a == i && b == k) return s == 0 ? -2.f : 1.f;
+  if (a == j && b == k) return 1.f;
+  return 0.f;
+}
+
+struct HCsr {
+  int n = 0, m = 0;
+  std::vector<int> rp, ci;
+  std::vector<double> va;
+};
+struct DCsr {
+  const int* rp = nullptr;
+  const int* ci = nullptr;
+  const float* va = nullptr;
+};
+struct TaLevel {
+  int n = 0;
+  DCsr A, P, R;
+  float* dinv = nullptr;
+  float c0 = 0, c1 = 0, c2 = 0;  // Chebyshev: step 0 d = c0 D^-1 r, step 1 d = c1 d + c2 D^-1 r
+  float *xa = nullptr, *xb = nullptr, *b = nullptr, *r = nullptr, *d = nullptr;
+};
+
+static unsigned ta_grid(int64_t work) {
+  const int64_t b = (work + kTaThreads - 1) / kTaThreads;
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, kTaMaxBlocks));
+}
+}  // namespace
+
+struct TetAux {
+  int nlev = 0;  // levels with sparse operators; the last of them is solved densely
+  TaLevel lev[kTaMaxLevels];
+  float* cinv = nullptr;  // nc x nc inverse of S A S (coarsest)
+  float* cs = nullptr;    // S = diag^-1/2 (coarsest)
+  int nfree = 0;          // free vertices (rows of the AMG)
+  int nn = 0;             // nodal rows: free vertices, then free edge bubbles (order 2)
+  int* gnode = nullptr;   // 3 per dof: free vertex indices, -1 = none
+  int* gedge = nullptr;   // 3 per dof: free edge-bubble indices (order 2), -1 = none
+  float* dl = nullptr;    // 1 / diag of the nodal operator, nn (order 2)
+  float* rn = nullptr;    // nodal residual G^T r, nn x rcap
+  DCsr Gt;                // G^T, nn x ndof
+  int64_t nface0 = 0;     // first face dof (order 2); ndof for order 1
+  int rcap = 0;
+  std::vector<void*> owned;  // device blocks
+};
+
+// ---- device kernels ---------------------------------------------------------------
+// element nodal matrices A_e = G_e^T K_e G_e (G_e rows of essential dofs zeroed), upper triangle
+template <int L>
+__global__ void k_ta_elem(int64_t ne, int p, const double* __restrict__ K, const int32_t* __restrict__ edofs,
+                          const uint8_t* __restrict__ ess, double* __restrict__ out) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  float g[L][4];
+  for (int I = 0; I < L; ++I) {
+    int v[3];
+    float c[3];
+    const int nn = ta_local(p, I, c_ta_edges, c_ta_faces, v, c);
+    for (int k = 0; k < 4; ++k) g[I][k] = 0.f;
+    if (ess[edofs[e * L + I]]) continue;
+    for (int k = 0; k < nn; ++k) g[I][v[k]] = c[k];
+  }
+  const double* Ke = K + e * L * L;
+  double A[4][4];
+  for (int b = 0; b < 4; ++b) {
+    double t[L];
+    for (int I = 0; I < L; ++I) {
+      double s = 0.0;
+      for (int J = 0; J < L; ++J) s += Ke[I * L + J] * (double)g[J][b];
+      t[I] = s;
+    }
+    for (int a = 0; a < 4; ++a) {
+      double s = 0.0;
+      for (int I = 0; I < L; ++I) s += (double)g[I][a] * t[I];
+      A[a][b] = s;
+    }
+  }
+  const int nout = p == 1 ? 10 : 16;
+  int k = 0;
+  for (int a = 0; a < 4; ++a)
+    for (int b = a; b < 4; ++b) out[e * nout + k++] = 0.5 * (A[a][b] + A[b][a]);
+  if (p == 1) return;
+  // diagonal of the edge-bubble block: g_k^T K g_k for the 6 local edges
+  for (int ke = 0; ke < 6; ++ke) {
+    float gb[L];
+    for (int I = 0; I < L; ++I) gb[I] = ess[edofs[e * L + I]] ? 0.f : ta_bubble(I, ke, c_ta_edges, c_ta_faces);
+    double sacc = 0.0;
+    for (int I = 0; I < L; ++I) {
+      if (gb[I] == 0.f) continue;
+      double t = 0.0;
+      for (int J = 0; J < L; ++J) t += Ke[I * L + J] * (double)gb[J];
+      sacc += (double)gb[I] * t;
+    }
+    out[e * nout + 10 + ke] = sacc;
+  }
+}
+
+// y = G u on all dofs (u on mesh vertices): every element writes its dofs (equal values)
+template <int L>
+__global__ void k_ta_grad(int64_t ne, int p, const int32_t* __restrict__ sv, const int32_t* __restrict__ edofs,
+                          const double* __restrict__ u, double* __restrict__ y) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  double uv[4];
+  for (int k = 0; k < 4; ++k) uv[k] = u[sv[4 * e + k]];
+  for (int I = 0; I < L; ++I) {
+    int v[3];
+    float c[3];
+    const int nn = ta_local(p, I, c_ta_edges, c_ta_faces, v, c);
+    double s = 0.0;
+    for (int k = 0; k < nn; ++k) s += (double)c[k] * uv[v[k]];
+    y[edofs[e * L + I]] = s;
+  }
+}
+
+#define TA_LOOP(t, n, R) \
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)(n) * (R); t += (int64_t)gridDim.x * blockDim.x)
+
+template <int R>
+__device__ __forceinline__ float ta_row(const DCsr& M, int i, int c, const float* __restrict__ x) {
+  float s = 0.f;
+  const int e = M.rp[i + 1];
+  for (int k = M.rp[i]; k < e; ++k) s += M.va[k] * x[(int64_t)M.ci[k] * R + c];
+  return s;
+}
+
+// b = G^T r (nn nodal rows); fuse: x = d = c0 D^-1 b on the nv vertex rows
+// (first Chebyshev step of the AMG's finest level)
+template <typename T, int R>
+__global__ void __launch_bounds__(kTaThreads)
+    k_ta_gt(int n, int nv, DCsr Gt, const T* __restrict__ r, float* __restrict__ b, float* __restrict__ x,
+            float* __restrict__ d, const float* __restrict__ dinv, float c0, int fuse, const int* done) {
+  if (done && *done) return;
+  TA_LOOP(t, n, R) {
+    const int i = (int)(t / R), c = (int)(t % R);
+    T s = 0;
+    const int e = Gt.rp[i + 1];
+    for (int k = Gt.rp[i]; k < e; ++k) s += (T)Gt.va[k] * r[(int64_t)Gt.ci[k] * R + c];
+    const float bs = (float)s;
+    b[t] = bs;
+    if (fuse && i < nv) {
+      const float dv = c0 * dinv[i] * bs;
+      d[t] = dv;
+      x[t] = dv;
+    }
+  }
+}
+
+// Chebyshev step: r = b - A xin; d = (first ? 0 : c1 d) + c2 D^-1 r; xout = xin + d
+template <int R>
+__global__ void __launch_bounds__(kTaThreads)
+    k_ta_step(int n, DCsr A, const float* __restrict__ dinv, const float* __restrict__ b,
+              const float* __restrict__ xin, float* __restrict__ xout, float* __restrict__ d, float c1, float c2,
+              int first, const int* done) {
+  if (done && *done) return;
+  TA_LOOP(t, n, R) {
+    const int i = (int)(t / R), c = (int)(t % R);
+    const float rr = b[t] - ta_row<R>(A, i, c, xin);
+    const float dn = (first ? 0.f : c1 * d[t]) + c2 * dinv[i] * rr;
+    d[t] = dn;
+    xout[t] = xin[t] + dn;
+  }
+}
+
+template <int R>
+__global__ void __launch_bounds__(kTaThreads)
+    k_ta_resid(int n, DCsr A, const float* __restrict__ b, const float* __restrict__ x, float* __restrict__ r,
+               const int* done) {
+  if (done && *done) return;
+  TA_LOOP(t, n, R) {
+    const int i = (int)(t / R), c = (int)(t % R);
+    r[t] = b[t] - ta_row<R>(A, i, c, x);
+  }
+}
+
+// bc = R r; fuse: xc = dc = c0 D^-1 bc
+template <int R>
+__global__ void __launch_bounds__(kTaThreads)
+    k_ta_restrict(int nc, DCsr Rm, const float* __restrict__ r, float* __restrict__ bc, float* __restrict__ xc,
+                  float* __restrict__ dc, const float* __restrict__ dinv, float c0, int fuse, const int* done) {
+  if (done && *done) return;
+  TA_LOOP(t, nc, R) {
+    const int i = (int)(t / R), c = (int)(t % R);
+    const float s = ta_row<R>(Rm, i, c, r);
+    bc[t] = s;
+    if (fuse) {
+      const float dv = c0 * dinv[i] * s;
+      dc[t] = dv;
+      xc[t] = dv;
+    }
+  }
+}
+
+template <int R>
+__global__ void __launch_bounds__(kTaThreads)
+    k_ta_prolong(int n, DCsr P, const float* __restrict__ xc, float* __restrict__ x, const int* done) {
+  if (done && *done) return;
+  TA_LOOP(t, n, R) {
+    const int i = (int)(t / R), c = (int)(t % R);
+    x[t] += ta_row<R>(P, i, c, xc);
+  }
+}
+
+// x = S Cinv S b (coarsest level)
+template <int R>
+__global__ void __launch_bounds__(kTaThreads)
+    k_ta_dense(int nc, const float* __restrict__ cinv, const float* __restrict__ cs, const float* __restrict__ b,
+               float* __restrict__ x, const int* done) {
+  if (done && *done) return;
+  TA_LOOP(t, nc, R) {
+    const int i = (int)(t / R), c = (int)(t % R);
+    const float* row = cinv + (int64_t)i * nc;
+    float s = 0.f;
+    for (int j = 0; j < nc; ++j) s += row[j] * cs[j] * b[(int64_t)j * R + c];
+    x[t] = cs[i] * s;
+  }
+}
+
+// z = D^-1 r + (PG) x with the nodal correction x = V rn: vertex rows
+// x = x0 + D_L^-1 rn (x0 the V-cycle result), edge-bubble rows x = D_L^-1 rn
+// (order 2; gedge == nullptr for order 1: x = x0)
+template <typename T, int R>
+__global__ void __launch_bounds__(kTaThreads)
+    k_ta_g(int64_t ndof, const int* __restrict__ gnode, const int* __restrict__ gedge, int64_t nface0, int nv,
+           const float* __restrict__ x0, const float* __restrict__ rn, const float* __restrict__ dl,
+           const T* __restrict__ r, const T* __restrict__ dinv, T* __restrict__ z, const int* done) {
+  if (done && *done) return;
+  TA_LOOP(t, ndof, R) {
+    const int64_t dof = t / R;
+    const int c = (int)(t % R);
+    const bool face = dof >= nface0;
+    const bool s1 = face && ((dof - nface0) & 1);
+    float v = 0.f;
+    {
+      const int n0 = gnode[3 * dof], n1 = gnode[3 * dof + 1], n2 = gnode[3 * dof + 2];
+      const float c0 = -1.f, c1 = face ? (s1 ? -1.f : 2.f) : 1.f, c2 = face ? (s1 ? 2.f : -1.f) : 0.f;
+      auto xv = [&](int nd) {
+        const int64_t q = (int64_t)nd * R + c;
+        return dl ? x0[q] + dl[nd] * rn[q] : x0[q];
+      };
+      if (n0 >= 0) v += c0 * xv(n0);
+      if (n1 >= 0) v += c1 * xv(n1);
+      if (n2 >= 0) v += c2 * xv(n2);
+    }
+    if (gedge) {
+      const int e0 = gedge[3 * dof], e1 = gedge[3 * dof + 1], e2 = gedge[3 * dof + 2];
+      // edge dofs: (+1 | -1) on their own bubble; face dofs F0: (1, -2, 1), F1: (-2, 1, 1) on edges ij, ik, jk
+      const float b0 = face ? (s1 ? -2.f : 1.f) : (((dof & 1) == 0) ? 1.f : -1.f);
+      const float b1 = s1 ? 1.f : -2.f, b2 = 1.f;
+      auto xe = [&](int ge) {
+        const int nd = nv + ge;
+        return dl[nd] * rn[(int64_t)nd * R + c];
+      };
+      if (e0 >= 0) v += b0 * xe(e0);
+      if (e1 >= 0) v += b1 * xe(e1);
+      if (e2 >= 0) v += b2 * xe(e2);
+    }
+    z[t] = dinv[dof] * r[t] + (T)v;
+  }
+}
+
+// ---- host AMG setup -----------------------------------------------------------------
+namespace {
+
+int aggregate(const HCsr& A, const std::vector<double>& dg, std::vector<int>& agg) {
+  const int n = A.n;
+  auto strong = [&](int i, int k) {
+    const int j = A.ci[k];
+    return j != i && std::fabs(A.va[k]) > kTaTheta * std::sqrt(std::fabs(dg[i] * dg[j]));
+  };
+  agg.assign(n, -1);
+  int na = 0;
+  for (int i = 0; i < n; ++i) {
+    if (agg[i] != -1) continue;
+    bool ok = true;
+    for (int k = A.rp[i]; k < A.rp[i + 1] && ok; ++k)
+      if (strong(i, k) && agg[A.ci[k]] != -1) ok = false;
+    if (!ok) continue;
+    agg[i] = na;
+    for (int k = A.rp[i]; k < A.rp[i + 1]; ++k)
+      if (strong(i, k)) agg[A.ci[k]] = na;
+    ++na;
+  }
+  const std::vector<int> a1 = agg;
+  for (int i = 0; i < n; ++i) {
+    if (a1[i] != -1) continue;
+    int best = -1;
+    double bs = 0.0;
+    for (int k = A.rp[i]; k < A.rp[i + 1]; ++k)
+      if (strong(i, k) && a1[A.ci[k]] >= 0 && std::fabs(A.va[k]) > bs) {
+        bs = std::fabs(A.va[k]);
+        best = a1[A.ci[k]];
+      }
+    if (best >= 0) agg[i] = best;
+  }
+  for (int i = 0; i < n; ++i) {
+    if (agg[i] != -1) continue;
+    agg[i] = na;
+    for (int k = A.rp[i]; k < A.rp[i + 1]; ++k)
+      if (strong(i, k) && agg[A.ci[k]] == -1) agg[A.ci[k]] = na;
+    ++na;
+  }
+  return na;
+}
+
+std::vector<double> diagonal(const HCsr& A) {
+  std::vector<double> d(A.n, 0.0);
+  for (int i = 0; i < A.n; ++i)
+    for (int k = A.rp[i]; k < A.rp[i + 1]; ++k)
+      if (A.ci[k] == i) d[i] = A.va[k];
+  return d;
+}
+
+// largest eigenvalue of D^-1 A (power iteration on D^-1/2 A D^-1/2)
+double lmax_scaled(const HCsr& A, const std::vector<double>& dg) {
+  const int n = A.n;
+  std::vector<double> s(n), x(n), y(n);
+  for (int i = 0; i < n; ++i) {
+    s[i] = 1.0 / std::sqrt(std::fabs(dg[i]));
+    x[i] = 1.0 + 0.37 * std::sin(1.0 + 7.3 * i);  // deterministic start
+  }
+  double lam = 1.0;
+  for (int it = 0; it < 40; ++it) {
+    double nx = 0.0;
+    for (double v : x) nx += v * v;
+    nx = std::sqrt(nx);
+    for (double& v : x) v /= nx;
+    double xy = 0.0;
+    for (int i = 0; i < n; ++i) {
+      double t = 0.0;
+      for (int k = A.rp[i]; k < A.rp[i + 1]; ++k) t += A.va[k] * s[A.ci[k]] * x[A.ci[k]];
+      y[i] = s[i] * t;
+      xy += x[i] * y[i];
+    }
+    lam = xy;
+    x.swap(y);
+  }
+  return lam;
+}
+
+HCsr smooth_prolongator(const HCsr& A, const std::vector<double>& dg, const std::vector<int>& agg, int na,
+                        double omega) {
+  std::vector<int> cnt(na, 0);
+  for (int a : agg) ++cnt[a];
+  std::vector<double> pt(A.n);
+  for (int i = 0; i < A.n; ++i) pt[i] = 1.0 / std::sqrt((double)cnt[agg[i]]);
+  HCsr P;
+  P.n = A.n;
+  P.m = na;
+  P.rp.assign(1, 0);
+  std::vector<std::pair<int, double>> acc;
+  for (int i = 0; i < A.n; ++i) {
+    acc.clear();
+    auto add = [&](int col, double v) {
+      for (auto& q : acc)
+        if (q.first == col) {
+          q.second += v;
+          return;
+        }
+      acc.push_back({col, v});
+    };
+    add(agg[i], pt[i]);
+    for (int k = A.rp[i]; k < A.rp[i + 1]; ++k) add(agg[A.ci[k]], -omega / dg[i] * A.va[k] * pt[A.ci[k]]);
+    std::sort(acc.begin(), acc.end());
+    for (auto& q : acc) {
+      P.ci.push_back(q.first);
+      P.va.push_back(q.second);
+    }
+    P.rp.push_back((int)P.ci.size());
+  }
+  return P;
+}
+
+HCsr transpose(const HCsr& P) {
+  HCsr T;
+  T.n = P.m;
+  T.m = P.n;
+  T.rp.assign(P.m + 1, 0);
+  for (int c : P.ci) ++T.rp[c + 1];
+  for (int i = 0; i < P.m; ++i) T.rp[i + 1] += T.rp[i];
+  T.ci.resize(P.ci.size());
+  T.va.resize(P.va.size());
+  std::vector<int> pos(T.rp.begin(), T.rp.end() - 1);
+  for (int i = 0; i < P.n; ++i)
+    for (int k = P.rp[i]; k < P.rp[i + 1]; ++k) {
+      const int q = pos[P.ci[k]]++;
+      T.ci[q] = i;
+      T.va[q] = P.va[k];
+    }
+  return T;
+}
+
+HCsr spgemm(const HCsr& A, const HCsr& B) {
+  HCsr C;
+  C.n = A.n;
+  C.m = B.m;
+  C.rp.assign(1, 0);
+  std::vector<int> marker(B.m, -1);
+  std::vector<std::pair<int, double>> row;
+  for (int i = 0; i < A.n; ++i) {
+    row.clear();
+    for (int ka = A.rp[i]; ka < A.rp[i + 1]; ++ka) {
+      const int j = A.ci[ka];
+      const double av = A.va[ka];
+      for (int kb = B.rp[j]; kb < B.rp[j + 1]; ++kb) {
+        const int c = B.ci[kb];
+        if (marker[c] < 0) {
+          marker[c] = (int)row.size();
+          row.push_back({c, av * B.va[kb]});
+        } else {
+          row[marker[c]].second += av * B.va[kb];
+        }
+      }
+    }
+    for (auto& q : row) marker[q.first] = -1;
+    std::sort(row.begin(), row.end());
+    for (auto& q : row) {
+      C.ci.push_back(q.first);
+      C.va.push_back(q.second);
+    }
+    C.rp.push_back((int)C.ci.size());
+  }
+  return C;
+}
+
+// inverse of the SPD matrix S A S (S = diag^-1/2) by Cholesky; returns false if not positive definite
+bool dense_scaled_inverse(const HCsr& A, const std::vector<double>& dg, std::vector<float>& inv,
+                          std::vector<float>& sc) {
+  const int n = A.n;
+  std::vector<double> M((size_t)n * n, 0.0), s(n);
+  for (int i = 0; i < n; ++i) s[i] = 1.0 / std::sqrt(std::fabs(dg[i]));
+  for (int i = 0; i < n; ++i)
+    for (int k = A.rp[i]; k < A.rp[i + 1]; ++k) M[(size_t)i * n + A.ci[k]] = s[i] * A.va[k] * s[A.ci[k]];
+  // Cholesky, lower triangle in place
+  for (int j = 0; j < n; ++j) {
+    double d = M[(size_t)j * n + j];
+    for (int k = 0; k < j; ++k) d -= M[(size_t)j * n + k] * M[(size_t)j * n + k];
+    if (!(d > 1e-12)) return false;
+    d = std::sqrt(d);
+    M[(size_t)j * n + j] = d;
+    for (int i = j + 1; i < n; ++i) {
+      double v = M[(size_t)i * n + j];
+      for (int k = 0; k < j; ++k) v -= M[(size_t)i * n + k] * M[(size_t)j * n + k];
+      M[(size_t)i * n + j] = v / d;
+    }
+  }
+  // Linv (lower), then inv = Linv^T Linv
+  std::vector<double> Li((size_t)n * n, 0.0);
+  for (int j = 0; j < n; ++j) {
+    Li[(size_t)j * n + j] = 1.0 / M[(size_t)j * n + j];
+    for (int i = j + 1; i < n; ++i) {
+      double v = 0.0;
+      for (int k = j; k < i; ++k) v -= M[(size_t)i * n + k] * Li[(size_t)k * n + j];
+      Li[(size_t)i * n + j] = v / M[(size_t)i * n + i];
+    }
+  }
+  inv.assign((size_t)n * n, 0.f);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j <= i; ++j) {
+      double v = 0.0;
+      for (int k = i; k < n; ++k) v += Li[(size_t)k * n + i] * Li[(size_t)k * n + j];
+      inv[(size_t)i * n + j] = inv[(size_t)j * n + i] = (float)v;
+    }
+  sc.resize(n);
+  for (int i = 0; i < n; ++i) sc[i] = (float)s[i];
+  return true;
+}
+
+}  // namespace
+
+template <typename V>
+static cudaError_t upload(hcop* h, TetAux* X, const std::vector<V>& v, const V** out) {
+  void* p = nullptr;
+  const size_t bytes = std::max<size_t>(1, v.size()) * sizeof(V);
+  cudaError_t e = dmalloc(h, &p, bytes);
+  if (e != cudaSuccess) return e;
+  X->owned.push_back(p);
+  if (!v.empty()) e = cudaMemcpyAsync(p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice, h->stream);
+  *out = static_cast<const V*>(p);
+  return e;
+}
+
+static cudaError_t upload_csr(hcop* h, TetAux* X, const HCsr& M, DCsr& D) {
+  std::vector<float> vf(M.va.begin(), M.va.end());
+  cudaError_t e = upload(h, X, M.rp, &D.rp);
+  if (e == cudaSuccess) e = upload(h, X, M.ci, &D.ci);
+  if (e == cudaSuccess) e = upload(h, X, vf, &D.va);
+  return e;
+}
+
+void tetaux_free(hcop* h) {
+  TetAux* X = static_cast<TetAux*>(h->taux);
+  if (!X) return;
+  for (void* p : X->owned) dfree(h, p);
+  delete X;
+  h->taux = nullptr;
+}
+
+hc_status tetaux_setup(hcop* h) {
+  if (h->taux) return HC_OK;
+  if (h->type != HC_TET) {
+    h->err = "tetaux_setup: tet meshes only";
+    return HC_ENOTSUP;
+  }
+  const int p = h->p, L = p == 1 ? 6 : 20;
+  const int64_t ne = h->ne, N = h->ndof;
+  cudaStream_t s = h->stream;
+  std::vector<int32_t> sv(ne * 4), ed(ne * L);
+  const int nout = p == 1 ? 10 : 16;  // vertex block (upper triangle) + edge-bubble diagonal
+  std::vector<double> Ae(ne * nout);
+  double* dAe = nullptr;
+  HC_CUDA_TRY(h, dmalloc(h, (void**)&dAe, Ae.size() * sizeof(double)));
+  if (L == 6)
+    k_ta_elem<6><<<(unsigned)((ne + 127) / 128), 128, 0, s>>>(ne, p, h->tetK64, h->tet_edofs, h->ess, dAe);
+  else
+    k_ta_elem<20><<<(unsigned)((ne + 127) / 128), 128, 0, s>>>(ne, p, h->tetK64, h->tet_edofs, h->ess, dAe);
+  HC_CUDA_TRY(h, cudaGetLastError());
+  HC_CUDA_TRY(h, cudaMemcpyAsync(Ae.data(), dAe, Ae.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  HC_CUDA_TRY(h, cudaMemcpyAsync(sv.data(), h->tet_sv, sv.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  HC_CUDA_TRY(h, cudaMemcpyAsync(ed.data(), h->tet_edofs, ed.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  HC_CUDA_TRY(h, cudaStreamSynchronize(s));
+  dfree(h, dAe);
+  const std::vector<uint8_t>& ess = h->ess_host;
+
+  // nodes: fixed where a vertex carries an essential dof of an element
+  int nv = 0;
+  for (int32_t v : sv) nv = std::max(nv, v + 1);
+  std::vector<uint8_t> used(nv, 0), fixed(nv, 0);
+  for (int64_t e = 0; e < ne; ++e) {
+    for (int k = 0; k < 4; ++k) used[sv[4 * e + k]] = 1;
+    for (int I = 0; I < L; ++I) {
+      if (!ess[ed[e * L + I]]) continue;
+      int v[3];
+      float c[3];
+      const int nn = ta_local(p, I, kHEdges, kHFaces, v, c);
+      for (int k = 0; k < nn; ++k) fixed[sv[4 * e + v[k]]] = 1;
+    }
+  }
+  bool any_fixed = false;
+  for (int v = 0; v < nv; ++v) any_fixed |= used[v] && fixed[v];
+  if (!any_fixed)  // no essential boundary: pin one vertex (G has the constants in its kernel)
+    for (int v = 0; v < nv; ++v)
+      if (used[v]) {
+        fixed[v] = 1;
+        break;
+      }
+  std::vector<int> fmap(nv, -1);
+  int nfree = 0;
+  for (int v = 0; v < nv; ++v)
+    if (used[v] && !fixed[v]) fmap[v] = nfree++;
+  if (nfree == 0) {
+    h->err = "auxiliary-space preconditioner: no free vertex";
+    return HC_ENOTSUP;
+  }
+
+  // G structure: free nodes of every non-essential dof
+  std::vector<int> gnode(3 * N, -1);
+  for (int64_t e = 0; e < ne; ++e)
+    for (int I = 0; I < L; ++I) {
+      const int64_t d = ed[e * L + I];
+      if (ess[d]) continue;
+      int v[3];
+      float c[3];
+      const int nn = ta_local(p, I, kHEdges, kHFaces, v, c);
+      for (int k = 0; k < nn; ++k) gnode[3 * d + k] = fmap[sv[4 * e + v[k]]];
+    }
+  const int64_t nface0 = p == 1 ? N : 2 * h->n_edges;
+  // order 2: free edge bubbles (an edge with essential dofs is fixed) and their dofs
+  std::vector<int> gedge;
+  std::vector<int> emap;
+  int nfe = 0;
+  if (p == 2) {
+    const int64_t nE = h->n_edges;
+    emap.assign(nE, -1);
+    for (int64_t g = 0; g < nE; ++g)
+      if (!ess[2 * g] && !ess[2 * g + 1]) emap[g] = nfe++;
+    gedge.assign(3 * N, -1);
+    const int le[4][3] = {{0, 1, 3}, {0, 2, 4}, {1, 2, 5}, {3, 4, 5}};  // local edges ij, ik, jk of each face
+    for (int64_t e = 0; e < ne; ++e)
+      for (int I = 0; I < L; ++I) {
+        const int64_t d = ed[e * L + I];
+        if (ess[d]) continue;
+        if (I < 12) {
+          gedge[3 * d] = emap[d / 2];
+        } else {
+          const int f = (I - 12) / 2;
+          for (int k = 0; k < 3; ++k) gedge[3 * d + k] = emap[ed[e * L + 2 * le[f][k]] / 2];
+        }
+      }
+  }
+  const int nn = nfree + nfe;
+  auto slot_coef = [&](int64_t d, int k, bool bubble) -> float {
+    const bool face = d >= nface0, s1 = face && ((d - nface0) & 1);
+    if (!bubble) {
+      const float c[3] = {-1.f, face ? (s1 ? -1.f : 2.f) : 1.f, face ? (s1 ? 2.f : -1.f) : 0.f};
+      return c[k];
+    }
+    if (!face) return k == 0 ? ((d & 1) == 0 ? 1.f : -1.f) : 0.f;
+    const float c[3] = {s1 ? -2.f : 1.f, s1 ? 1.f : -2.f, 1.f};
+    return c[k];
+  };
+  HCsr Gt;
+  Gt.n = nn;
+  Gt.rp.assign(nn + 1, 0);
+  for (int64_t d = 0; d < N; ++d)
+    for (int k = 0; k < 3; ++k) {
+      if (gnode[3 * d + k] >= 0) ++Gt.rp[gnode[3 * d + k] + 1];
+      if (nfe && gedge[3 * d + k] >= 0) ++Gt.rp[nfree + gedge[3 * d + k] + 1];
+    }
+  for (int i = 0; i < nn; ++i) Gt.rp[i + 1] += Gt.rp[i];
+  Gt.ci.resize(Gt.rp[nn]);
+  Gt.va.resize(Gt.rp[nn]);
+  {
+    std::vector<int> pos(Gt.rp.begin(), Gt.rp.end() - 1);
+    for (int64_t d = 0; d < N; ++d)
+      for (int k = 0; k < 3; ++k) {
+        const int nd = gnode[3 * d + k];
+        if (nd >= 0) {
+          const int q = pos[nd]++;
+          Gt.ci[q] = (int)d;
+          Gt.va[q] = slot_coef(d, k, false);
+        }
+        if (nfe && gedge[3 * d + k] >= 0) {
+          const int q = pos[nfree + gedge[3 * d + k]]++;
+          Gt.ci[q] = (int)d;
+          Gt.va[q] = slot_coef(d, k, true);
+        }
+      }
+  }
+
+  // nodal operator on free nodes: pattern = vertex graph of the elements
+  HCsr A;
+  A.n = A.m = nfree;
+  {
+    std::vector<uint64_t> keys;
+    keys.reserve(ne * 6);
+    for (int64_t e = 0; e < ne; ++e)
+      for (auto& q : kHEdges) {
+        const int a = fmap[sv[4 * e + q[0]]], b = fmap[sv[4 * e + q[1]]];
+        if (a >= 0 && b >= 0) keys.push_back((uint64_t)std::min(a, b) * (uint64_t)nfree + (uint64_t)std::max(a, b));
+      }
+    std::sort(keys.begin(), keys.end());
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    A.rp.assign(nfree + 1, 0);
+    for (int i = 0; i < nfree; ++i) A.rp[i + 1] = 1;
+    for (uint64_t k : keys) {
+      ++A.rp[k / nfree + 1];
+      ++A.rp[k % nfree + 1];
+    }
+    for (int i = 0; i < nfree; ++i) A.rp[i + 1] += A.rp[i];
+    A.ci.resize(A.rp[nfree]);
+    A.va.assign(A.rp[nfree], 0.0);
+    std::vector<int> pos(A.rp.begin(), A.rp.end() - 1);
+    for (int i = 0; i < nfree; ++i) A.ci[pos[i]++] = i;
+    for (uint64_t k : keys) {
+      const int a = (int)(k / nfree), b = (int)(k % nfree);
+      A.ci[pos[a]++] = b;
+      A.ci[pos[b]++] = a;
+    }
+    for (int i = 0; i < nfree; ++i) std::sort(A.ci.begin() + A.rp[i], A.ci.begin() + A.rp[i + 1]);
+    const int tri[4][4] = {{0, 1, 2, 3}, {1, 4, 5, 6}, {2, 5, 7, 8}, {3, 6, 8, 9}};
+    for (int64_t e = 0; e < ne; ++e)
+      for (int a = 0; a < 4; ++a) {
+        const int i = fmap[sv[4 * e + a]];
+        if (i < 0) continue;
+        for (int b = 0; b < 4; ++b) {
+          const int j = fmap[sv[4 * e + b]];
+          if (j < 0) continue;
+          const int* lo = &A.ci[A.rp[i]];
+          const int* hi = &A.ci[A.rp[i + 1]];
+          A.va[std::lower_bound(lo, hi, j) - &A.ci[0]] += Ae[e * nout + tri[a][b]];
+        }
+      }
+  }
+
+  // order 2: D_L^-1 on the nodal rows (vertex block diagonal, edge-bubble diagonal)
+  std::vector<float> dl;
+  if (p == 2) {
+    dl.assign(nn, 0.f);
+    std::vector<double> bd(nfe, 0.0);
+    for (int64_t e = 0; e < ne; ++e)
+      for (int ke = 0; ke < 6; ++ke) {
+        const int fe = emap[ed[e * L + 2 * ke] / 2];
+        if (fe >= 0) bd[fe] += Ae[e * nout + 10 + ke];
+      }
+    for (int i = 0; i < nfree; ++i)
+      for (int k = A.rp[i]; k < A.rp[i + 1]; ++k)
+        if (A.ci[k] == i) dl[i] = A.va[k] > 0 ? (float)(1.0 / A.va[k]) : 0.f;
+    for (int i = 0; i < nfe; ++i) dl[nfree + i] = bd[i] > 0 ? (float)(1.0 / bd[i]) : 0.f;
+  }
+
+  TetAux* X = new TetAux();
+  h->taux = X;
+  X->nfree = nfree;
+  X->nn = nn;
+  X->nface0 = nface0;
+  cudaError_t e = cudaSuccess;
+  {
+    const int* gp = nullptr;
+    e = upload(h, X, gnode, &gp);
+    X->gnode = const_cast<int*>(gp);
+    if (e == cudaSuccess && p == 2) {
+      e = upload(h, X, gedge, &gp);
+      X->gedge = const_cast<int*>(gp);
+      const float* dp = nullptr;
+      if (e == cudaSuccess) e = upload(h, X, dl, &dp);
+      X->dl = const_cast<float*>(dp);
+    }
+  }
+  if (e == cudaSuccess) e = upload_csr(h, X, Gt, X->Gt);
+  // hierarchy
+  HCsr cur = std::move(A);
+  int nl = 0;
+  std::vector<float> cinv, csc;
+  for (;;) {
+    TaLevel& Lv = X->lev[nl];
+    Lv.n = cur.n;
+    const std::vector<double> dg = diagonal(cur);
+    for (int i = 0; i < cur.n; ++i)
+      if (!(dg[i] > 0.0)) {
+        h->err = "auxiliary-space preconditioner: nodal operator has a non-positive diagonal";
+        tetaux_free(h);
+        return HC_ENOTSUP;
+      }
+    const double lmax = 1.1 * lmax_scaled(cur, dg);
+    const double lmin = lmax / kTaRatio;
+    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
+    const double s1 = theta / delta, rho0 = 1.0 / s1, rho1 = 1.0 / (2.0 * s1 - rho0);
+    Lv.c0 = (float)(1.0 / theta);
+    Lv.c1 = (float)(rho1 * rho0);
+    Lv.c2 = (float)(2.0 * rho1 / delta);
+    std::vector<float> di(cur.n);
+    for (int i = 0; i < cur.n; ++i) di[i] = (float)(1.0 / dg[i]);
+    const float* dd = nullptr;
+    if (e == cudaSuccess) e = upload(h, X, di, &dd);
+    Lv.dinv = const_cast<float*>(dd);
+    if (e == cudaSuccess) e = upload_csr(h, X, cur, Lv.A);
+    ++nl;
+    const bool last_allowed = cur.n <= kTaDenseMax;
+    if (cur.n <= kTaCoarse || nl == kTaMaxLevels) {
+      if (!last_allowed || !dense_scaled_inverse(cur, dg, cinv, csc)) cinv.clear();
+      break;
+    }
+    std::vector<int> agg;
+    const int na = aggregate(cur, dg, agg);
+    if (na >= (int)(0.85 * cur.n) && last_allowed) {  // coarsening stalled
+      if (!dense_scaled_inverse(cur, dg, cinv, csc)) cinv.clear();
+      break;
+    }
+    const double lraw = lmax / 1.1;
+    HCsr P = smooth_prolongator(cur, dg, agg, na, 4.0 / (3.0 * lraw));
+    HCsr R = transpose(P);
+    HCsr Ac = spgemm(R, spgemm(cur, P));
+    if (e == cudaSuccess) e = upload_csr(h, X, P, Lv.P);
+    if (e == cudaSuccess) e = upload_csr(h, X, R, Lv.R);
+    cur = std::move(Ac);
+  }
+  X->nlev = nl;
+  if (!cinv.empty()) {
+    const float* ci = nullptr;
+    const float* cs = nullptr;
+    if (e == cudaSuccess) e = upload(h, X, cinv, &ci);
+    if (e == cudaSuccess) e = upload(h, X, csc, &cs);
+    X->cinv = const_cast<float*>(ci);
+    X->cs = const_cast<float*>(cs);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    h->err = std::string("auxiliary-space preconditioner setup: ") + cudaGetErrorString(e);
+    tetaux_free(h);
+    return HC_ECUDA;
+  }
+  return HC_OK;
+}
+
+hc_status tetaux_reserve(hcop* h, int R) {
+  TetAux* X = static_cast<TetAux*>(h->taux);
+  if (!X) return HC_EINVAL;
+  if (X->rcap >= R) return HC_OK;
+  // older (smaller) blocks stay owned until the handle goes
+  auto grab = [&](float** q, size_t rows) -> bool {
+    void* pnew = nullptr;
+    if (dmalloc(h, &pnew, rows * R * sizeof(float)) != cudaSuccess) return false;
+    X->owned.push_back(pnew);
+    *q = static_cast<float*>(pnew);
+    return true;
+  };
+  bool ok = grab(&X->rn, X->nn);
+  for (int l = 0; l < X->nlev && ok; ++l) {
+    TaLevel& Lv = X->lev[l];
+    ok = grab(&Lv.xa, Lv.n) && grab(&Lv.xb, Lv.n) && grab(&Lv.r, Lv.n) && grab(&Lv.d, Lv.n);
+    if (ok && l > 0) ok = grab(&Lv.b, Lv.n);
+  }
+  if (!ok) {
+    h->err = "auxiliary-space work vectors allocation failed";
+    return HC_ENOMEM;
+  }
+  X->lev[0].b = X->rn;
+  X->rcap = R;
+  return HC_OK;
+}
+
+template <int R>
+static float* ta_vcycle(const TetAux* X, int l, const int* done, cudaStream_t s) {
+  const TaLevel& Lv = X->lev[l];
+  const unsigned g = ta_grid((int64_t)Lv.n * R);
+  if (l == X->nlev - 1) {
+    if (X->cinv) {
+      k_ta_dense<R><<<g, kTaThreads, 0, s>>>(Lv.n, X->cinv, X->cs, Lv.b, Lv.xb, done);
+      return Lv.xb;
+    }
+    // no dense inverse: Chebyshev steps only (x = d = c0 D^-1 b was set by the producer)
+    k_ta_step<R><<<g, kTaThreads, 0, s>>>(Lv.n, Lv.A, Lv.dinv, Lv.b, Lv.xa, Lv.xb, Lv.d, Lv.c1, Lv.c2, 0, done);
+    return Lv.xb;
+  }
+  const TaLevel& Nx = X->lev[l + 1];
+  const bool next_dense = (l + 1 == X->nlev - 1) && X->cinv;
+  k_ta_step<R><<<g, kTaThreads, 0, s>>>(Lv.n, Lv.A, Lv.dinv, Lv.b, Lv.xa, Lv.xb, Lv.d, Lv.c1, Lv.c2, 0, done);
+  k_ta_resid<R><<<g, kTaThreads, 0, s>>>(Lv.n, Lv.A, Lv.b, Lv.xb, Lv.r, done);
+  k_ta_restrict<R><<<ta_grid((int64_t)Nx.n * R), kTaThreads, 0, s>>>(Nx.n, Lv.R, Lv.r, Nx.b, Nx.xa, Nx.d, Nx.dinv,
+                                                                      Nx.c0, next_dense ? 0 : 1, done);
+  const float* xc = ta_vcycle<R>(X, l + 1, done, s);
+  k_ta_prolong<R><<<g, kTaThreads, 0, s>>>(Lv.n, Lv.P, xc, Lv.xb, done);
+  k_ta_step<R><<<g, kTaThreads, 0, s>>>(Lv.n, Lv.A, Lv.dinv, Lv.b, Lv.xb, Lv.xa, Lv.d, 0.f, Lv.c0, 1, done);
+  k_ta_step<R><<<g, kTaThreads, 0, s>>>(Lv.n, Lv.A, Lv.dinv, Lv.b, Lv.xa, Lv.xb, Lv.d, Lv.c1, Lv.c2, 0, done);
+  return Lv.xb;
+}
+
+template <typename T, int R>
+static cudaError_t ta_apply_r(const hcop* h, const T* r, T* z, const T* dinv, const int* done, cudaStream_t s) {
+  const TetAux* X = static_cast<const TetAux*>(h->taux);
+  const TaLevel& L0 = X->lev[0];
+  const bool dense0 = X->nlev == 1 && X->cinv;
+  // level 0's right-hand side is the vertex block of rn (L0.b == X->rn)
+  k_ta_gt<T, R><<<ta_grid((int64_t)X->nn * R), kTaThreads, 0, s>>>(X->nn, X->nfree, X->Gt, r, X->rn, L0.xa, L0.d,
+                                                                    L0.dinv, L0.c0, dense0 ? 0 : 1, done);
+  const float* x0 = ta_vcycle<R>(X, 0, done, s);
+  k_ta_g<T, R><<<ta_grid(h->ndof * R), kTaThreads, 0, s>>>(h->ndof, X->gnode, X->gedge, X->nface0, X->nfree, x0,
+                                                            X->rn, X->dl, r, dinv, z, done);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t tetaux_apply(const hcop* h, int R, const T* r, T* z, const T* dinv, const int* done, cudaStream_t s) {
+  const TetAux* X = static_cast<const TetAux*>(h->taux);
+  if (!X || X->rcap < R) return cudaErrorInvalidValue;
+  switch (R) {
+    case 1: return ta_apply_r<T, 1>(h, r, z, dinv, done, s);
+    case 2: return ta_apply_r<T, 2>(h, r, z, dinv, done, s);
+    case 4: return ta_apply_r<T, 4>(h, r, z, dinv, done, s);
+    case 8: return ta_apply_r<T, 8>(h, r, z, dinv, done, s);
+    case 16: return ta_apply_r<T, 16>(h, r, z, dinv, done, s);
+    case 32: return ta_apply_r<T, 32>(h, r, z, dinv, done, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+template cudaError_t tetaux_apply<double>(const hcop*, int, const double*, double*, const double*, const int*,
+                                          cudaStream_t);
+template cudaError_t tetaux_apply<float>(const hcop*, int, const float*, float*, const float*, const int*,
+                                         cudaStream_t);
+
+cudaError_t tet_gradient(const hcop* h, const double* u, double* y, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(y, 0, h->ndof * sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  const unsigned b = (unsigned)((h->ne + 127) / 128);
+  if (h->p == 1)
+    k_ta_grad<6><<<b, 128, 0, s>>>(h->ne, 1, h->tet_sv, h->tet_edofs, u, y);
+  else
+    k_ta_grad<20><<<b, 128, 0, s>>>(h->ne, 2, h->tet_sv, h->tet_edofs, u, y);
+  return cudaGetLastError();
+}
+
+}  // namespace hc

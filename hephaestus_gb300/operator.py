@@ -293,6 +293,12 @@ class HCurlOperator:
         N.check(N.lib().hc_mult_multi_device(self.h, prec, nrhs, _dev_ptr(X, name), _dev_ptr(Y, name)), self.h)
         return Y
 
+    def GradientDevice(self, u, y):
+        """y = G u: discrete gradient of P1 vertex values u (float64 CUDA tensor
+        of n_vert entries) into this Nedelec space (tet meshes)."""
+        N.check(N.lib().hc_tet_gradient_device(self.h, _dev_ptr(u, "float64"), _dev_ptr(y, "float64")), self.h)
+        return y
+
     def ApplyFormDevice(self, x, y):
         N.check(N.lib().hc_apply_form_device(self.h, _dev_ptr(x, "float64"), _dev_ptr(y, "float64")), self.h)
         return y

@@ -205,6 +205,11 @@ int32_t hc_elem_type(const hcop_t* h);
 /* Tet meshes: the FP64 element matrix (L x L, L = 6 or 20) of element e,
  * rows/columns in the local dof order of the basis.                        */
 hc_status hc_tet_element_matrix(hcop_t* h, int64_t e, double* out);
+/* y = G u: the discrete gradient from P1 vertex values u (n_vert device
+ * doubles) into this Nedelec space (ndof device doubles), the G that HypreAMS
+ * takes (MFEM's DiscreteLinearOperator with a GradientInterpolator); exact:
+ * curl(G u) = 0.  Tet meshes.                                              */
+hc_status hc_tet_gradient_device(hcop_t* h, const double* u, double* y);
 /* Solve J X = B for nrhs right-hand sides together (block PCG with Jacobi,
  * one batched element-matrix apply per iteration for all columns), device
  * pointers in the [dof][rhs] layout of hc_mult_multi_device; X holds the
@@ -214,7 +219,11 @@ hc_status hc_tet_element_matrix(hcop_t* h, int64_t e, double* out);
  * residuals inside FP64 iterative refinement, with an FP64 block PCG from
  * the refined X when a refinement step stops cutting the residuals.  info
  * holds nrhs reports; returns the first non-OK column status.  Tet meshes;
- * nrhs in {1, 2, 4, 8, 16, 32}; precond HC_PRECOND_JACOBI.  Replaces R
+ * nrhs in {1, 2, 4, 8, 16, 32}; precond HC_PRECOND_JACOBI, or
+ * HC_PRECOND_AUX: Jacobi plus the gradient-space correction (PG) V (PG)^T
+ * with V one V-cycle of a smoothed-aggregation AMG on the P1 nodal operator
+ * (PG)^T J (PG), applied to all columns at once (hc_solve / hc_solve_device
+ * with HC_PRECOND_AUX on a tet mesh run this with nrhs = 1).  Replaces R
  * separate HyprePCG solves of the same operator
  * (hcurl_formulation.cpp:81-85, problem_builder_base.cpp:221-253).        */
 hc_status hc_solve_multi_device(hcop_t* h, const hc_solve_params* prm, int32_t nrhs, const double* B, double* X,
