@@ -126,6 +126,7 @@ _SIGS = {
     "hc_graph_solve_info": (C.c_int, [C.c_void_p, C.POINTER(SolveInfo)]),
     "hc_solve_complex_batch": (C.c_int, [C.c_int32, C.c_void_p, C.POINTER(SolveParams), C.c_void_p, C.c_void_p,
                                          C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(SolveInfo)]),
+    "hc_aux_levels": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32]),
     "hc_tet_gradient_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "hc_solve_multi_device": (C.c_int, [C.c_void_p, C.POINTER(SolveParams), C.c_int32, C.c_void_p, C.c_void_p,
                                         C.POINTER(SolveInfo)]),

@@ -23,7 +23,7 @@ namespace hc {
 
 constexpr int kMaxRhs = 32;
 constexpr int kMThreads = 256;
-constexpr int kMBlocks = 608;  // 4 x 152 SMs
+constexpr int kMBlocks = 1216;  // 8 x 152 SMs: 64 resident warps per SM
 
 struct MScalars {
   double rz[kMaxRhs], rr[kMaxRhs], bb[kMaxRhs], tol2[kMaxRhs], alpha[kMaxRhs], beta[kMaxRhs];
@@ -66,14 +66,16 @@ __device__ const double* mgrid_sum(double (&v)[NV], int R, double* partials, uns
   __syncthreads();
   if (!last) return nullptr;
   __threadfence();
-  if (threadIdx.x < R) {
+  // one warp per (value, rhs) pair: lanes stride over the block partials in a
+  // fixed order, then a fixed shuffle tree
+  for (int pr = w; pr < NV * R; pr += kMThreads / 32) {
+    const int k = pr / R, rr = pr % R;
+    const volatile double* src = partials + ((size_t)k * R + rr) * gridDim.x;
+    double s = 0.0;
+    for (unsigned int b = lane; b < gridDim.x; b += 32) s += src[b];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      double s = 0.0;
-      for (unsigned int b = 0; b < gridDim.x; ++b)
-        s += ((volatile double*)partials)[((size_t)k * R + threadIdx.x) * gridDim.x + b];
-      tot[k * kMaxRhs + threadIdx.x] = s;
-    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) tot[k * kMaxRhs + rr] = s;
   }
   __syncthreads();
   if (threadIdx.x != 0) return nullptr;
@@ -81,24 +83,63 @@ __device__ const double* mgrid_sum(double (&v)[NV], int R, double* partials, uns
   return tot;
 }
 
-// loop over entries i = dof * R + rhs owned by this thread (one rhs per thread)
-#define M_LOOP(i, n, R) \
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (n) * (R); i += (int64_t)gridDim.x * blockDim.x)
+// Loop over the entries i = dof * R + rhs of this thread.  The grid stride is a
+// multiple of R, so every thread keeps one right-hand side, K_COL = tid % R,
+// and the dof is i >> lgR (R a power of two).
+#define M_THREAD(R)                                                          \
+  const int64_t m_t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;       \
+  const int64_t m_stride = (int64_t)gridDim.x * blockDim.x;                  \
+  const int K_COL = (int)(m_t0 & ((R) - 1));                                 \
+  const int m_lg = __ffs(R) - 1;                                             \
+  (void)K_COL;                                                               \
+  (void)m_lg
+#define M_LOOP(i, n, R) _Pragma("unroll 4") for (int64_t i = m_t0; i < (n) * (R); i += m_stride)
+
+// Per-thread partial sums.  FP32 vectors accumulate runs of 32 terms in FP32
+// and flush them into FP64 (GB300's FP64 rate is a small fraction of its FP32
+// rate); FP64 vectors accumulate in FP64.
+template <typename T, int NV>
+struct MAcc {
+  double v[NV];
+  T a[NV];
+  int cnt;
+  __device__ MAcc() : cnt(0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      v[k] = 0.0;
+      a[k] = T(0);
+    }
+  }
+  __device__ __forceinline__ void flush() {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      v[k] += (double)a[k];
+      a[k] = T(0);
+    }
+    cnt = 0;
+  }
+  __device__ __forceinline__ void step() {
+    if (sizeof(T) == 4 && ++cnt == 32) flush();
+  }
+};
 
 // r = b - q; bb, rr, rz per rhs; tolerances and the first stopping test
 template <typename T>
 __global__ void __launch_bounds__(kMThreads)
     k_m_setup(int64_t n, int R, const T* __restrict__ b, const T* __restrict__ q, T* __restrict__ r,
               const T* __restrict__ dinv, MScalars* S, double* partials) {
-  double v[3] = {0, 0, 0};
+  M_THREAD(R);
+  MAcc<T, 3> acc;
   M_LOOP(i, n, R) {
-    const double bi = b[i], ri = bi - (double)q[i];
-    r[i] = (T)ri;
-    v[0] += bi * bi;
-    v[1] += ri * ri;
-    v[2] += ri * ri * (double)dinv[i / R];
+    const T bi = b[i], ri = bi - q[i];
+    r[i] = ri;
+    acc.a[0] += bi * bi;
+    acc.a[1] += ri * ri;
+    acc.a[2] += ri * ri * dinv[i >> m_lg];
+    acc.step();
   }
-  if (const double* tot = mgrid_sum<3>(v, R, partials, &S->counter[0])) {
+  acc.flush();
+  if (const double* tot = mgrid_sum<3>(acc.v, R, partials, &S->counter[0])) {
     int all = 1;
     for (int k = 0; k < R; ++k) {
       S->bb[k] = tot[k];
@@ -125,14 +166,17 @@ __global__ void __launch_bounds__(kMThreads)
 
 // p = z + beta p with z = B r (z == nullptr: z = D^-1 r; p = 0 for a stopped rhs); q = (I - P) p
 template <typename T>
-__global__ void k_m_dir(int64_t n, int R, const T* __restrict__ r, const T* __restrict__ z, const T* __restrict__ dinv,
-                        T* __restrict__ p, T* __restrict__ q, const uint8_t* __restrict__ ess, const MScalars* S) {
+__global__ void __launch_bounds__(kMThreads)
+    k_m_dir(int64_t n, int R, const T* __restrict__ r, const T* __restrict__ z, const T* __restrict__ dinv,
+            T* __restrict__ p, T* __restrict__ q, const uint8_t* __restrict__ ess, const MScalars* S) {
   if (S->all_done) return;
+  M_THREAD(R);
+  const bool stop = S->done[K_COL] != 0;
+  const T beta = (T)S->beta[K_COL];
   M_LOOP(i, n, R) {
-    const int k = (int)(i % R);
-    const int64_t d = i / R;
+    const int64_t d = i >> m_lg;
     const T zi = z ? z[i] : dinv[d] * r[i];
-    const T pi = S->done[k] ? T(0) : zi + (T)S->beta[k] * p[i];
+    const T pi = stop ? T(0) : zi + beta * p[i];
     p[i] = pi;
     q[i] = ess[d] ? pi : T(0);
   }
@@ -143,9 +187,14 @@ template <typename T>
 __global__ void __launch_bounds__(kMThreads)
     k_m_alpha(int64_t n, int R, const T* __restrict__ p, const T* __restrict__ q, MScalars* S, double* partials) {
   if (S->all_done) return;
-  double v[1] = {0};
-  M_LOOP(i, n, R) v[0] += (double)p[i] * (double)q[i];
-  if (const double* tot = mgrid_sum<1>(v, R, partials, &S->counter[1])) {
+  M_THREAD(R);
+  MAcc<T, 1> acc;
+  M_LOOP(i, n, R) {
+    acc.a[0] += p[i] * q[i];
+    acc.step();
+  }
+  acc.flush();
+  if (const double* tot = mgrid_sum<1>(acc.v, R, partials, &S->counter[1])) {
     for (int k = 0; k < R; ++k) {
       if (S->done[k]) {
         S->alpha[k] = 0.0;
@@ -169,17 +218,19 @@ __global__ void __launch_bounds__(kMThreads)
     k_m_update(int64_t n, int R, T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
                const T* __restrict__ q, const T* __restrict__ dinv, int jac, MScalars* S, double* partials) {
   if (S->all_done) return;
-  double v[2] = {0, 0};
+  M_THREAD(R);
+  const T a = (T)S->alpha[K_COL];
+  MAcc<T, 2> acc;
   M_LOOP(i, n, R) {
-    const int k = (int)(i % R);
-    const T a = (T)S->alpha[k];
     x[i] += a * p[i];
     const T ri = r[i] - a * q[i];
     r[i] = ri;
-    v[0] += (double)ri * (double)ri;
-    if (jac) v[1] += (double)ri * (double)ri * (double)dinv[i / R];
+    acc.a[0] += ri * ri;
+    if (jac) acc.a[1] += ri * ri * dinv[i >> m_lg];
+    acc.step();
   }
-  if (const double* tot = mgrid_sum<2>(v, R, partials, &S->counter[2])) {
+  acc.flush();
+  if (const double* tot = mgrid_sum<2>(acc.v, R, partials, &S->counter[2])) {
     S->iter += 1;
     int all = 1;
     for (int k = 0; k < R; ++k) {
@@ -213,9 +264,14 @@ __global__ void __launch_bounds__(kMThreads)
     k_m_rz(int64_t n, int R, const T* __restrict__ r, const T* __restrict__ z, int first, MScalars* S,
            double* partials) {
   if (S->all_done) return;
-  double v[1] = {0};
-  M_LOOP(i, n, R) v[0] += (double)r[i] * (double)z[i];
-  if (const double* tot = mgrid_sum<1>(v, R, partials, &S->counter[1])) {
+  M_THREAD(R);
+  MAcc<T, 1> acc;
+  M_LOOP(i, n, R) {
+    acc.a[0] += r[i] * z[i];
+    acc.step();
+  }
+  acc.flush();
+  if (const double* tot = mgrid_sum<1>(acc.v, R, partials, &S->counter[1])) {
     for (int k = 0; k < R; ++k) {
       if (first) {
         S->rz[k] = tot[k];
@@ -232,6 +288,7 @@ __global__ void __launch_bounds__(kMThreads)
 __global__ void __launch_bounds__(kMThreads)
     k_m_resid64(int64_t n, int R, const double* __restrict__ b, double* __restrict__ r, MScalars* S,
                 double* partials) {
+  M_THREAD(R);
   double v[2] = {0, 0};
   M_LOOP(i, n, R) {
     const double bi = b[i], ri = bi - r[i];
@@ -246,17 +303,22 @@ __global__ void __launch_bounds__(kMThreads)
     }
 }
 // rf = r / |r_k| per column (FP32); c = 0
-__global__ void k_m_d2f(int64_t n, int R, const double* __restrict__ r, const double* __restrict__ inv,
-                        float* __restrict__ rf, float* __restrict__ c) {
+__global__ void __launch_bounds__(kMThreads)
+    k_m_d2f(int64_t n, int R, const double* __restrict__ r, const double* __restrict__ inv, float* __restrict__ rf,
+            float* __restrict__ c) {
+  M_THREAD(R);
+  const double s = inv[K_COL];
   M_LOOP(i, n, R) {
-    rf[i] = (float)(r[i] * inv[i % R]);
+    rf[i] = (float)(r[i] * s);
     c[i] = 0.0f;
   }
 }
 // x += |r_k| c per column
-__global__ void k_m_axpy(int64_t n, int R, const float* __restrict__ c, const double* __restrict__ scale,
-                         double* __restrict__ x) {
-  M_LOOP(i, n, R) x[i] += scale[i % R] * (double)c[i];
+__global__ void __launch_bounds__(kMThreads)
+    k_m_axpy(int64_t n, int R, const float* __restrict__ c, const double* __restrict__ scale, double* __restrict__ x) {
+  M_THREAD(R);
+  const double s = scale[K_COL];
+  M_LOOP(i, n, R) x[i] += s * (double)c[i];
 }
 
 static inline unsigned mgrid(int64_t n, int R) {

@@ -107,6 +107,11 @@ struct TaLevel {
   float *xa = nullptr, *xb = nullptr, *b = nullptr, *r = nullptr, *d = nullptr;
 };
 
+// one warp per row, at most 16 blocks of 8 warps per SM
+static unsigned ta_rows_grid(int64_t rows) {
+  const int64_t b = (rows + kTaThreads / 32 - 1) / (kTaThreads / 32);
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 16));
+}
 static unsigned ta_grid(int64_t work) {
   const int64_t b = (work + kTaThreads - 1) / kTaThreads;
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, kTaMaxBlocks));
@@ -199,35 +204,122 @@ __global__ void k_ta_grad(int64_t ne, int p, const int32_t* __restrict__ sv, con
   }
 }
 
-#define TA_LOOP(t, n, R) \
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)(n) * (R); t += (int64_t)gridDim.x * blockDim.x)
+// Node-major kernels over [row][R] blocks: a thread owns W consecutive columns of
+// one row (W = 4 for R >= 4: 128-bit accesses for FP32, two 128-bit for FP64).
+template <int R>
+struct TaW {
+  static constexpr int W = R >= 4 ? 4 : 1;
+  static constexpr int G = R / W;  // threads per row
+};
+#define TA_VLOOP(t, n, R)                                                                          \
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)(n) * TaW<R>::G; \
+       t += (int64_t)gridDim.x * blockDim.x)
+
+template <int W>
+__device__ __forceinline__ void ldv(const float* __restrict__ p, float (&o)[W]) {
+  if constexpr (W == 4) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    o[0] = q.x;
+    o[1] = q.y;
+    o[2] = q.z;
+    o[3] = q.w;
+  } else {
+    o[0] = *p;
+  }
+}
+template <int W>
+__device__ __forceinline__ void ldv(const double* __restrict__ p, double (&o)[W]) {
+  if constexpr (W == 4) {
+    const double2 a = *reinterpret_cast<const double2*>(p), b = *reinterpret_cast<const double2*>(p + 2);
+    o[0] = a.x;
+    o[1] = a.y;
+    o[2] = b.x;
+    o[3] = b.y;
+  } else {
+    o[0] = *p;
+  }
+}
+template <int W>
+__device__ __forceinline__ void stv(float* __restrict__ p, const float (&o)[W]) {
+  if constexpr (W == 4)
+    *reinterpret_cast<float4*>(p) = make_float4(o[0], o[1], o[2], o[3]);
+  else
+    *p = o[0];
+}
+template <int W>
+__device__ __forceinline__ void stv(double* __restrict__ p, const double (&o)[W]) {
+  if constexpr (W == 4) {
+    *reinterpret_cast<double2*>(p) = make_double2(o[0], o[1]);
+    *reinterpret_cast<double2*>(p + 2) = make_double2(o[2], o[3]);
+  } else {
+    *p = o[0];
+  }
+}
+
+// Row-block kernels of the V-cycle: one warp per row, lane = column c (R
+// lanes) x nonzero slice (32 / R slices), slices combined by shuffles; the
+// row's elementwise work is done by the first slice.
+template <int R>
+struct TaRow {
+  static constexpr int S = 32 / R;
+};
+#define TA_WARP_ROWS(i, n)                                                              \
+  const int lane = threadIdx.x & 31, c = lane % R, slice = lane / R;                    \
+  (void)c;                                                                              \
+  (void)slice;                                                                          \
+  for (int i = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < (n);   \
+       i += (int)(((int64_t)gridDim.x * blockDim.x) >> 5))
 
 template <int R>
-__device__ __forceinline__ float ta_row(const DCsr& M, int i, int c, const float* __restrict__ x) {
+__device__ __forceinline__ float ta_row(const DCsr& M, int i, int c, int slice, const float* __restrict__ x) {
   float s = 0.f;
   const int e = M.rp[i + 1];
-  for (int k = M.rp[i]; k < e; ++k) s += M.va[k] * x[(int64_t)M.ci[k] * R + c];
+  for (int k = M.rp[i] + slice; k < e; k += TaRow<R>::S) s += M.va[k] * x[(int64_t)M.ci[k] * R + c];
+#pragma unroll
+  for (int o = R; o < 32; o <<= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   return s;
 }
 
 // b = G^T r (nn nodal rows); fuse: x = d = c0 D^-1 b on the nv vertex rows
-// (first Chebyshev step of the AMG's finest level)
+// (first Chebyshev step of the AMG's finest level).  One warp per row: lane =
+// column group (W columns, 128-bit accesses) x nonzero slice.
 template <typename T, int R>
 __global__ void __launch_bounds__(kTaThreads)
     k_ta_gt(int n, int nv, DCsr Gt, const T* __restrict__ r, float* __restrict__ b, float* __restrict__ x,
             float* __restrict__ d, const float* __restrict__ dinv, float c0, int fuse, const int* done) {
   if (done && *done) return;
-  TA_LOOP(t, n, R) {
-    const int i = (int)(t / R), c = (int)(t % R);
-    T s = 0;
+  constexpr int W = TaW<R>::W, G = TaW<R>::G, S = 32 / G;
+  const int lane = threadIdx.x & 31, c = (lane % G) * W, slice = lane / G;
+  for (int i = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < n;
+       i += (int)(((int64_t)gridDim.x * blockDim.x) >> 5)) {
+    T sacc[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) sacc[w] = T(0);
     const int e = Gt.rp[i + 1];
-    for (int k = Gt.rp[i]; k < e; ++k) s += (T)Gt.va[k] * r[(int64_t)Gt.ci[k] * R + c];
-    const float bs = (float)s;
-    b[t] = bs;
-    if (fuse && i < nv) {
-      const float dv = c0 * dinv[i] * bs;
-      d[t] = dv;
-      x[t] = dv;
+    for (int k = Gt.rp[i] + slice; k < e; k += S) {
+      const T a = (T)Gt.va[k];
+      T rv[W];
+      ldv<W>(r + (int64_t)Gt.ci[k] * R + c, rv);
+#pragma unroll
+      for (int w = 0; w < W; ++w) sacc[w] += a * rv[w];
+    }
+#pragma unroll
+    for (int o = G; o < 32; o <<= 1)
+#pragma unroll
+      for (int w = 0; w < W; ++w) sacc[w] += __shfl_xor_sync(0xffffffffu, sacc[w], o);
+    if (slice == 0) {
+      const int64_t q = (int64_t)i * R + c;
+      float bs[W];
+#pragma unroll
+      for (int w = 0; w < W; ++w) bs[w] = (float)sacc[w];
+      stv<W>(b + q, bs);
+      if (fuse && i < nv) {
+        const float f = c0 * dinv[i];
+#pragma unroll
+        for (int w = 0; w < W; ++w) bs[w] *= f;
+        stv<W>(d + q, bs);
+        stv<W>(x + q, bs);
+      }
     }
   }
 }
@@ -239,12 +331,14 @@ __global__ void __launch_bounds__(kTaThreads)
               const float* __restrict__ xin, float* __restrict__ xout, float* __restrict__ d, float c1, float c2,
               int first, const int* done) {
   if (done && *done) return;
-  TA_LOOP(t, n, R) {
-    const int i = (int)(t / R), c = (int)(t % R);
-    const float rr = b[t] - ta_row<R>(A, i, c, xin);
-    const float dn = (first ? 0.f : c1 * d[t]) + c2 * dinv[i] * rr;
-    d[t] = dn;
-    xout[t] = xin[t] + dn;
+  TA_WARP_ROWS(i, n) {
+    const float ax = ta_row<R>(A, i, c, slice, xin);
+    if (slice == 0) {
+      const int64_t q = (int64_t)i * R + c;
+      const float dn = (first ? 0.f : c1 * d[q]) + c2 * dinv[i] * (b[q] - ax);
+      d[q] = dn;
+      xout[q] = xin[q] + dn;
+    }
   }
 }
 
@@ -253,9 +347,12 @@ __global__ void __launch_bounds__(kTaThreads)
     k_ta_resid(int n, DCsr A, const float* __restrict__ b, const float* __restrict__ x, float* __restrict__ r,
                const int* done) {
   if (done && *done) return;
-  TA_LOOP(t, n, R) {
-    const int i = (int)(t / R), c = (int)(t % R);
-    r[t] = b[t] - ta_row<R>(A, i, c, x);
+  TA_WARP_ROWS(i, n) {
+    const float ax = ta_row<R>(A, i, c, slice, x);
+    if (slice == 0) {
+      const int64_t q = (int64_t)i * R + c;
+      r[q] = b[q] - ax;
+    }
   }
 }
 
@@ -265,14 +362,16 @@ __global__ void __launch_bounds__(kTaThreads)
     k_ta_restrict(int nc, DCsr Rm, const float* __restrict__ r, float* __restrict__ bc, float* __restrict__ xc,
                   float* __restrict__ dc, const float* __restrict__ dinv, float c0, int fuse, const int* done) {
   if (done && *done) return;
-  TA_LOOP(t, nc, R) {
-    const int i = (int)(t / R), c = (int)(t % R);
-    const float s = ta_row<R>(Rm, i, c, r);
-    bc[t] = s;
-    if (fuse) {
-      const float dv = c0 * dinv[i] * s;
-      dc[t] = dv;
-      xc[t] = dv;
+  TA_WARP_ROWS(i, nc) {
+    const float sv = ta_row<R>(Rm, i, c, slice, r);
+    if (slice == 0) {
+      const int64_t q = (int64_t)i * R + c;
+      bc[q] = sv;
+      if (fuse) {
+        const float dv = c0 * dinv[i] * sv;
+        dc[q] = dv;
+        xc[q] = dv;
+      }
     }
   }
 }
@@ -281,9 +380,9 @@ template <int R>
 __global__ void __launch_bounds__(kTaThreads)
     k_ta_prolong(int n, DCsr P, const float* __restrict__ xc, float* __restrict__ x, const int* done) {
   if (done && *done) return;
-  TA_LOOP(t, n, R) {
-    const int i = (int)(t / R), c = (int)(t % R);
-    x[t] += ta_row<R>(P, i, c, xc);
+  TA_WARP_ROWS(i, n) {
+    const float pv = ta_row<R>(P, i, c, slice, xc);
+    if (slice == 0) x[(int64_t)i * R + c] += pv;
   }
 }
 
@@ -293,12 +392,13 @@ __global__ void __launch_bounds__(kTaThreads)
     k_ta_dense(int nc, const float* __restrict__ cinv, const float* __restrict__ cs, const float* __restrict__ b,
                float* __restrict__ x, const int* done) {
   if (done && *done) return;
-  TA_LOOP(t, nc, R) {
-    const int i = (int)(t / R), c = (int)(t % R);
+  TA_WARP_ROWS(i, nc) {
     const float* row = cinv + (int64_t)i * nc;
-    float s = 0.f;
-    for (int j = 0; j < nc; ++j) s += row[j] * cs[j] * b[(int64_t)j * R + c];
-    x[t] = cs[i] * s;
+    float acc = 0.f;
+    for (int j = slice; j < nc; j += TaRow<R>::S) acc += row[j] * cs[j] * b[(int64_t)j * R + c];
+#pragma unroll
+    for (int o = R; o < 32; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (slice == 0) x[(int64_t)i * R + c] = cs[i] * acc;
   }
 }
 
@@ -311,37 +411,57 @@ __global__ void __launch_bounds__(kTaThreads)
            const float* __restrict__ x0, const float* __restrict__ rn, const float* __restrict__ dl,
            const T* __restrict__ r, const T* __restrict__ dinv, T* __restrict__ z, const int* done) {
   if (done && *done) return;
-  TA_LOOP(t, ndof, R) {
-    const int64_t dof = t / R;
-    const int c = (int)(t % R);
+  constexpr int W = TaW<R>::W, G = TaW<R>::G;
+  TA_VLOOP(t, ndof, R) {
+    const int64_t dof = t / G;
+    const int c = (int)(t % G) * W;
     const bool face = dof >= nface0;
     const bool s1 = face && ((dof - nface0) & 1);
-    float v = 0.f;
+    float v[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) v[w] = 0.f;
+    auto addv = [&](int nd, float coef) {  // vertex row: coef (x0 + D_L^-1 rn)
+      const int64_t q = (int64_t)nd * R + c;
+      float xv[W];
+      ldv<W>(x0 + q, xv);
+      if (dl) {
+        float rv[W];
+        ldv<W>(rn + q, rv);
+        const float f = dl[nd];
+#pragma unroll
+        for (int w = 0; w < W; ++w) xv[w] += f * rv[w];
+      }
+#pragma unroll
+      for (int w = 0; w < W; ++w) v[w] += coef * xv[w];
+    };
+    auto adde = [&](int ge, float coef) {  // edge-bubble row: coef D_L^-1 rn
+      const int nd = nv + ge;
+      float rv[W];
+      ldv<W>(rn + (int64_t)nd * R + c, rv);
+      const float f = coef * dl[nd];
+#pragma unroll
+      for (int w = 0; w < W; ++w) v[w] += f * rv[w];
+    };
     {
       const int n0 = gnode[3 * dof], n1 = gnode[3 * dof + 1], n2 = gnode[3 * dof + 2];
-      const float c0 = -1.f, c1 = face ? (s1 ? -1.f : 2.f) : 1.f, c2 = face ? (s1 ? 2.f : -1.f) : 0.f;
-      auto xv = [&](int nd) {
-        const int64_t q = (int64_t)nd * R + c;
-        return dl ? x0[q] + dl[nd] * rn[q] : x0[q];
-      };
-      if (n0 >= 0) v += c0 * xv(n0);
-      if (n1 >= 0) v += c1 * xv(n1);
-      if (n2 >= 0) v += c2 * xv(n2);
+      if (n0 >= 0) addv(n0, -1.f);
+      if (n1 >= 0) addv(n1, face ? (s1 ? -1.f : 2.f) : 1.f);
+      if (n2 >= 0) addv(n2, s1 ? 2.f : -1.f);
     }
     if (gedge) {
       const int e0 = gedge[3 * dof], e1 = gedge[3 * dof + 1], e2 = gedge[3 * dof + 2];
       // edge dofs: (+1 | -1) on their own bubble; face dofs F0: (1, -2, 1), F1: (-2, 1, 1) on edges ij, ik, jk
-      const float b0 = face ? (s1 ? -2.f : 1.f) : (((dof & 1) == 0) ? 1.f : -1.f);
-      const float b1 = s1 ? 1.f : -2.f, b2 = 1.f;
-      auto xe = [&](int ge) {
-        const int nd = nv + ge;
-        return dl[nd] * rn[(int64_t)nd * R + c];
-      };
-      if (e0 >= 0) v += b0 * xe(e0);
-      if (e1 >= 0) v += b1 * xe(e1);
-      if (e2 >= 0) v += b2 * xe(e2);
+      if (e0 >= 0) adde(e0, face ? (s1 ? -2.f : 1.f) : (((dof & 1) == 0) ? 1.f : -1.f));
+      if (e1 >= 0) adde(e1, s1 ? 1.f : -2.f);
+      if (e2 >= 0) adde(e2, 1.f);
     }
-    z[t] = dinv[dof] * r[t] + (T)v;
+    const int64_t o = dof * R + c;
+    T rv[W], zv[W];
+    ldv<W>(r + o, rv);
+    const T di = dinv[dof];
+#pragma unroll
+    for (int w = 0; w < W; ++w) zv[w] = di * rv[w] + (T)v[w];
+    stv<W>(z + o, zv);
   }
 }
 
@@ -889,7 +1009,7 @@ hc_status tetaux_reserve(hcop* h, int R) {
 template <int R>
 static float* ta_vcycle(const TetAux* X, int l, const int* done, cudaStream_t s) {
   const TaLevel& Lv = X->lev[l];
-  const unsigned g = ta_grid((int64_t)Lv.n * R);
+  const unsigned g = ta_rows_grid(Lv.n);
   if (l == X->nlev - 1) {
     if (X->cinv) {
       k_ta_dense<R><<<g, kTaThreads, 0, s>>>(Lv.n, X->cinv, X->cs, Lv.b, Lv.xb, done);
@@ -903,7 +1023,7 @@ static float* ta_vcycle(const TetAux* X, int l, const int* done, cudaStream_t s)
   const bool next_dense = (l + 1 == X->nlev - 1) && X->cinv;
   k_ta_step<R><<<g, kTaThreads, 0, s>>>(Lv.n, Lv.A, Lv.dinv, Lv.b, Lv.xa, Lv.xb, Lv.d, Lv.c1, Lv.c2, 0, done);
   k_ta_resid<R><<<g, kTaThreads, 0, s>>>(Lv.n, Lv.A, Lv.b, Lv.xb, Lv.r, done);
-  k_ta_restrict<R><<<ta_grid((int64_t)Nx.n * R), kTaThreads, 0, s>>>(Nx.n, Lv.R, Lv.r, Nx.b, Nx.xa, Nx.d, Nx.dinv,
+  k_ta_restrict<R><<<ta_rows_grid(Nx.n), kTaThreads, 0, s>>>(Nx.n, Lv.R, Lv.r, Nx.b, Nx.xa, Nx.d, Nx.dinv,
                                                                       Nx.c0, next_dense ? 0 : 1, done);
   const float* xc = ta_vcycle<R>(X, l + 1, done, s);
   k_ta_prolong<R><<<g, kTaThreads, 0, s>>>(Lv.n, Lv.P, xc, Lv.xb, done);
@@ -918,10 +1038,10 @@ static cudaError_t ta_apply_r(const hcop* h, const T* r, T* z, const T* dinv, co
   const TaLevel& L0 = X->lev[0];
   const bool dense0 = X->nlev == 1 && X->cinv;
   // level 0's right-hand side is the vertex block of rn (L0.b == X->rn)
-  k_ta_gt<T, R><<<ta_grid((int64_t)X->nn * R), kTaThreads, 0, s>>>(X->nn, X->nfree, X->Gt, r, X->rn, L0.xa, L0.d,
+  k_ta_gt<T, R><<<ta_rows_grid(X->nn), kTaThreads, 0, s>>>(X->nn, X->nfree, X->Gt, r, X->rn, L0.xa, L0.d,
                                                                     L0.dinv, L0.c0, dense0 ? 0 : 1, done);
   const float* x0 = ta_vcycle<R>(X, 0, done, s);
-  k_ta_g<T, R><<<ta_grid(h->ndof * R), kTaThreads, 0, s>>>(h->ndof, X->gnode, X->gedge, X->nface0, X->nfree, x0,
+  k_ta_g<T, R><<<ta_grid(h->ndof * TaW<R>::G), kTaThreads, 0, s>>>(h->ndof, X->gnode, X->gedge, X->nface0, X->nfree, x0,
                                                             X->rn, X->dl, r, dinv, z, done);
   return cudaGetLastError();
 }
@@ -957,3 +1077,11 @@ cudaError_t tet_gradient(const hcop* h, const double* u, double* y, cudaStream_t
 }
 
 }  // namespace hc
+
+extern "C" int32_t hc_aux_levels(const hcop_t* h, int64_t* sizes, int32_t max_levels) {
+  if (!h || !h->taux) return 0;
+  const hc::TetAux* X = static_cast<const hc::TetAux*>(h->taux);
+  for (int l = 0; l < X->nlev && l < max_levels; ++l) sizes[l] = X->lev[l].n;
+  if (max_levels > X->nlev) sizes[X->nlev] = X->nn - X->nfree;  // edge-bubble rows after the levels
+  return X->nlev;
+}

@@ -293,6 +293,13 @@ class HCurlOperator:
         N.check(N.lib().hc_mult_multi_device(self.h, prec, nrhs, _dev_ptr(X, name), _dev_ptr(Y, name)), self.h)
         return Y
 
+    def AuxLevels(self):
+        """Sizes of the tet auxiliary-space AMG levels (free vertices first) and
+        the number of free edge bubbles, once an 'aux' solve has set it up."""
+        sizes = np.zeros(16, dtype=np.int64)
+        n = N.lib().hc_aux_levels(self.h, _ptr(sizes), 15)
+        return {"levels": [int(x) for x in sizes[:n]], "edge_bubbles": int(sizes[n]) if n else 0}
+
     def GradientDevice(self, u, y):
         """y = G u: discrete gradient of P1 vertex values u (float64 CUDA tensor
         of n_vert entries) into this Nedelec space (tet meshes)."""

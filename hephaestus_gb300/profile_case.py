@@ -11,6 +11,9 @@ dt = 0.01 (the benchmark's coefficient distributions) and applies it:
           the coil load, capped at 8 inner iterations and 1 refinement step
   complex - y = (C + i omega M) x in FP32 (fused complex kernel), 5 times
   tets  - Kuhn N^3 tet mesh (jitter 0.15 h), order P: 16-RHS FP32 apply, 3 times
+  tetsolve - the same tet mesh: one mixed-precision 16-RHS block solve of coil
+          loads (auxiliary-space preconditioner), capped at 8 inner iterations
+          and 1 refinement step
 """
 import sys
 
@@ -26,11 +29,27 @@ def main(argv):
     p = int(argv[1]) if len(argv) > 1 else 2
     mode = argv[2] if len(argv) > 2 else "mult"
     rng = np.random.default_rng(0)
-    if mode == "tets":
+    if mode in ("tets", "tetsolve"):
         v, t, bt, ba = meshes.kuhn_mesh(n, jitter=0.15, seed=0)
         ne = len(t)
         op = HCurlOperator.from_tets(v, t, p, meshes.loguniform(ne, 1, 1e3, rng), meshes.loguniform(ne, 1e-2, 1e6, rng),
                                      dt=0.01, btris=bt, battr=ba, ess_attr_bits=0x3F)
+        if mode == "tetsolve":
+            from hephaestus_gb300 import GpuHCurlPCGSolver
+
+            B = torch.empty(op.ndof, 16, dtype=torch.float64, device="cuda")
+            col = torch.empty(op.ndof, dtype=torch.float64, device="cuda")
+            free = torch.tensor(op.ess_mask() == 0, device="cuda")
+            for k in range(16):
+                op.LoadCoilDevice(col, I0=0.5 + 0.1 * k, xc=0.45 + 0.01 * k, q=4)
+                B[:, k] = col * free
+            X = torch.zeros_like(B)
+            s = GpuHCurlPCGSolver({"Tolerance": 1e-10, "MaxIter": 8, "MaxOuter": 1, "Precision": "mixed",
+                                   "Preconditioner": "aux"}, op)
+            s.MultMultiDevice(B, X)
+            torch.cuda.synchronize()
+            print("ok", mode, op.ndof, op.AuxLevels())
+            return
         X = torch.randn(op.ndof, 16, device="cuda")
         Y = torch.empty_like(X)
         for _ in range(3):

@@ -228,6 +228,11 @@ hc_status hc_tet_gradient_device(hcop_t* h, const double* u, double* y);
  * (hcurl_formulation.cpp:81-85, problem_builder_base.cpp:221-253).        */
 hc_status hc_solve_multi_device(hcop_t* h, const hc_solve_params* prm, int32_t nrhs, const double* B, double* X,
                                 hc_solve_info* info);
+/* Tet auxiliary-space preconditioner, once set up by an HC_PRECOND_AUX solve:
+ * returns the number of AMG levels and writes their sizes (free vertices on
+ * level 0) to sizes[0..], followed by the number of free edge bubbles when
+ * max_levels allows; 0 before set-up.                                       */
+int32_t hc_aux_levels(const hcop_t* h, int64_t* sizes, int32_t max_levels);
 
 /* ---- frequency domain: A = C_nu + i omega M_sigma ------------------------------
  * The complex operator of ComplexMaxwellOperator::Solve
