@@ -760,8 +760,13 @@ hc_status hc_solve_device(hcop_t* h, const hc_solve_params* prm, const double* b
   hc_solve_info loc{};
   if (!info) info = &loc;
   std::memset(info, 0, sizeof(*info));
-  if (prm->precond == HC_PRECOND_AUX && h->type == HC_TET)  // one-column block PCG with the tet AMG
+  if (prm->precond == HC_PRECOND_AUX && h->type == HC_TET) {  // one-column block PCG with the tet AMG
+    if ((reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(x)) % 16 != 0) {
+      h->err = "hc_solve_device: b and x must be 16-byte aligned for tet AUX solves";
+      return HC_EINVAL;
+    }
     return multi_solve_device(h, prm, 1, b, x, info);
+  }
   if (prm->precond == HC_PRECOND_AUX) {
     st = auxmg_setup(h);
     if (st != HC_OK) return st;

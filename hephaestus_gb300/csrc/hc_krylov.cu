@@ -95,16 +95,8 @@ __global__ void __launch_bounds__(kRedThreads)
     k_dot_alpha(int64_t n, const T* __restrict__ p, const T* __restrict__ q, KrylovScalars* S, double* partials) {
   if (S->done) return;
   double v[1] = {0.0}, tot[1];
-  T acc = T(0);
-  int c = 0;
-  GS_LOOP(i, n) {
-    acc += p[i] * q[i];
-    if (++c == 8) {
-      v[0] += (double)acc;
-      acc = T(0);
-      c = 0;
-    }
-  }
+  T acc = T(0);  // per-thread sum in T: no per-element FP64 work (GB300's FP64 rate is low)
+  GS_LOOP(i, n) acc += p[i] * q[i];
   v[0] += (double)acc;
   block_sum_n<1>(v);
   if (grid_sum_n<1>(v, partials, &S->counter[0], tot)) {
@@ -162,14 +154,18 @@ __global__ void __launch_bounds__(kRedThreads)
     k_pcg_setup(int64_t n, const T* __restrict__ b, const T* __restrict__ q, T* __restrict__ r,
                 const T* __restrict__ dinv, KrylovScalars* S, double* partials) {
   double v[3] = {0.0, 0.0, 0.0}, tot[3];
+  T a0 = T(0), a1 = T(0), a2 = T(0);  // per-thread sums in T (no per-element FP64 work)
   GS_LOOP(i, n) {
-    const double bi = (double)b[i];
-    const double ri = bi - (double)q[i];
-    r[i] = (T)ri;
-    v[0] += bi * bi;
-    v[1] += ri * ri;
-    if (JAC) v[2] += ri * ri * (dinv ? (double)dinv[i] : 1.0);
+    const T bi = b[i];
+    const T ri = bi - q[i];
+    r[i] = ri;
+    a0 += bi * bi;
+    a1 += ri * ri;
+    if (JAC) a2 += ri * ri * (dinv ? dinv[i] : T(1));
   }
+  v[0] = (double)a0;
+  v[1] = (double)a1;
+  v[2] = (double)a2;
   block_sum_n<3>(v);
   if (grid_sum_n<3>(v, partials, &S->counter[4], tot)) {
     S->bb = tot[0];
@@ -200,8 +196,7 @@ __global__ void __launch_bounds__(kRedThreads)
   if (S->done) return;
   const T a = (T)S->alpha;
   double v[2] = {0.0, 0.0}, tot[2];
-  T rrt = T(0), rzt = T(0);
-  int c = 0;
+  T rrt = T(0), rzt = T(0);  // per-thread sums in T (no per-element FP64 work)
   GS_LOOP(i, n) {
     x[i] += a * p[i];
     const T ri = r[i] - a * q[i];
@@ -209,12 +204,6 @@ __global__ void __launch_bounds__(kRedThreads)
     if (zout) zout[i] = dinv[i] * ri;
     rrt += ri * ri;
     if (JAC) rzt += ri * ri * (dinv ? dinv[i] : T(1));
-    if (++c == 8) {
-      v[0] += (double)rrt;
-      v[1] += (double)rzt;
-      rrt = rzt = T(0);
-      c = 0;
-    }
   }
   v[0] += (double)rrt;
   v[1] += (double)rzt;
@@ -266,16 +255,8 @@ __global__ void __launch_bounds__(kRedThreads)
               double* partials) {
   if (S->done) return;
   double v[1] = {0.0}, tot[1];
-  T acc = T(0);
-  int c = 0;
-  GS_LOOP(i, n) {
-    acc += r[i] * z[i];
-    if (++c == 8) {
-      v[0] += (double)acc;
-      acc = T(0);
-      c = 0;
-    }
-  }
+  T acc = T(0);  // per-thread sum in T (no per-element FP64 work)
+  GS_LOOP(i, n) acc += r[i] * z[i];
   v[0] += (double)acc;
   block_sum_n<1>(v);
   if (grid_sum_n<1>(v, partials, &S->counter[5], tot)) {

@@ -34,22 +34,27 @@ struct MScalars {
 };
 static_assert(sizeof(MScalars) <= 4096, "pinned scalar blocks are 4 KB");
 
-// Segmented (per right-hand side) sum of NV values per thread; thread t owns
-// rhs t % R.  Returns, on thread 0 of the last block, the grid totals in
-// shared memory (total of value k for rhs r at [k * kMaxRhs + r]); nullptr
-// elsewhere.
-template <int NV>
-__device__ const double* mgrid_sum(double (&v)[NV], int R, double* partials, unsigned int* counter) {
+// Segmented (per right-hand side) sum of NV x W values per thread; thread t
+// owns the W columns (W t) % R .. + W - 1 (W = 1: rhs t % R).  Returns, on
+// thread 0 of the last block, the grid totals in shared memory (total of value
+// k for rhs r at [k * kMaxRhs + r]); nullptr elsewhere.
+template <int NV, int W>
+__device__ const double* mgrid_sum(double (&v)[NV][W], int R, double* partials, unsigned int* counter) {
   __shared__ double sh[NV][kMThreads / 32][kMaxRhs];
   __shared__ double tot[NV * kMaxRhs];
   __shared__ bool last;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int G = R / W;  // lanes l and l + G own the same columns
 #pragma unroll
   for (int k = 0; k < NV; ++k)
-    for (int o = 16; o >= R; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
-  if (lane < R)
 #pragma unroll
-    for (int k = 0; k < NV; ++k) sh[k][w][lane] = v[k];
+    for (int q = 0; q < W; ++q)
+      for (int o = 16; o >= G; o >>= 1) v[k][q] += __shfl_down_sync(0xffffffffu, v[k][q], o);
+  if (lane < G)
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+#pragma unroll
+      for (int q = 0; q < W; ++q) sh[k][w][W * lane + q] = v[k][q];
   __syncthreads();
   // block partial per rhs, written by thread r < R
   if (threadIdx.x < R) {
@@ -59,8 +64,8 @@ __device__ const double* mgrid_sum(double (&v)[NV], int R, double* partials, uns
       for (int i = 0; i < kMThreads / 32; ++i) s += sh[k][i][threadIdx.x];
       partials[((size_t)k * R + threadIdx.x) * gridDim.x + blockIdx.x] = s;
     }
+    __threadfence();  // the partial writers publish before the ticket
   }
-  __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
   __syncthreads();
@@ -83,63 +88,113 @@ __device__ const double* mgrid_sum(double (&v)[NV], int R, double* partials, uns
   return tot;
 }
 
-// Loop over the entries i = dof * R + rhs of this thread.  The grid stride is a
-// multiple of R, so every thread keeps one right-hand side, K_COL = tid % R,
+// Loop over this thread's entries, W consecutive ones at a time (i = dof * R +
+// rhs; W = 4 for R >= 4: 128-bit accesses).  The grid stride is a multiple of
+// R, so a thread keeps its columns K_COL .. K_COL + W - 1, K_COL = (W tid) % R,
 // and the dof is i >> lgR (R a power of two).
-#define M_THREAD(R)                                                          \
+#define M_THREAD(R, W)                                                       \
   const int64_t m_t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;       \
-  const int64_t m_stride = (int64_t)gridDim.x * blockDim.x;                  \
-  const int K_COL = (int)(m_t0 & ((R) - 1));                                 \
+  const int64_t m_stride = (int64_t)gridDim.x * blockDim.x * (W);            \
+  const int K_COL = (int)((m_t0 * (W)) & ((R) - 1));                         \
   const int m_lg = __ffs(R) - 1;                                             \
   (void)K_COL;                                                               \
   (void)m_lg
-#define M_LOOP(i, n, R) _Pragma("unroll 4") for (int64_t i = m_t0; i < (n) * (R); i += m_stride)
+#define M_LOOP(i, n, R, W) _Pragma("unroll 4") for (int64_t i = m_t0 * (W); i < (n) * (R); i += m_stride)
 
-// Per-thread partial sums.  FP32 vectors accumulate runs of 32 terms in FP32
-// and flush them into FP64 (GB300's FP64 rate is a small fraction of its FP32
-// rate); FP64 vectors accumulate in FP64.
-template <typename T, int NV>
+template <int W>
+__device__ __forceinline__ void mld(const float* __restrict__ p, float (&o)[W]) {
+  if constexpr (W == 4) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    o[0] = q.x;
+    o[1] = q.y;
+    o[2] = q.z;
+    o[3] = q.w;
+  } else {
+    o[0] = *p;
+  }
+}
+template <int W>
+__device__ __forceinline__ void mld(const double* __restrict__ p, double (&o)[W]) {
+  if constexpr (W == 4) {
+    const double2 a = *reinterpret_cast<const double2*>(p), b = *reinterpret_cast<const double2*>(p + 2);
+    o[0] = a.x;
+    o[1] = a.y;
+    o[2] = b.x;
+    o[3] = b.y;
+  } else {
+    o[0] = *p;
+  }
+}
+template <int W>
+__device__ __forceinline__ void mst(float* __restrict__ p, const float (&o)[W]) {
+  if constexpr (W == 4)
+    *reinterpret_cast<float4*>(p) = make_float4(o[0], o[1], o[2], o[3]);
+  else
+    *p = o[0];
+}
+template <int W>
+__device__ __forceinline__ void mst(double* __restrict__ p, const double (&o)[W]) {
+  if constexpr (W == 4) {
+    *reinterpret_cast<double2*>(p) = make_double2(o[0], o[1]);
+    *reinterpret_cast<double2*>(p + 2) = make_double2(o[2], o[3]);
+  } else {
+    *p = o[0];
+  }
+}
+
+// Per-thread partial sums in the vectors' precision (a thread sums at most a
+// few hundred terms: n R / (W x 311,296 threads)), combined across threads,
+// blocks and the grid in FP64.  GB300's FP64 rate is a small fraction of its
+// FP32 rate, so FP32 vectors must not do per-element FP64 work.
+template <typename T, int NV, int W>
 struct MAcc {
-  double v[NV];
-  T a[NV];
-  int cnt;
-  __device__ MAcc() : cnt(0) {
+  double v[NV][W];
+  T a[NV][W];
+  __device__ MAcc() {
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      v[k] = 0.0;
-      a[k] = T(0);
-    }
+    for (int k = 0; k < NV; ++k)
+#pragma unroll
+      for (int q = 0; q < W; ++q) {
+        v[k][q] = 0.0;
+        a[k][q] = T(0);
+      }
   }
   __device__ __forceinline__ void flush() {
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      v[k] += (double)a[k];
-      a[k] = T(0);
-    }
-    cnt = 0;
+    for (int k = 0; k < NV; ++k)
+#pragma unroll
+      for (int q = 0; q < W; ++q) {
+        v[k][q] += (double)a[k][q];
+        a[k][q] = T(0);
+      }
   }
-  __device__ __forceinline__ void step() {
-    if (sizeof(T) == 4 && ++cnt == 32) flush();
-  }
+  __device__ __forceinline__ void step() {}
 };
 
 // r = b - q; bb, rr, rz per rhs; tolerances and the first stopping test
-template <typename T>
+template <typename T, int W>
 __global__ void __launch_bounds__(kMThreads)
     k_m_setup(int64_t n, int R, const T* __restrict__ b, const T* __restrict__ q, T* __restrict__ r,
               const T* __restrict__ dinv, MScalars* S, double* partials) {
-  M_THREAD(R);
-  MAcc<T, 3> acc;
-  M_LOOP(i, n, R) {
-    const T bi = b[i], ri = bi - q[i];
-    r[i] = ri;
-    acc.a[0] += bi * bi;
-    acc.a[1] += ri * ri;
-    acc.a[2] += ri * ri * dinv[i >> m_lg];
+  M_THREAD(R, W);
+  MAcc<T, 3, W> acc;
+  M_LOOP(i, n, R, W) {
+    T bv[W], qv[W];
+    mld<W>(b + i, bv);
+    mld<W>(q + i, qv);
+    const T di = dinv[i >> m_lg];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      qv[w] = bv[w] - qv[w];
+      acc.a[0][w] += bv[w] * bv[w];
+      acc.a[1][w] += qv[w] * qv[w];
+      acc.a[2][w] += qv[w] * qv[w] * di;
+    }
+    mst<W>(r + i, qv);
     acc.step();
   }
   acc.flush();
-  if (const double* tot = mgrid_sum<3>(acc.v, R, partials, &S->counter[0])) {
+  if (const double* tot = mgrid_sum<3, W>(acc.v, R, partials, &S->counter[0])) {
     int all = 1;
     for (int k = 0; k < R; ++k) {
       S->bb[k] = tot[k];
@@ -165,36 +220,59 @@ __global__ void __launch_bounds__(kMThreads)
 }
 
 // p = z + beta p with z = B r (z == nullptr: z = D^-1 r; p = 0 for a stopped rhs); q = (I - P) p
-template <typename T>
+template <typename T, int W>
 __global__ void __launch_bounds__(kMThreads)
     k_m_dir(int64_t n, int R, const T* __restrict__ r, const T* __restrict__ z, const T* __restrict__ dinv,
             T* __restrict__ p, T* __restrict__ q, const uint8_t* __restrict__ ess, const MScalars* S) {
   if (S->all_done) return;
-  M_THREAD(R);
-  const bool stop = S->done[K_COL] != 0;
-  const T beta = (T)S->beta[K_COL];
-  M_LOOP(i, n, R) {
+  M_THREAD(R, W);
+  T beta[W];
+  bool stop[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    stop[w] = S->done[K_COL + w] != 0;
+    beta[w] = (T)S->beta[K_COL + w];
+  }
+  M_LOOP(i, n, R, W) {
     const int64_t d = i >> m_lg;
-    const T zi = z ? z[i] : dinv[d] * r[i];
-    const T pi = stop ? T(0) : zi + beta * p[i];
-    p[i] = pi;
-    q[i] = ess[d] ? pi : T(0);
+    T zv[W], pv[W];
+    if (z) {
+      mld<W>(z + i, zv);
+    } else {
+      mld<W>(r + i, zv);
+      const T di = dinv[d];
+#pragma unroll
+      for (int w = 0; w < W; ++w) zv[w] *= di;
+    }
+    mld<W>(p + i, pv);
+#pragma unroll
+    for (int w = 0; w < W; ++w) pv[w] = stop[w] ? T(0) : zv[w] + beta[w] * pv[w];
+    mst<W>(p + i, pv);
+    if (!ess[d]) {
+#pragma unroll
+      for (int w = 0; w < W; ++w) pv[w] = T(0);
+    }
+    mst<W>(q + i, pv);
   }
 }
 
 // alpha = rz / p.q per rhs (q = J p)
-template <typename T>
+template <typename T, int W>
 __global__ void __launch_bounds__(kMThreads)
     k_m_alpha(int64_t n, int R, const T* __restrict__ p, const T* __restrict__ q, MScalars* S, double* partials) {
   if (S->all_done) return;
-  M_THREAD(R);
-  MAcc<T, 1> acc;
-  M_LOOP(i, n, R) {
-    acc.a[0] += p[i] * q[i];
+  M_THREAD(R, W);
+  MAcc<T, 1, W> acc;
+  M_LOOP(i, n, R, W) {
+    T pv[W], qv[W];
+    mld<W>(p + i, pv);
+    mld<W>(q + i, qv);
+#pragma unroll
+    for (int w = 0; w < W; ++w) acc.a[0][w] += pv[w] * qv[w];
     acc.step();
   }
   acc.flush();
-  if (const double* tot = mgrid_sum<1>(acc.v, R, partials, &S->counter[1])) {
+  if (const double* tot = mgrid_sum<1, W>(acc.v, R, partials, &S->counter[1])) {
     for (int k = 0; k < R; ++k) {
       if (S->done[k]) {
         S->alpha[k] = 0.0;
@@ -213,24 +291,36 @@ __global__ void __launch_bounds__(kMThreads)
 }
 
 // x += alpha p; r -= alpha q; rr per rhs and stopping tests; jac: rz = r.D^-1 r and beta
-template <typename T>
+template <typename T, int W>
 __global__ void __launch_bounds__(kMThreads)
     k_m_update(int64_t n, int R, T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
                const T* __restrict__ q, const T* __restrict__ dinv, int jac, MScalars* S, double* partials) {
   if (S->all_done) return;
-  M_THREAD(R);
-  const T a = (T)S->alpha[K_COL];
-  MAcc<T, 2> acc;
-  M_LOOP(i, n, R) {
-    x[i] += a * p[i];
-    const T ri = r[i] - a * q[i];
-    r[i] = ri;
-    acc.a[0] += ri * ri;
-    if (jac) acc.a[1] += ri * ri * dinv[i >> m_lg];
+  M_THREAD(R, W);
+  T a[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) a[w] = (T)S->alpha[K_COL + w];
+  MAcc<T, 2, W> acc;
+  M_LOOP(i, n, R, W) {
+    T xv[W], rv[W], pv[W], qv[W];
+    mld<W>(x + i, xv);
+    mld<W>(r + i, rv);
+    mld<W>(p + i, pv);
+    mld<W>(q + i, qv);
+    const T di = jac ? dinv[i >> m_lg] : T(0);
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      xv[w] += a[w] * pv[w];
+      rv[w] -= a[w] * qv[w];
+      acc.a[0][w] += rv[w] * rv[w];
+      acc.a[1][w] += rv[w] * rv[w] * di;
+    }
+    mst<W>(x + i, xv);
+    mst<W>(r + i, rv);
     acc.step();
   }
   acc.flush();
-  if (const double* tot = mgrid_sum<2>(acc.v, R, partials, &S->counter[2])) {
+  if (const double* tot = mgrid_sum<2, W>(acc.v, R, partials, &S->counter[2])) {
     S->iter += 1;
     int all = 1;
     for (int k = 0; k < R; ++k) {
@@ -259,19 +349,23 @@ __global__ void __launch_bounds__(kMThreads)
 }
 
 // rz = r.z per rhs; first: beta = 0, else beta = rz_new / rz_old (columns still running)
-template <typename T>
+template <typename T, int W>
 __global__ void __launch_bounds__(kMThreads)
     k_m_rz(int64_t n, int R, const T* __restrict__ r, const T* __restrict__ z, int first, MScalars* S,
            double* partials) {
   if (S->all_done) return;
-  M_THREAD(R);
-  MAcc<T, 1> acc;
-  M_LOOP(i, n, R) {
-    acc.a[0] += r[i] * z[i];
+  M_THREAD(R, W);
+  MAcc<T, 1, W> acc;
+  M_LOOP(i, n, R, W) {
+    T rv[W], zv[W];
+    mld<W>(r + i, rv);
+    mld<W>(z + i, zv);
+#pragma unroll
+    for (int w = 0; w < W; ++w) acc.a[0][w] += rv[w] * zv[w];
     acc.step();
   }
   acc.flush();
-  if (const double* tot = mgrid_sum<1>(acc.v, R, partials, &S->counter[1])) {
+  if (const double* tot = mgrid_sum<1, W>(acc.v, R, partials, &S->counter[1])) {
     for (int k = 0; k < R; ++k) {
       if (first) {
         S->rz[k] = tot[k];
@@ -288,15 +382,15 @@ __global__ void __launch_bounds__(kMThreads)
 __global__ void __launch_bounds__(kMThreads)
     k_m_resid64(int64_t n, int R, const double* __restrict__ b, double* __restrict__ r, MScalars* S,
                 double* partials) {
-  M_THREAD(R);
-  double v[2] = {0, 0};
-  M_LOOP(i, n, R) {
+  M_THREAD(R, 1);
+  double v[2][1] = {{0}, {0}};
+  M_LOOP(i, n, R, 1) {
     const double bi = b[i], ri = bi - r[i];
     r[i] = ri;
-    v[0] += ri * ri;
-    v[1] += bi * bi;
+    v[0][0] += ri * ri;
+    v[1][0] += bi * bi;
   }
-  if (const double* tot = mgrid_sum<2>(v, R, partials, &S->counter[3]))
+  if (const double* tot = mgrid_sum<2, 1>(v, R, partials, &S->counter[3]))
     for (int k = 0; k < R; ++k) {
       S->rr[k] = tot[k];
       S->bb[k] = tot[kMaxRhs + k];
@@ -306,9 +400,9 @@ __global__ void __launch_bounds__(kMThreads)
 __global__ void __launch_bounds__(kMThreads)
     k_m_d2f(int64_t n, int R, const double* __restrict__ r, const double* __restrict__ inv, float* __restrict__ rf,
             float* __restrict__ c) {
-  M_THREAD(R);
+  M_THREAD(R, 1);
   const double s = inv[K_COL];
-  M_LOOP(i, n, R) {
+  M_LOOP(i, n, R, 1) {
     rf[i] = (float)(r[i] * s);
     c[i] = 0.0f;
   }
@@ -316,16 +410,24 @@ __global__ void __launch_bounds__(kMThreads)
 // x += |r_k| c per column
 __global__ void __launch_bounds__(kMThreads)
     k_m_axpy(int64_t n, int R, const float* __restrict__ c, const double* __restrict__ scale, double* __restrict__ x) {
-  M_THREAD(R);
+  M_THREAD(R, 1);
   const double s = scale[K_COL];
-  M_LOOP(i, n, R) x[i] += s * (double)c[i];
+  M_LOOP(i, n, R, 1) x[i] += s * (double)c[i];
 }
 
-static inline unsigned mgrid(int64_t n, int R) {
-  // the grid stride (blocks x threads) is a multiple of 32 >= R: one rhs per thread
-  const int64_t b = (n * R + kMThreads - 1) / kMThreads;
+static inline unsigned mgrid(int64_t n, int R, int W = 1) {
+  // the grid stride (W x blocks x threads) is a multiple of R: fixed columns per thread
+  const int64_t b = (n * R / W + kMThreads - 1) / kMThreads;
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, kMBlocks));
 }
+// launch kernel<T, W> with W = 4 (128-bit accesses) when R >= 4
+#define M_LAUNCH(kern, ...)                                                    \
+  do {                                                                        \
+    if (R >= 4)                                                               \
+      kern<T, 4><<<mgrid(n, R, 4), kMThreads, 0, s>>>(__VA_ARGS__);           \
+    else                                                                      \
+      kern<T, 1><<<mgrid(n, R, 1), kMThreads, 0, s>>>(__VA_ARGS__);           \
+  } while (0)
 
 // Y = J X for R right-hand sides (masked): tets batch the element matrices,
 // hex grids apply column by column
@@ -408,7 +510,7 @@ static hc_status mpcg_run(hcop* h, int R, double rtol, double atol, int maxit, c
   auto precond = [&](int first) -> hc_status {
     if (!aux) return HC_OK;
     HC_CUDA_TRY(h, tetaux_apply<T>(h, R, r, z, dinv, all_done, s));
-    k_m_rz<T><<<mgrid(n, R), kMThreads, 0, s>>>(n, R, r, z, first, w->S, w->partials);
+    M_LAUNCH(k_m_rz, n, R, r, z, first, w->S, w->partials);
     return HC_OK;
   };
   MScalars* hs = w->hS;
@@ -419,11 +521,11 @@ static hc_status mpcg_run(hcop* h, int R, double rtol, double atol, int maxit, c
   HC_CUDA_TRY(h, cudaMemcpyAsync(w->S, hs, sizeof(MScalars), cudaMemcpyHostToDevice, s));
   const unsigned g = mgrid(n, R);
   HC_CUDA_TRY(h, multi_apply<T>(h, R, X, q, s));
-  k_m_setup<T><<<g, kMThreads, 0, s>>>(n, R, B, q, r, dinv, w->S, w->partials);
+  M_LAUNCH(k_m_setup, n, R, B, q, r, dinv, w->S, w->partials);
   HC_CUDA_TRY(h, cudaMemsetAsync(p, 0, n * R * sizeof(T), s));
   hc_status pst = precond(1);
   if (pst != HC_OK) return pst;
-  k_m_dir<T><<<g, kMThreads, 0, s>>>(n, R, r, z, dinv, p, q, h->ess, w->S);
+  M_LAUNCH(k_m_dir, n, R, r, z, dinv, p, q, h->ess, w->S);
   HC_CUDA_TRY(h, cudaGetLastError());
   const int chunk = 25;
   for (int launched = 0;;) {
@@ -431,11 +533,11 @@ static hc_status mpcg_run(hcop* h, int R, double rtol, double atol, int maxit, c
       // q holds (I-P) p; the apply adds P K P p
       HC_CUDA_TRY(h, tet_apply_launch<T>(h, sizeof(T) == 8 ? (const T*)h->tetK64 : (const T*)h->tetK32, p, q, R,
                                          true, 1.0, &w->S->all_done, s));
-      k_m_alpha<T><<<g, kMThreads, 0, s>>>(n, R, p, q, w->S, w->partials);
-      k_m_update<T><<<g, kMThreads, 0, s>>>(n, R, X, r, p, q, dinv, aux ? 0 : 1, w->S, w->partials);
+      M_LAUNCH(k_m_alpha, n, R, p, q, w->S, w->partials);
+      M_LAUNCH(k_m_update, n, R, X, r, p, q, dinv, aux ? 0 : 1, w->S, w->partials);
       pst = precond(0);
       if (pst != HC_OK) return pst;
-      k_m_dir<T><<<g, kMThreads, 0, s>>>(n, R, r, z, dinv, p, q, h->ess, w->S);
+      M_LAUNCH(k_m_dir, n, R, r, z, dinv, p, q, h->ess, w->S);
     }
     HC_CUDA_TRY(h, cudaGetLastError());
     HC_CUDA_TRY(h, cudaMemcpyAsync(hs, w->S, sizeof(MScalars), cudaMemcpyDeviceToHost, s));
@@ -588,6 +690,10 @@ extern "C" hc_status hc_solve_multi_device(hcop_t* h, const hc_solve_params* prm
   }
   if (prm->precision != HC_FP64 && prm->precision != HC_MIXED) {
     h->err = "precision must be HC_FP64 or HC_MIXED";
+    return HC_EINVAL;
+  }
+  if ((reinterpret_cast<uintptr_t>(B) | reinterpret_cast<uintptr_t>(X)) % 16 != 0) {
+    h->err = "hc_solve_multi_device: B and X must be 16-byte aligned";  // 128-bit vector accesses
     return HC_EINVAL;
   }
   if (prm->precond != HC_PRECOND_JACOBI && prm->precond != HC_PRECOND_AUX) {

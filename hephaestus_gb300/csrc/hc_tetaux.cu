@@ -46,7 +46,7 @@ namespace hc {
 
 namespace {
 constexpr int kTaMaxLevels = 10;
-constexpr int kTaCoarse = 600;
+constexpr int kTaCoarse = 1500;
 constexpr int kTaDenseMax = 1500;
 constexpr double kTaTheta = 0.08;
 constexpr double kTaRatio = 30.0;

@@ -223,7 +223,8 @@ hc_status hc_tet_gradient_device(hcop_t* h, const double* u, double* y);
  * HC_PRECOND_AUX: Jacobi plus the gradient-space correction (PG) V (PG)^T
  * with V one V-cycle of a smoothed-aggregation AMG on the P1 nodal operator
  * (PG)^T J (PG), applied to all columns at once (hc_solve / hc_solve_device
- * with HC_PRECOND_AUX on a tet mesh run this with nrhs = 1).  Replaces R
+ * with HC_PRECOND_AUX on a tet mesh run this with nrhs = 1).  B and X must
+ * be 16-byte aligned (cudaMalloc and PyTorch allocations are).  Replaces R
  * separate HyprePCG solves of the same operator
  * (hcurl_formulation.cpp:81-85, problem_builder_base.cpp:221-253).        */
 hc_status hc_solve_multi_device(hcop_t* h, const hc_solve_params* prm, int32_t nrhs, const double* B, double* X,
