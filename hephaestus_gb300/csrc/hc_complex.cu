@@ -122,6 +122,9 @@ __global__ void k_cinv_diag(int64_t n, const uint8_t* __restrict__ ess, const do
 }
 
 // ---- COCG kernels ---------------------------------------------------------------------
+// The bilinear dots r^T z of COCG are not positive and can cancel, so their
+// products and sums stay in FP64 even for FP32 vectors (the real PCG kernels,
+// whose dots are positive, sum in the vectors' precision per thread).
 // r = b - Ax (q holds Ax); z = D^-1 r; p = z; rho = r^T z; rr = |r|^2; bb = |b|^2
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads)
@@ -130,26 +133,20 @@ __global__ void __launch_bounds__(kRedThreads)
   // active (may be null): 0 skips the launch (a stopped refinement loop);
   // qr == nullptr: x = 0, r = b
   if (active && !*active) return;
-  // per-thread sums in T: FP32 vectors do no per-element FP64 work (GB300's FP64 rate is low)
   double v[4] = {0, 0, 0, 0}, tot[4];
-  T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
   GS_LOOP(k, n) {
-    const T a = qr ? br[k] - qr[k] : br[k];
-    const T b = qr ? bi[k] - qi[k] : bi[k];
-    rr_[k] = a;
-    ri_[k] = b;
-    const T zr = a * dr[k] - b * di[k], zi = a * di[k] + b * dr[k];
-    pr[k] = zr;
-    pi[k] = zi;
-    s0 += a * zr - b * zi;
-    s1 += a * zi + b * zr;
-    s2 += a * a + b * b;
-    s3 += br[k] * br[k] + bi[k] * bi[k];
+    const double a = qr ? (double)br[k] - (double)qr[k] : (double)br[k];
+    const double b = qr ? (double)bi[k] - (double)qi[k] : (double)bi[k];
+    rr_[k] = (T)a;
+    ri_[k] = (T)b;
+    const double zr = a * (double)dr[k] - b * (double)di[k], zi = a * (double)di[k] + b * (double)dr[k];
+    pr[k] = (T)zr;
+    pi[k] = (T)zi;
+    v[0] += a * zr - b * zi;
+    v[1] += a * zi + b * zr;
+    v[2] += a * a + b * b;
+    v[3] += (double)br[k] * (double)br[k] + (double)bi[k] * (double)bi[k];
   }
-  v[0] = (double)s0;
-  v[1] = (double)s1;
-  v[2] = (double)s2;
-  v[3] = (double)s3;
   block_sum_n<4>(v);
   if (grid_sum_n<4>(v, partials, &S->counter[0], tot)) {
     S->rho_r = tot[0];
@@ -176,14 +173,11 @@ __global__ void __launch_bounds__(kRedThreads)
     k_c_alpha(int64_t n, const T* pr, const T* pi, const T* qr, const T* qi, CScalars* S, double* partials) {
   if (S->done) return;
   double v[2] = {0, 0}, tot[2];
-  T s0 = T(0), s1 = T(0);  // per-thread sums in T
   GS_LOOP(k, n) {
-    const T a = pr[k], b = pi[k], c = qr[k], d = qi[k];
-    s0 += a * c - b * d;
-    s1 += a * d + b * c;
+    const double a = pr[k], b = pi[k], c = qr[k], d = qi[k];
+    v[0] += a * c - b * d;
+    v[1] += a * d + b * c;
   }
-  v[0] = (double)s0;
-  v[1] = (double)s1;
   block_sum_n<2>(v);
   if (grid_sum_n<2>(v, partials, &S->counter[1], tot)) {
     const double den = tot[0] * tot[0] + tot[1] * tot[1];
@@ -207,7 +201,6 @@ __global__ void __launch_bounds__(kRedThreads)
   if (S->done) return;
   const T ar = (T)S->alpha_r, ai = (T)S->alpha_i;
   double v[3] = {0, 0, 0}, tot[3];
-  T s0 = T(0), s1 = T(0), s2 = T(0);  // per-thread sums in T
   GS_LOOP(k, n) {
     const T p_r = pr[k], p_i = pi[k];
     xr[k] += ar * p_r - ai * p_i;
@@ -216,14 +209,12 @@ __global__ void __launch_bounds__(kRedThreads)
     const T a = rr_[k] - (ar * q_r - ai * q_i), b = ri_[k] - (ar * q_i + ai * q_r);
     rr_[k] = a;
     ri_[k] = b;
-    const T zr = a * dr[k] - b * di[k], zi = a * di[k] + b * dr[k];
-    s0 += a * zr - b * zi;
-    s1 += a * zi + b * zr;
-    s2 += a * a + b * b;
+    const double da = a, db = b, zr = da * (double)dr[k] - db * (double)di[k],
+                 zi = da * (double)di[k] + db * (double)dr[k];
+    v[0] += da * zr - db * zi;
+    v[1] += da * zi + db * zr;
+    v[2] += da * da + db * db;
   }
-  v[0] = (double)s0;
-  v[1] = (double)s1;
-  v[2] = (double)s2;
   block_sum_n<3>(v);
   if (grid_sum_n<3>(v, partials, &S->counter[2], tot)) {
     S->it += 1;
@@ -271,17 +262,14 @@ __global__ void __launch_bounds__(kRedThreads)
                double* partials, const int* active) {
   if (active && !*active) return;
   double v[2] = {0, 0}, tot[2];
-  T s0 = T(0), s1 = T(0);  // per-thread sums in T
   GS_LOOP(k, n) {
-    const T a = qr ? br[k] - qr[k] : br[k];
-    const T b = qr ? bi[k] - qi[k] : bi[k];
-    rr_[k] = a;
-    ri_[k] = b;
-    s0 += a * a + b * b;
-    s1 += br[k] * br[k] + bi[k] * bi[k];
+    const double a = qr ? (double)br[k] - (double)qr[k] : (double)br[k];
+    const double b = qr ? (double)bi[k] - (double)qi[k] : (double)bi[k];
+    rr_[k] = (T)a;
+    ri_[k] = (T)b;
+    v[0] += a * a + b * b;
+    v[1] += (double)br[k] * (double)br[k] + (double)bi[k] * (double)bi[k];
   }
-  v[0] = (double)s0;
-  v[1] = (double)s1;
   block_sum_n<2>(v);
   if (grid_sum_n<2>(v, partials, &S->counter[0], tot)) {
     S->rr = tot[0];
@@ -308,7 +296,6 @@ __global__ void __launch_bounds__(kRedThreads)
   if (S->done) return;
   const T ar = (T)S->alpha_r, ai = (T)S->alpha_i;
   double v[1] = {0}, tot[1];
-  T s0 = T(0);  // per-thread sum in T
   GS_LOOP(k, n) {
     const T p_r = pr[k], p_i = pi[k];
     xr[k] += ar * p_r - ai * p_i;
@@ -317,9 +304,8 @@ __global__ void __launch_bounds__(kRedThreads)
     const T a = rr_[k] - (ar * q_r - ai * q_i), b = ri_[k] - (ar * q_i + ai * q_r);
     rr_[k] = a;
     ri_[k] = b;
-    s0 += a * a + b * b;
+    v[0] += (double)a * (double)a + (double)b * (double)b;
   }
-  v[0] = (double)s0;
   block_sum_n<1>(v);
   if (grid_sum_n<1>(v, partials, &S->counter[2], tot)) {
     S->it += 1;
@@ -356,14 +342,11 @@ __global__ void __launch_bounds__(kRedThreads)
              double* partials) {
   if (S->done) return;
   double v[2] = {0, 0}, tot[2];
-  T s0 = T(0), s1 = T(0);  // per-thread sums in T
   GS_LOOP(k, n) {
-    const T a = rr_[k], b = ri_[k], c = zr[k], d = zi[k];
-    s0 += a * c - b * d;
-    s1 += a * d + b * c;
+    const double a = rr_[k], b = ri_[k], c = zr[k], d = zi[k];
+    v[0] += a * c - b * d;
+    v[1] += a * d + b * c;
   }
-  v[0] = (double)s0;
-  v[1] = (double)s1;
   block_sum_n<2>(v);
   if (grid_sum_n<2>(v, partials, &S->counter[4], tot)) {
     if (first) {
