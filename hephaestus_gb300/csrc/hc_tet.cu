@@ -429,6 +429,119 @@ __global__ void __launch_bounds__(256) tet_apply_lanes64(int64_t ne, const int32
   }
 }
 
+// Order 2, FP32 vectors, R in {4, 8, 16, 32}: register-tiled form.  32 / R
+// elements per warp; lane (row group g < 4, column group c < R/4) of an
+// element computes the 5 x 4 output tile Y[5g .. 5g+4][4c .. 4c+3]: per
+// 4-column chunk of the element matrix it reads 5 K quads (128-bit, shared by
+// the lanes of its row group) and 4 X quads of the staged block (128-bit
+// shared-memory reads), 80 FMAs; outputs leave as 5 128-bit atomic adds.
+// Shared-memory reads per element drop from 20 x L x R / 4 (one row per lane)
+// to 5 x L x R / 4 quads.
+template <int R, typename TK>
+__global__ void __launch_bounds__(256, 4) tet_apply_tiles20(int64_t ne, const int32_t* __restrict__ edofs,
+                                                         const TK* __restrict__ K, const uint8_t* __restrict__ ess,
+                                                         int masked, float scale, const float* __restrict__ x,
+                                                         float* __restrict__ y, const int* done) {
+  if (done && *done) return;
+  constexpr int L = 20, W = 8, EPW = 32 / R, CG = R / 4;
+  __shared__ __align__(16) float xs_all[W][EPW][L * R];
+  __shared__ int sdof_all[W][EPW][L];
+  __shared__ unsigned char sess_all[W][EPW][L];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane / R, t = lane % R, g = t / CG, c = t % CG;
+  float* xs = xs_all[wid][sub];
+  int* sdof = sdof_all[wid][sub];
+  unsigned char* sess = sess_all[wid][sub];
+  const int64_t wstride = (int64_t)gridDim.x * W * EPW;
+  for (int64_t e0 = ((int64_t)blockIdx.x * W + wid) * EPW; e0 < ne; e0 += wstride) {
+    const int64_t e = e0 + sub;
+    const bool live = e < ne;
+    if (live)
+      for (int j = t; j < L; j += R) {
+        const int d = __ldg(edofs + e * L + j);
+        sdof[j] = d;
+        sess[j] = (masked && ess[d]) ? 1 : 0;
+      }
+    __syncwarp();
+    if (live)
+      for (int q = t; q < L * CG; q += R) {
+        const int j = q / CG, c4 = q - j * CG;
+        float4 v = __ldg(reinterpret_cast<const float4*>(x + (int64_t)sdof[j] * R) + c4);
+        if (sess[j]) v = make_float4(0.f, 0.f, 0.f, 0.f);
+        *reinterpret_cast<float4*>(xs + j * R + 4 * c4) = v;
+      }
+    __syncwarp();
+    if (live) {
+      float acc[5][4];
+#pragma unroll
+      for (int i = 0; i < 5; ++i)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[i][k] = 0.f;
+      const TK* Kg = K + (e * L + 5 * g) * L;
+#pragma unroll
+      for (int j0 = 0; j0 < L; j0 += 4) {
+        float kq[5][4];
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+          if constexpr (sizeof(TK) == 2) {
+            const uint2 v = __ldg(reinterpret_cast<const uint2*>(Kg + i * L + j0));
+            const float2 fa = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v.x));
+            const float2 fb = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v.y));
+            kq[i][0] = fa.x;
+            kq[i][1] = fa.y;
+            kq[i][2] = fb.x;
+            kq[i][3] = fb.y;
+          } else {
+            const float4 v = __ldg(reinterpret_cast<const float4*>(Kg + i * L + j0));
+            kq[i][0] = v.x;
+            kq[i][1] = v.y;
+            kq[i][2] = v.z;
+            kq[i][3] = v.w;
+          }
+        }
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+          const float4 xv = *reinterpret_cast<const float4*>(xs + (j0 + jj) * R + 4 * c);
+#pragma unroll
+          for (int i = 0; i < 5; ++i) {
+            acc[i][0] += kq[i][jj] * xv.x;
+            acc[i][1] += kq[i][jj] * xv.y;
+            acc[i][2] += kq[i][jj] * xv.z;
+            acc[i][3] += kq[i][jj] * xv.w;
+          }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 5; ++i) {
+        const int row = 5 * g + i;
+        if (sess[row]) continue;
+        atomicAdd(reinterpret_cast<float4*>(y + (int64_t)sdof[row] * R) + c,
+                  make_float4(scale * acc[i][0], scale * acc[i][1], scale * acc[i][2], scale * acc[i][3]));
+      }
+    }
+    __syncwarp();  // the staged block is rewritten for the next elements
+  }
+}
+
+template <typename TK>
+static bool tet_tiles20_launch(const hcop* h, const TK* K, const float* x, float* y, int nrhs, bool masked,
+                               float scale, const int* done, cudaStream_t s) {
+  // 128-bit accesses: x, y 16-byte aligned (rows of R >= 4 floats keep the alignment)
+  if (h->p != 2 || ((uintptr_t)x | (uintptr_t)y) % 16 != 0) return false;
+  const int m = masked ? 1 : 0;
+  auto blocks = [&](int epw) {
+    const int64_t b = (h->ne + 8 * epw - 1) / (8 * epw);
+    return (unsigned)std::min<int64_t>(b, 152 * 16);
+  };
+  switch (nrhs) {
+    case 4: tet_apply_tiles20<4, TK><<<blocks(8), 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess, m, scale, x, y, done); return true;
+    case 8: tet_apply_tiles20<8, TK><<<blocks(4), 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess, m, scale, x, y, done); return true;
+    case 16: tet_apply_tiles20<16, TK><<<blocks(2), 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess, m, scale, x, y, done); return true;
+    case 32: tet_apply_tiles20<32, TK><<<blocks(1), 256, 0, s>>>(h->ne, h->tet_edofs, K, h->ess, m, scale, x, y, done); return true;
+    default: return false;
+  }
+}
+
 template <typename T, int L, typename TK>
 static cudaError_t tet_rows_launch(const hcop* h, const TK* K, const T* x, T* y, int nrhs, bool masked, T scale,
                                    const int* done, cudaStream_t s) {
@@ -469,6 +582,7 @@ cudaError_t tet_apply_launch(const hcop* h, const T* K, const T* x, T* y, int nr
     return cudaGetLastError();
   } else {
     if (h->p == 1) return tet_rows_launch<T, 6, T>(h, K, x, y, nrhs, masked, (T)scale, done, s);
+    if (tet_tiles20_launch<float>(h, K, x, y, nrhs, masked, (float)scale, done, s)) return cudaGetLastError();
     return tet_rows_launch<T, 20, T>(h, K, x, y, nrhs, masked, (T)scale, done, s);
   }
 }
@@ -481,6 +595,7 @@ template cudaError_t tet_apply_launch<float>(const hcop*, const float*, const fl
 cudaError_t tet_apply_launch_bf16(const hcop* h, const float* x, float* y, int nrhs, bool masked, cudaStream_t s) {
   const __nv_bfloat16* K = static_cast<const __nv_bfloat16*>(h->tetK16);
   if (h->p == 1) return tet_rows_launch<float, 6, __nv_bfloat16>(h, K, x, y, nrhs, masked, 1.0f, nullptr, s);
+  if (tet_tiles20_launch<__nv_bfloat16>(h, K, x, y, nrhs, masked, 1.0f, nullptr, s)) return cudaGetLastError();
   return tet_rows_launch<float, 20, __nv_bfloat16>(h, K, x, y, nrhs, masked, 1.0f, nullptr, s);
 }
 

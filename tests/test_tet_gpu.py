@@ -53,12 +53,12 @@ def test_tet_apply_parity(p):
     assert np.abs(d - ref.diag_masked()).max() < 1e-12 * np.abs(d).max()
 
 
-@pytest.mark.parametrize("prec", ["float64", "float32"])
-def test_tet_multi_rhs_parity(prec):
+@pytest.mark.parametrize("prec,nrhs", [("float64", 16), ("float32", 16), ("float32", 4), ("float32", 8),
+                                       ("float32", 32), ("float32", 2)])
+def test_tet_multi_rhs_parity(prec, nrhs):
     import torch
 
     op, ref, rng = _pair(4, 2)
-    nrhs = 16
     X = rng.standard_normal((op.ndof, nrhs))
     Xd = torch.tensor(X, dtype=getattr(torch, prec), device="cuda")
     Yd = torch.empty_like(Xd)
