@@ -429,49 +429,105 @@ __global__ void __launch_bounds__(256) tet_apply_lanes64(int64_t ne, const int32
   }
 }
 
-// Order 2, FP32 vectors, R in {4, 8, 16, 32}: register-tiled form.  32 / R
-// elements per warp; lane (row group g < 4, column group c < R/4) of an
-// element computes the 5 x 4 output tile Y[5g .. 5g+4][4c .. 4c+3]: per
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(a), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(a), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit_wait() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+// Order 2, FP32 vectors, R in {4, 8, 16, 32}: register-tiled, software-pipelined
+// form.  32 / R elements per warp; lane (row group g < 4, column group c < R/4)
+// of an element computes the 5 x 4 output tile Y[5g .. 5g+4][4c .. 4c+3]: per
 // 4-column chunk of the element matrix it reads 5 K quads (128-bit, shared by
 // the lanes of its row group) and 4 X quads of the staged block (128-bit
 // shared-memory reads), 80 FMAs; outputs leave as 5 128-bit atomic adds.
-// Shared-memory reads per element drop from 20 x L x R / 4 (one row per lane)
-// to 5 x L x R / 4 quads.
+// Pipeline (per warp, element groups i = 0, 1, ...): before group i computes,
+// cp.async copies the X rows of group i + 1 (dofs already in shared memory)
+// into the other X buffer and the dof indices of group i + 2 into the third
+// dof slot; they land while group i computes and adds.  Rows of essential dofs
+// are zeroed after the copies complete.
 template <int R, typename TK>
-__global__ void __launch_bounds__(256, 4) tet_apply_tiles20(int64_t ne, const int32_t* __restrict__ edofs,
-                                                         const TK* __restrict__ K, const uint8_t* __restrict__ ess,
-                                                         int masked, float scale, const float* __restrict__ x,
-                                                         float* __restrict__ y, const int* done) {
+__global__ void __launch_bounds__(256, 3) tet_apply_tiles20(int64_t ne, const int32_t* __restrict__ edofs,
+                                                            const TK* __restrict__ K, const uint8_t* __restrict__ ess,
+                                                            int masked, float scale, const float* __restrict__ x,
+                                                            float* __restrict__ y, const int* done) {
   if (done && *done) return;
   constexpr int L = 20, W = 8, EPW = 32 / R, CG = R / 4;
-  __shared__ __align__(16) float xs_all[W][EPW][L * R];
-  __shared__ int sdof_all[W][EPW][L];
-  __shared__ unsigned char sess_all[W][EPW][L];
+  constexpr int ND = (L + R - 1) / R;  // dof indices a lane copies per element
+  constexpr int NX = L * CG / R;       // X quads a lane copies per element (= 5)
+  static_assert(NX * R == L * CG, "X quads split evenly over the element's lanes");
+  __shared__ __align__(16) float xs_all[W][2][EPW][L * R];
+  __shared__ __align__(16) int sdof_all[W][3][EPW][L];
+  __shared__ unsigned char sess_all[W][3][EPW][L];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int sub = lane / R, t = lane % R, g = t / CG, c = t % CG;
-  float* xs = xs_all[wid][sub];
-  int* sdof = sdof_all[wid][sub];
-  unsigned char* sess = sess_all[wid][sub];
   const int64_t wstride = (int64_t)gridDim.x * W * EPW;
-  for (int64_t e0 = ((int64_t)blockIdx.x * W + wid) * EPW; e0 < ne; e0 += wstride) {
+  const int64_t first = ((int64_t)blockIdx.x * W + wid) * EPW;
+  if (first >= ne) return;  // uniform over the warp: no shared state with other warps
+
+  auto copy_dofs = [&](int64_t e, int ds) {  // async: dof indices of element e -> slot ds
+    if (e >= ne) return;
+#pragma unroll
+    for (int k = 0; k < ND; ++k) {
+      const int j = t + k * R;
+      if (j < L) cp_async4(&sdof_all[wid][ds][sub][j], edofs + e * L + j);
+    }
+  };
+  auto copy_x = [&](int64_t e, int ds, int xb) {  // async: X rows of element e (dofs in slot ds) -> buffer xb
+    if (e >= ne) return;
+#pragma unroll
+    for (int k = 0; k < NX; ++k) {
+      const int q = t + k * R, j = q / CG, c4 = q - j * CG;
+      cp_async16(&xs_all[wid][xb][sub][j * R + 4 * c4],
+                 x + (int64_t)sdof_all[wid][ds][sub][j] * R + 4 * c4);
+    }
+  };
+  auto ess_flags = [&](int64_t e, int ds, unsigned char (&er)[NX]) {
+#pragma unroll
+    for (int k = 0; k < NX; ++k) {
+      const int j = (t + k * R) / CG;
+      er[k] = (e < ne && masked) ? ess[sdof_all[wid][ds][sub][j]] : 0;
+    }
+  };
+  auto mask_rows = [&](int64_t e, int ds, int xb, const unsigned char (&er)[NX]) {  // after the copies landed
+    if (e >= ne) return;
+#pragma unroll
+    for (int k = 0; k < NX; ++k) {
+      const int q = t + k * R, j = q / CG, c4 = q - j * CG;
+      if (er[k]) *reinterpret_cast<float4*>(&xs_all[wid][xb][sub][j * R + 4 * c4]) = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (c4 == 0) sess_all[wid][ds][sub][j] = er[k];
+    }
+  };
+
+  // prologue: dofs of groups 0 and 1, X of group 0
+  copy_dofs(first + sub, 0);
+  copy_dofs(first + wstride + sub, 1);
+  cp_async_commit_wait();
+  __syncwarp();
+  {
+    unsigned char er[NX];
+    ess_flags(first + sub, 0, er);
+    copy_x(first + sub, 0, 0);
+    cp_async_commit_wait();
+    mask_rows(first + sub, 0, 0, er);
+    __syncwarp();
+  }
+  int it = 0;
+  for (int64_t e0 = first; e0 < ne; e0 += wstride, ++it) {
+    const int d0 = it % 3, d1 = (it + 1) % 3, d2 = (it + 2) % 3, xb = it & 1;
     const int64_t e = e0 + sub;
-    const bool live = e < ne;
-    if (live)
-      for (int j = t; j < L; j += R) {
-        const int d = __ldg(edofs + e * L + j);
-        sdof[j] = d;
-        sess[j] = (masked && ess[d]) ? 1 : 0;
-      }
-    __syncwarp();
-    if (live)
-      for (int q = t; q < L * CG; q += R) {
-        const int j = q / CG, c4 = q - j * CG;
-        float4 v = __ldg(reinterpret_cast<const float4*>(x + (int64_t)sdof[j] * R) + c4);
-        if (sess[j]) v = make_float4(0.f, 0.f, 0.f, 0.f);
-        *reinterpret_cast<float4*>(xs + j * R + 4 * c4) = v;
-      }
-    __syncwarp();
-    if (live) {
+    // in flight during the compute: X of group it + 1, dofs of group it + 2
+    copy_x(e + wstride, d1, xb ^ 1);
+    copy_dofs(e + 2 * wstride, d2);
+    if (e < ne) {
+      const float* xs = xs_all[wid][xb][sub];
       float acc[5][4];
 #pragma unroll
       for (int i = 0; i < 5; ++i)
@@ -514,12 +570,16 @@ __global__ void __launch_bounds__(256, 4) tet_apply_tiles20(int64_t ne, const in
 #pragma unroll
       for (int i = 0; i < 5; ++i) {
         const int row = 5 * g + i;
-        if (sess[row]) continue;
-        atomicAdd(reinterpret_cast<float4*>(y + (int64_t)sdof[row] * R) + c,
+        if (sess_all[wid][d0][sub][row]) continue;
+        atomicAdd(reinterpret_cast<float4*>(y + (int64_t)sdof_all[wid][d0][sub][row] * R) + c,
                   make_float4(scale * acc[i][0], scale * acc[i][1], scale * acc[i][2], scale * acc[i][3]));
       }
     }
-    __syncwarp();  // the staged block is rewritten for the next elements
+    unsigned char en[NX];
+    ess_flags(e + wstride, d1, en);  // reads only the next group's dof slot
+    cp_async_commit_wait();
+    mask_rows(e + wstride, d1, xb ^ 1, en);
+    __syncwarp();  // next group's X, flags and dofs visible to the warp; buffers of this group free
   }
 }
 
