@@ -114,3 +114,28 @@ def test_tet_descriptor_validation():
         h = C.c_void_p()
         assert L.hc_create(C.byref(d), C.byref(h)) == N.HC_EINVAL
         assert msg in N.last_error(None)
+
+
+def test_block_solve_and_gradient_entries_reject_null_arguments():
+    """The multi-RHS solve, the discrete gradient and the AMG level query
+    reject missing handles or arrays before any device work."""
+    L = N.lib()
+    p = N.SolveParams()
+    info = (N.SolveInfo * 16)()
+    assert L.hc_solve_multi_device(None, C.byref(p), 16, None, None, info) == N.HC_EINVAL
+    assert L.hc_tet_gradient_device(None, None, None) == N.HC_EINVAL
+    sizes = np.zeros(8, dtype=np.int64)
+    assert L.hc_aux_levels(None, sizes.ctypes.data_as(C.c_void_p), 8) == 0
+    assert L.hc_load_coil_device(None, None, 4, None) == N.HC_EINVAL
+
+
+def test_solver_option_names_map_to_the_abi():
+    """GpuHCurlPCGSolver reads the reference's option names plus the build's
+    precision/preconditioner options into hc_solve_params."""
+    from hephaestus_gb300 import GpuHCurlPCGSolver
+
+    s = GpuHCurlPCGSolver({"Tolerance": 1e-10, "AbsTolerance": 0.0, "MaxIter": 123, "Precision": "mixed",
+                           "Preconditioner": "aux", "InnerTolerance": 0.1, "MaxOuter": 7})
+    assert s.p.rtol == 1e-10 and s.p.atol == 0.0 and s.p.maxit == 123
+    assert s.p.precision == N.HC_MIXED and s.p.precond == N.HC_PRECOND_AUX
+    assert s.p.inner_rtol == 0.1 and s.p.max_outer == 7
