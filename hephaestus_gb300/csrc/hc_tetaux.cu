@@ -40,6 +40,7 @@
 #include <numeric>
 #include <vector>
 
+#include "hc_amg_host.h"
 #include "hc_internal.h"
 
 namespace hc {
@@ -89,11 +90,6 @@ __host__ __device__ inline float ta_bubble(int I, int ke, const int (*E)[2], con
   return 0.f;
 }
 
-struct HCsr {
-  int n = 0, m = 0;
-  std::vector<int> rp, ci;
-  std::vector<double> va;
-};
 struct DCsr {
   const int* rp = nullptr;
   const int* ci = nullptr;
@@ -465,214 +461,8 @@ __global__ void __launch_bounds__(kTaThreads)
   }
 }
 
-// ---- host AMG setup -----------------------------------------------------------------
-namespace {
-
-int aggregate(const HCsr& A, const std::vector<double>& dg, std::vector<int>& agg) {
-  const int n = A.n;
-  auto strong = [&](int i, int k) {
-    const int j = A.ci[k];
-    return j != i && std::fabs(A.va[k]) > kTaTheta * std::sqrt(std::fabs(dg[i] * dg[j]));
-  };
-  agg.assign(n, -1);
-  int na = 0;
-  for (int i = 0; i < n; ++i) {
-    if (agg[i] != -1) continue;
-    bool ok = true;
-    for (int k = A.rp[i]; k < A.rp[i + 1] && ok; ++k)
-      if (strong(i, k) && agg[A.ci[k]] != -1) ok = false;
-    if (!ok) continue;
-    agg[i] = na;
-    for (int k = A.rp[i]; k < A.rp[i + 1]; ++k)
-      if (strong(i, k)) agg[A.ci[k]] = na;
-    ++na;
-  }
-  const std::vector<int> a1 = agg;
-  for (int i = 0; i < n; ++i) {
-    if (a1[i] != -1) continue;
-    int best = -1;
-    double bs = 0.0;
-    for (int k = A.rp[i]; k < A.rp[i + 1]; ++k)
-      if (strong(i, k) && a1[A.ci[k]] >= 0 && std::fabs(A.va[k]) > bs) {
-        bs = std::fabs(A.va[k]);
-        best = a1[A.ci[k]];
-      }
-    if (best >= 0) agg[i] = best;
-  }
-  for (int i = 0; i < n; ++i) {
-    if (agg[i] != -1) continue;
-    agg[i] = na;
-    for (int k = A.rp[i]; k < A.rp[i + 1]; ++k)
-      if (strong(i, k) && agg[A.ci[k]] == -1) agg[A.ci[k]] = na;
-    ++na;
-  }
-  return na;
-}
-
-std::vector<double> diagonal(const HCsr& A) {
-  std::vector<double> d(A.n, 0.0);
-  for (int i = 0; i < A.n; ++i)
-    for (int k = A.rp[i]; k < A.rp[i + 1]; ++k)
-      if (A.ci[k] == i) d[i] = A.va[k];
-  return d;
-}
-
-// largest eigenvalue of D^-1 A (power iteration on D^-1/2 A D^-1/2)
-double lmax_scaled(const HCsr& A, const std::vector<double>& dg) {
-  const int n = A.n;
-  std::vector<double> s(n), x(n), y(n);
-  for (int i = 0; i < n; ++i) {
-    s[i] = 1.0 / std::sqrt(std::fabs(dg[i]));
-    x[i] = 1.0 + 0.37 * std::sin(1.0 + 7.3 * i);  // deterministic start
-  }
-  double lam = 1.0;
-  for (int it = 0; it < 40; ++it) {
-    double nx = 0.0;
-    for (double v : x) nx += v * v;
-    nx = std::sqrt(nx);
-    for (double& v : x) v /= nx;
-    double xy = 0.0;
-    for (int i = 0; i < n; ++i) {
-      double t = 0.0;
-      for (int k = A.rp[i]; k < A.rp[i + 1]; ++k) t += A.va[k] * s[A.ci[k]] * x[A.ci[k]];
-      y[i] = s[i] * t;
-      xy += x[i] * y[i];
-    }
-    lam = xy;
-    x.swap(y);
-  }
-  return lam;
-}
-
-HCsr smooth_prolongator(const HCsr& A, const std::vector<double>& dg, const std::vector<int>& agg, int na,
-                        double omega) {
-  std::vector<int> cnt(na, 0);
-  for (int a : agg) ++cnt[a];
-  std::vector<double> pt(A.n);
-  for (int i = 0; i < A.n; ++i) pt[i] = 1.0 / std::sqrt((double)cnt[agg[i]]);
-  HCsr P;
-  P.n = A.n;
-  P.m = na;
-  P.rp.assign(1, 0);
-  std::vector<std::pair<int, double>> acc;
-  for (int i = 0; i < A.n; ++i) {
-    acc.clear();
-    auto add = [&](int col, double v) {
-      for (auto& q : acc)
-        if (q.first == col) {
-          q.second += v;
-          return;
-        }
-      acc.push_back({col, v});
-    };
-    add(agg[i], pt[i]);
-    for (int k = A.rp[i]; k < A.rp[i + 1]; ++k) add(agg[A.ci[k]], -omega / dg[i] * A.va[k] * pt[A.ci[k]]);
-    std::sort(acc.begin(), acc.end());
-    for (auto& q : acc) {
-      P.ci.push_back(q.first);
-      P.va.push_back(q.second);
-    }
-    P.rp.push_back((int)P.ci.size());
-  }
-  return P;
-}
-
-HCsr transpose(const HCsr& P) {
-  HCsr T;
-  T.n = P.m;
-  T.m = P.n;
-  T.rp.assign(P.m + 1, 0);
-  for (int c : P.ci) ++T.rp[c + 1];
-  for (int i = 0; i < P.m; ++i) T.rp[i + 1] += T.rp[i];
-  T.ci.resize(P.ci.size());
-  T.va.resize(P.va.size());
-  std::vector<int> pos(T.rp.begin(), T.rp.end() - 1);
-  for (int i = 0; i < P.n; ++i)
-    for (int k = P.rp[i]; k < P.rp[i + 1]; ++k) {
-      const int q = pos[P.ci[k]]++;
-      T.ci[q] = i;
-      T.va[q] = P.va[k];
-    }
-  return T;
-}
-
-HCsr spgemm(const HCsr& A, const HCsr& B) {
-  HCsr C;
-  C.n = A.n;
-  C.m = B.m;
-  C.rp.assign(1, 0);
-  std::vector<int> marker(B.m, -1);
-  std::vector<std::pair<int, double>> row;
-  for (int i = 0; i < A.n; ++i) {
-    row.clear();
-    for (int ka = A.rp[i]; ka < A.rp[i + 1]; ++ka) {
-      const int j = A.ci[ka];
-      const double av = A.va[ka];
-      for (int kb = B.rp[j]; kb < B.rp[j + 1]; ++kb) {
-        const int c = B.ci[kb];
-        if (marker[c] < 0) {
-          marker[c] = (int)row.size();
-          row.push_back({c, av * B.va[kb]});
-        } else {
-          row[marker[c]].second += av * B.va[kb];
-        }
-      }
-    }
-    for (auto& q : row) marker[q.first] = -1;
-    std::sort(row.begin(), row.end());
-    for (auto& q : row) {
-      C.ci.push_back(q.first);
-      C.va.push_back(q.second);
-    }
-    C.rp.push_back((int)C.ci.size());
-  }
-  return C;
-}
-
-// inverse of the SPD matrix S A S (S = diag^-1/2) by Cholesky; returns false if not positive definite
-bool dense_scaled_inverse(const HCsr& A, const std::vector<double>& dg, std::vector<float>& inv,
-                          std::vector<float>& sc) {
-  const int n = A.n;
-  std::vector<double> M((size_t)n * n, 0.0), s(n);
-  for (int i = 0; i < n; ++i) s[i] = 1.0 / std::sqrt(std::fabs(dg[i]));
-  for (int i = 0; i < n; ++i)
-    for (int k = A.rp[i]; k < A.rp[i + 1]; ++k) M[(size_t)i * n + A.ci[k]] = s[i] * A.va[k] * s[A.ci[k]];
-  // Cholesky, lower triangle in place
-  for (int j = 0; j < n; ++j) {
-    double d = M[(size_t)j * n + j];
-    for (int k = 0; k < j; ++k) d -= M[(size_t)j * n + k] * M[(size_t)j * n + k];
-    if (!(d > 1e-12)) return false;
-    d = std::sqrt(d);
-    M[(size_t)j * n + j] = d;
-    for (int i = j + 1; i < n; ++i) {
-      double v = M[(size_t)i * n + j];
-      for (int k = 0; k < j; ++k) v -= M[(size_t)i * n + k] * M[(size_t)j * n + k];
-      M[(size_t)i * n + j] = v / d;
-    }
-  }
-  // Linv (lower), then inv = Linv^T Linv
-  std::vector<double> Li((size_t)n * n, 0.0);
-  for (int j = 0; j < n; ++j) {
-    Li[(size_t)j * n + j] = 1.0 / M[(size_t)j * n + j];
-    for (int i = j + 1; i < n; ++i) {
-      double v = 0.0;
-      for (int k = j; k < i; ++k) v -= M[(size_t)i * n + k] * Li[(size_t)k * n + j];
-      Li[(size_t)i * n + j] = v / M[(size_t)i * n + i];
-    }
-  }
-  inv.assign((size_t)n * n, 0.f);
-  for (int i = 0; i < n; ++i)
-    for (int j = 0; j <= i; ++j) {
-      double v = 0.0;
-      for (int k = i; k < n; ++k) v += Li[(size_t)k * n + i] * Li[(size_t)k * n + j];
-      inv[(size_t)i * n + j] = inv[(size_t)j * n + i] = (float)v;
-    }
-  sc.resize(n);
-  for (int i = 0; i < n; ++i) sc[i] = (float)s[i];
-  return true;
-}
-
-}  // namespace
+// ---- host AMG setup: hc_amg_host.h ------------------------------------------------------
+using amg::HCsr;
 
 template <typename V>
 static cudaError_t upload(hcop* h, TetAux* X, const std::vector<V>& v, const V** out) {
@@ -921,14 +711,14 @@ hc_status tetaux_setup(hcop* h) {
   for (;;) {
     TaLevel& Lv = X->lev[nl];
     Lv.n = cur.n;
-    const std::vector<double> dg = diagonal(cur);
+    const std::vector<double> dg = amg::diagonal(cur);
     for (int i = 0; i < cur.n; ++i)
       if (!(dg[i] > 0.0)) {
         h->err = "auxiliary-space preconditioner: nodal operator has a non-positive diagonal";
         tetaux_free(h);
         return HC_ENOTSUP;
       }
-    const double lmax = 1.1 * lmax_scaled(cur, dg);
+    const double lmax = 1.1 * amg::lmax_scaled(cur, dg);
     const double lmin = lmax / kTaRatio;
     const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
     const double s1 = theta / delta, rho0 = 1.0 / s1, rho1 = 1.0 / (2.0 * s1 - rho0);
@@ -944,19 +734,19 @@ hc_status tetaux_setup(hcop* h) {
     ++nl;
     const bool last_allowed = cur.n <= kTaDenseMax;
     if (cur.n <= kTaCoarse || nl == kTaMaxLevels) {
-      if (!last_allowed || !dense_scaled_inverse(cur, dg, cinv, csc)) cinv.clear();
+      if (!last_allowed || !amg::dense_scaled_inverse(cur, dg, cinv, csc)) cinv.clear();
       break;
     }
     std::vector<int> agg;
-    const int na = aggregate(cur, dg, agg);
+    const int na = amg::aggregate(cur, dg, kTaTheta, agg);
     if (na >= (int)(0.85 * cur.n) && last_allowed) {  // coarsening stalled
-      if (!dense_scaled_inverse(cur, dg, cinv, csc)) cinv.clear();
+      if (!amg::dense_scaled_inverse(cur, dg, cinv, csc)) cinv.clear();
       break;
     }
     const double lraw = lmax / 1.1;
-    HCsr P = smooth_prolongator(cur, dg, agg, na, 4.0 / (3.0 * lraw));
-    HCsr R = transpose(P);
-    HCsr Ac = spgemm(R, spgemm(cur, P));
+    HCsr P = amg::smooth_prolongator(cur, dg, agg, na, 4.0 / (3.0 * lraw));
+    HCsr R = amg::transpose(P);
+    HCsr Ac = amg::spgemm(R, amg::spgemm(cur, P));
     if (e == cudaSuccess) e = upload_csr(h, X, P, Lv.P);
     if (e == cudaSuccess) e = upload_csr(h, X, R, Lv.R);
     cur = std::move(Ac);
