@@ -290,6 +290,8 @@ class HCurlOperator:
             prec = N.HC_BF16
         name = "float64" if prec == N.HC_FP64 else "float32"
         nrhs = 1 if X.dim() == 1 else X.shape[1]
+        if int(X.shape[0]) != self.ndof or tuple(Y.shape) != tuple(X.shape):
+            raise ValueError("X and Y must both be (ndof, nrhs) with ndof = %d" % self.ndof)
         N.check(N.lib().hc_mult_multi_device(self.h, prec, nrhs, _dev_ptr(X, name), _dev_ptr(Y, name)), self.h)
         return Y
 
@@ -425,6 +427,10 @@ class GpuHCurlPCGSolver:
         nrhs = 1 if B.dim() == 1 else int(B.shape[1])
         if tuple(X.shape) != tuple(B.shape):
             raise ValueError("B and X must have the same shape")
+        if int(B.shape[0]) != op.ndof:
+            raise ValueError("B has %d rows, the operator %d dofs" % (int(B.shape[0]), op.ndof))
+        if nrhs not in (1, 2, 4, 8, 16, 32):
+            raise ValueError("the number of right-hand sides must be 1, 2, 4, 8, 16 or 32")
         infos = (N.SolveInfo * nrhs)()
         st = N.lib().hc_solve_multi_device(op.h, C.byref(self.p), nrhs, _dev_ptr(B, "float64"),
                                            _dev_ptr(X, "float64"), infos)

@@ -139,3 +139,21 @@ def test_solver_option_names_map_to_the_abi():
     assert s.p.rtol == 1e-10 and s.p.atol == 0.0 and s.p.maxit == 123
     assert s.p.precision == N.HC_MIXED and s.p.precond == N.HC_PRECOND_AUX
     assert s.p.inner_rtol == 0.1 and s.p.max_outer == 7
+
+
+def test_block_solve_wrapper_checks_shapes_before_the_device():
+    """Shape errors are reported by the Python wrapper before any device call."""
+    torch = pytest.importorskip("torch")
+    from hephaestus_gb300 import GpuHCurlPCGSolver
+
+    class FakeOp:
+        ndof = 10
+        h = None
+
+    s = GpuHCurlPCGSolver({}, FakeOp())
+    with pytest.raises(ValueError, match="same shape"):
+        s.MultMultiDevice(torch.zeros(10, 4, dtype=torch.float64), torch.zeros(10, 2, dtype=torch.float64))
+    with pytest.raises(ValueError, match="rows"):
+        s.MultMultiDevice(torch.zeros(9, 4, dtype=torch.float64), torch.zeros(9, 4, dtype=torch.float64))
+    with pytest.raises(ValueError, match="right-hand sides"):
+        s.MultMultiDevice(torch.zeros(10, 3, dtype=torch.float64), torch.zeros(10, 3, dtype=torch.float64))
