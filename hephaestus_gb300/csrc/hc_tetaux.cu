@@ -41,6 +41,7 @@
 #include <vector>
 
 #include "hc_amg_host.h"
+#include "hc_tet_grad.h"
 #include "hc_internal.h"
 
 namespace hc {
@@ -56,40 +57,6 @@ constexpr int kTaMaxBlocks = 152 * 8;
 
 __constant__ int c_ta_edges[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
 __constant__ int c_ta_faces[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
-const int kHEdges[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
-const int kHFaces[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
-
-// local vertices (up to 3) and coefficients of local dof I in G
-__host__ __device__ inline int ta_local(int p, int I, const int (*E)[2], const int (*F)[3], int v[3], float c[3]) {
-  if (p == 1 || I < 12) {
-    const int k = p == 1 ? I : I / 2;
-    v[0] = E[k][0];
-    v[1] = E[k][1];
-    c[0] = -1.f;
-    c[1] = 1.f;
-    return 2;
-  }
-  const int f = (I - 12) / 2, s = (I - 12) % 2;
-  v[0] = F[f][0];
-  v[1] = F[f][1];
-  v[2] = F[f][2];
-  c[0] = -1.f;
-  c[1] = s == 0 ? 2.f : -1.f;
-  c[2] = s == 0 ? -1.f : 2.f;
-  return 3;
-}
-
-// coefficient of local order-2 dof I in grad of the bubble of local edge ke
-__host__ __device__ inline float ta_bubble(int I, int ke, const int (*E)[2], const int (*F)[3]) {
-  if (I < 12) return (I / 2 == ke) ? ((I % 2 == 0) ? 1.f : -1.f) : 0.f;
-  const int f = (I - 12) / 2, s = (I - 12) % 2;
-  const int i = F[f][0], j = F[f][1], k = F[f][2], a = E[ke][0], b = E[ke][1];
-  if (a == i && b == j) return s == 0 ? 1.f : -2.f;
-  if (a == i && b == k) return s == 0 ? -2.f : 1.f;
-  if (a == j && b == k) return 1.f;
-  return 0.f;
-}
-
 struct DCsr {
   const int* rp = nullptr;
   const int* ci = nullptr;
