@@ -130,6 +130,8 @@ _SIGS = {
     "hc_tet_gradient_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "hc_solve_multi_device": (C.c_int, [C.c_void_p, C.POINTER(SolveParams), C.c_int32, C.c_void_p, C.c_void_p,
                                         C.POINTER(SolveInfo)]),
+    "hc_solve_multi": (C.c_int, [C.c_void_p, C.POINTER(SolveParams), C.c_int32, C.c_void_p, C.c_void_p,
+                                 C.POINTER(SolveInfo)]),
     "hc_load_coil": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "hc_load_coil_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
 }

@@ -706,3 +706,38 @@ extern "C" hc_status hc_solve_multi_device(hcop_t* h, const hc_solve_params* prm
   }
   return multi_solve_device(h, prm, nrhs, B, X, info);
 }
+
+extern "C" hc_status hc_solve_multi(hcop_t* h, const hc_solve_params* prm, int32_t nrhs, const double* B, double* X,
+                                    hc_solve_info* info) {
+  if (!h || !prm || !B || !X || !info) return HC_EINVAL;
+  if (nrhs != 1 && nrhs != 2 && nrhs != 4 && nrhs != 8 && nrhs != 16 && nrhs != 32) {
+    h->err = "hc_solve_multi: nrhs must be 1, 2, 4, 8, 16 or 32";
+    return HC_EINVAL;
+  }
+  const size_t bytes = (size_t)h->ndof * nrhs * sizeof(double);
+  double *dB = nullptr, *dX = nullptr;
+  if (dmalloc(h, (void**)&dB, bytes) != cudaSuccess || dmalloc(h, (void**)&dX, bytes) != cudaSuccess) {
+    dfree(h, dB);
+    dfree(h, dX);
+    h->err = "hc_solve_multi: device staging allocation failed";
+    return HC_ENOMEM;
+  }
+  hc_status st = HC_OK;
+  if (cudaMemcpyAsync(dB, B, bytes, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+      cudaMemcpyAsync(dX, X, bytes, cudaMemcpyHostToDevice, h->stream) != cudaSuccess) {
+    h->err = "hc_solve_multi: host-to-device copy failed";
+    st = HC_ECUDA;
+  }
+  if (st == HC_OK) st = hc_solve_multi_device(h, prm, nrhs, dB, dX, info);
+  if (st == HC_OK || st == HC_NOT_CONVERGED || st == HC_BREAKDOWN) {
+    if (cudaMemcpyAsync(X, dX, bytes, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+        cudaStreamSynchronize(h->stream) != cudaSuccess) {
+      h->err = "hc_solve_multi: device-to-host copy failed";
+      st = HC_ECUDA;
+    }
+  }
+  dfree(h, dB);
+  dfree(h, dX);
+  cudaStreamSynchronize(h->stream);
+  return st;
+}

@@ -441,6 +441,30 @@ class GpuHCurlPCGSolver:
             out.append(self.result)
         return out
 
+    def MultMulti(self, B, X):
+        """Host form of MultMultiDevice: B, X are (ndof, nrhs) C-contiguous float64
+        numpy arrays ([dof][rhs]); X holds the initial guesses and is updated
+        in place.  Returns the per-column result dicts."""
+        op = self.op
+        if not (isinstance(X, np.ndarray) and X.dtype == np.float64 and X.flags.c_contiguous):
+            raise TypeError("X must be a C-contiguous float64 array (updated in place)")
+        B = np.ascontiguousarray(B, dtype=np.float64)
+        if B.shape != X.shape:
+            raise ValueError("B and X must have the same shape")
+        nrhs = 1 if B.ndim == 1 else int(B.shape[1])
+        if int(B.shape[0]) != op.ndof:
+            raise ValueError("B has %d rows, the operator %d dofs" % (int(B.shape[0]), op.ndof))
+        if nrhs not in (1, 2, 4, 8, 16, 32):
+            raise ValueError("the number of right-hand sides must be 1, 2, 4, 8, 16 or 32")
+        infos = (N.SolveInfo * nrhs)()
+        st = N.lib().hc_solve_multi(op.h, C.byref(self.p), nrhs, _ptr(B), _ptr(X), infos)
+        self._check(st)
+        out = []
+        for i in infos:
+            self.info = i
+            out.append(self.result)
+        return out
+
     def _check(self, st):
         if st in (N.HC_OK,):
             return

@@ -15,6 +15,7 @@
 #pragma once
 #include <cstdio>
 #include <string>
+#include <vector>
 
 #include "hcurl_op.h"
 #include "mfem.hpp"
@@ -98,10 +99,32 @@ public:
   }
   const hc_solve_info& Info() const { return info_; }
 
+  // Solve for the columns of B together (hc_solve_multi: one block PCG whose
+  // iterations share every operator apply; tet meshes).  B and X are
+  // ndof x nrhs, nrhs in {1, 2, 4, 8, 16, 32}; X holds the initial guesses
+  // (iterative_mode) and receives the solutions; Infos() has one report per column.
+  void MultBlock(const mfem::DenseMatrix& B, mfem::DenseMatrix& X) const {
+    const int n = B.Height(), r = B.Width();
+    if (X.Height() != n || X.Width() != r) MFEM_ABORT("GpuHCurlSolver::MultBlock: B and X shapes differ");
+    std::vector<double> b((size_t)n * r), x((size_t)n * r, 0.0);
+    for (int k = 0; k < r; ++k)
+      for (int i = 0; i < n; ++i) {
+        b[(size_t)i * r + k] = B(i, k);
+        if (iterative_mode) x[(size_t)i * r + k] = X(i, k);
+      }
+    infos_.assign(r, hc_solve_info{});
+    const hc_status st = hc_solve_multi(op_->Handle(), &prm_, r, b.data(), x.data(), infos_.data());
+    if (st != HC_OK && st != HC_NOT_CONVERGED) MFEM_ABORT("hc_solve_multi: " << last_error(op_->Handle()));
+    for (int k = 0; k < r; ++k)
+      for (int i = 0; i < n; ++i) X(i, k) = x[(size_t)i * r + k];
+  }
+  const std::vector<hc_solve_info>& Infos() const { return infos_; }
+
 private:
   const GpuHCurlOperator* op_ = nullptr;
   hc_solve_params prm_{};
   mutable hc_solve_info info_{};
+  mutable std::vector<hc_solve_info> infos_;
 };
 
 }  // namespace hcurl

@@ -229,6 +229,10 @@ hc_status hc_tet_gradient_device(hcop_t* h, const double* u, double* y);
  * (hcurl_formulation.cpp:81-85, problem_builder_base.cpp:221-253).        */
 hc_status hc_solve_multi_device(hcop_t* h, const hc_solve_params* prm, int32_t nrhs, const double* B, double* X,
                                 hc_solve_info* info);
+/* hc_solve_multi_device with host arrays (same [dof][rhs] layout; X holds
+ * the initial guesses and receives the solutions).                         */
+hc_status hc_solve_multi(hcop_t* h, const hc_solve_params* prm, int32_t nrhs, const double* B, double* X,
+                         hc_solve_info* info);
 /* Tet auxiliary-space preconditioner, once set up by an HC_PRECOND_AUX solve:
  * returns the number of AMG levels and writes their sizes (free vertices on
  * level 0) to sizes[0..], followed by the number of free edge bubbles when

@@ -11,5 +11,7 @@ int shim_smoke(hc_problem_desc d) {
   mfem::Vector b(op.Height()), x(op.Height());
   solver.Mult(b, x);
   op.Mult(x, b);
-  return solver.Info().iterations;
+  mfem::DenseMatrix B(op.Height(), 16), X(op.Height(), 16);
+  solver.MultBlock(B, X);
+  return solver.Info().iterations + (int)solver.Infos().size();
 }

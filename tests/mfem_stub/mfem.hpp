@@ -28,6 +28,18 @@ public:
 private:
   std::vector<double> d_;
 };
+class DenseMatrix {  // column-major, like MFEM's
+public:
+  DenseMatrix(int h = 0, int w = 0) : h_(h), w_(w), d_((size_t)h * w, 0.0) {}
+  int Height() const { return h_; }
+  int Width() const { return w_; }
+  double& operator()(int i, int j) { return d_[(size_t)j * h_ + i]; }
+  const double& operator()(int i, int j) const { return d_[(size_t)j * h_ + i]; }
+
+private:
+  int h_, w_;
+  std::vector<double> d_;
+};
 class Operator {
 public:
   virtual ~Operator() = default;

@@ -157,3 +157,10 @@ def test_block_solve_wrapper_checks_shapes_before_the_device():
         s.MultMultiDevice(torch.zeros(9, 4, dtype=torch.float64), torch.zeros(9, 4, dtype=torch.float64))
     with pytest.raises(ValueError, match="right-hand sides"):
         s.MultMultiDevice(torch.zeros(10, 3, dtype=torch.float64), torch.zeros(10, 3, dtype=torch.float64))
+
+
+def test_host_block_solve_rejects_bad_arguments():
+    L = N.lib()
+    p = N.SolveParams()
+    info = (N.SolveInfo * 16)()
+    assert L.hc_solve_multi(None, C.byref(p), 16, None, None, info) == N.HC_EINVAL

@@ -190,3 +190,19 @@ def test_tet_coil_load_matches_oracle(p):
         br = ref.load_coil(I0=1.3, xc=0.56, yc=0.45, q=q)
         assert np.count_nonzero(br) > 0
         assert np.linalg.norm(b - br) <= 1e-13 * np.linalg.norm(br), q
+
+
+def test_tet_host_block_solve_matches_device_block_solve():
+    """hc_solve_multi (host arrays, the MFEM shim's MultBlock) = hc_solve_multi_device."""
+    import torch
+
+    op, ref, rng = _pair(3, 2, seed=6)
+    B = rng.standard_normal((op.ndof, 4))
+    B[op.ess_mask() == 1, :] = 0.0
+    prm = {"Tolerance": 1e-12, "AbsTolerance": 0.0, "MaxIter": 100000, "Precision": "fp64"}
+    X = np.zeros_like(B)
+    res_h = GpuHCurlPCGSolver(prm, op).MultMulti(B, X)
+    Xd = torch.zeros(op.ndof, 4, dtype=torch.float64, device="cuda")
+    res_d = GpuHCurlPCGSolver(prm, op).MultMultiDevice(torch.tensor(B, device="cuda"), Xd)
+    assert all(r["status"] == "OK" for r in res_h + res_d)
+    assert np.linalg.norm(X - Xd.cpu().numpy()) <= 1e-9 * np.linalg.norm(X)
