@@ -519,7 +519,6 @@ static hc_status mpcg_run(hcop* h, int R, double rtol, double atol, int maxit, c
   hs->atol2 = atol * atol;
   hs->maxit = maxit;
   HC_CUDA_TRY(h, cudaMemcpyAsync(w->S, hs, sizeof(MScalars), cudaMemcpyHostToDevice, s));
-  const unsigned g = mgrid(n, R);
   HC_CUDA_TRY(h, multi_apply<T>(h, R, X, q, s));
   M_LAUNCH(k_m_setup, n, R, B, q, r, dinv, w->S, w->partials);
   HC_CUDA_TRY(h, cudaMemsetAsync(p, 0, n * R * sizeof(T), s));
