@@ -301,6 +301,13 @@ def run_ours(args):
     solves = None
     if args.solves > 0:
         solves = measure_solves(op, args.solves, args.solve_rtol, args.inner_rtol)
+    # ---- the tets workload's 16-RHS block solves (same metric, unstructured-tet configuration) ----
+    tets = None
+    if args.solves > 0 and not args.no_tets:
+        try:
+            tets = tet_block_summary(args)
+        except Exception as e:  # reported in the line; the hex numbers stand
+            tets = {"error": "%s: %s" % (type(e).__name__, e)}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -328,6 +335,7 @@ def run_ours(args):
                     "path": "hc_mult (FP64 operator, pinned host x/y, copies timed)"},
             "cpu_baseline": cpu,
             "solves": solves,
+            "tet_block_solves": tets,
             "gpu_launches": 2 * args.steps,
             "clocks": clocks,
         }
@@ -481,16 +489,9 @@ def run_tets(args):
     FP64 and FP32-inner/FP64-refinement) to the requested relative residual."""
     import torch
 
-    from hephaestus_gb300 import HCurlOperator, meshes
-
     dist_init()
-    n = 48
-    v, t, bt, ba = meshes.kuhn_mesh(n, jitter=0.15, seed=0)
-    rng = np.random.default_rng(0)
-    ne = len(t)
     t0 = time.perf_counter()
-    op = HCurlOperator.from_tets(v, t, 2, meshes.loguniform(ne, 1.0, 1e3, rng), meshes.loguniform(ne, 1e-2, 1e6, rng),
-                                 dt=0.01, btris=bt, battr=ba, ess_attr_bits=0x3F)
+    op, ne = make_tets48()
     setup_s = time.perf_counter() - t0
     nrhs = 16
     X32 = torch.randn(op.ndof, nrhs, device="cuda")
@@ -525,6 +526,33 @@ def run_tets(args):
             "fp32": out["fp32"], "fp64": out["fp64"], "bf16_matrices": out["bf16_matrices"],
             "setup_seconds": setup_s, "solves": solves}
     print(json.dumps(line))
+
+
+def make_tets48():
+    """Kuhn 48^3 tets (663,552), interior vertices jittered by U(-0.15h, 0.15h),
+    ND p=2, nu = 10^U(0,3), sigma = 10^U(-2,6) per element, dt = 0.01, A x n = 0."""
+    from hephaestus_gb300 import HCurlOperator, meshes
+
+    v, t, bt, ba = meshes.kuhn_mesh(48, jitter=0.15, seed=0)
+    rng = np.random.default_rng(0)
+    ne = len(t)
+    op = HCurlOperator.from_tets(v, t, 2, meshes.loguniform(ne, 1.0, 1e3, rng), meshes.loguniform(ne, 1e-2, 1e6, rng),
+                                 dt=0.01, btris=bt, battr=ba, ess_attr_bits=0x3F)
+    return op, ne
+
+
+def tet_block_summary(args):
+    """The tets workload's 16-RHS block solves, reported beside the hex line."""
+    import torch
+
+    op, ne = make_tets48()
+    try:
+        out = tet_solves(args, op, 16)
+        out["workload"] = "tets48: Kuhn 48^3 (%d tets), jitter 0.15h, ND p=2, %d dofs, 16 coil RHS" % (ne, op.ndof)
+        return out
+    finally:
+        op.close()
+        torch.cuda.synchronize()
 
 
 def tet_coil_rhs(op, nrhs, seed):
@@ -604,6 +632,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tets", action="store_true", help="skip the tets block solves reported beside the hex line")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--cpu-step-seconds", type=float, default=1.0)
     ap.add_argument("--workload", default="apply", choices=["apply", "batch", "serve", "tets"])
