@@ -11,6 +11,8 @@
 #include <utility>
 #include <vector>
 
+#include "hc_host_par.h"
+
 namespace hc {
 namespace amg {
 
@@ -20,24 +22,6 @@ struct HCsr {
   std::vector<double> va;
 };
 
-// Run f(lo, hi) over [0, n) in contiguous chunks on up to 16 host threads.
-template <typename F>
-inline void parallel_for(int n, F f) {
-  const int hw = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-  const int nt = std::max(1, std::min(hw, n / 64));
-  if (nt <= 1) {
-    f(0, n);
-    return;
-  }
-  std::vector<std::thread> th;
-  th.reserve(nt);
-  for (int k = 0; k < nt; ++k) {
-    const int lo = (int)((int64_t)n * k / nt), hi = (int)((int64_t)n * (k + 1) / nt);
-    th.emplace_back([&f, lo, hi] { f(lo, hi); });
-  }
-  for (auto& t : th) t.join();
-}
-
 // Build an n-row CSR whose rows are produced independently: row_fn(i, marker,
 // scratch, ci, va) appends row i's sorted (column, value) entries.  Rows are
 // computed in contiguous chunks on host threads (each with its own marker
@@ -45,8 +29,7 @@ inline void parallel_for(int n, F f) {
 // on the thread count.
 template <typename RowFn>
 inline HCsr build_rows(int n, int m, RowFn row_fn) {
-  const int hw = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-  const int nt = std::max(1, std::min(hw, n / 256));
+  const int nt = std::max(1, std::min(host_threads(), n / 256));
   std::vector<std::vector<int>> cis(nt), lens(nt);
   std::vector<std::vector<double>> vas(nt);
   auto work = [&](int c) {

@@ -28,118 +28,28 @@
 
 #include "hc_internal.h"
 #include "hc_reduce.cuh"
+#include "hc_tet_topo.h"
 
 namespace hc {
 
-namespace {
-const int kEdges[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
-const int kFaces[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
-}  // namespace
-
-// ---- host topology -------------------------------------------------------------
+// ---- host topology (hc_tet_topo.h) ------------------------------------------------
 hc_status tet_topology(hcop* h, const hc_problem_desc* d, std::vector<int32_t>& edofs,
                        std::vector<int32_t>& sorted_verts) {
-  const int64_t ne = d->n_elem, nv = d->n_vert;
-  const int p = d->order;
-  sorted_verts.resize(ne * 4);
-  for (int64_t e = 0; e < ne; ++e) {
-    int64_t s[4];
-    for (int k = 0; k < 4; ++k) {
-      s[k] = d->elem_verts[4 * e + k];
-      if (s[k] < 0 || s[k] >= nv) {
-        h->err = "hc_create: tet vertex index out of range";
-        return HC_EINVAL;
-      }
-    }
-    std::sort(s, s + 4);
-    if (s[0] == s[1] || s[1] == s[2] || s[2] == s[3]) {
-      h->err = "hc_create: degenerate tet (repeated vertex)";
-      return HC_EINVAL;
-    }
-    for (int k = 0; k < 4; ++k) sorted_verts[4 * e + k] = (int32_t)s[k];
+  topo::TetTopology T;
+  std::string msg;
+  const int st = topo::build_tet_topology(d->n_elem, d->n_vert, d->elem_verts, d->order, d->ess_mask, d->n_bdr,
+                                          d->bdr_tris, d->bdr_attr, d->ess_attr_bits, T, msg);
+  if (st != topo::kOk) {
+    h->err = msg;
+    return st == topo::kTooLarge ? HC_ENOTSUP : HC_EINVAL;
   }
-  std::vector<uint64_t> ekeys;
-  ekeys.reserve(ne * 6);
-  for (int64_t e = 0; e < ne; ++e)
-    for (auto& ed : kEdges)
-      ekeys.push_back((uint64_t)sorted_verts[4 * e + ed[0]] * (uint64_t)nv + (uint64_t)sorted_verts[4 * e + ed[1]]);
-  std::sort(ekeys.begin(), ekeys.end());
-  ekeys.erase(std::unique(ekeys.begin(), ekeys.end()), ekeys.end());
-  std::vector<std::array<int32_t, 3>> fkeys;
-  if (p == 2) {
-    fkeys.reserve(ne * 4);
-    for (int64_t e = 0; e < ne; ++e)
-      for (auto& f : kFaces)
-        fkeys.push_back({sorted_verts[4 * e + f[0]], sorted_verts[4 * e + f[1]], sorted_verts[4 * e + f[2]]});
-    std::sort(fkeys.begin(), fkeys.end());
-    fkeys.erase(std::unique(fkeys.begin(), fkeys.end()), fkeys.end());
-  }
-  const int64_t nE = (int64_t)ekeys.size(), nF = (int64_t)fkeys.size();
-  const int L = p == 1 ? 6 : 20;
-  h->ndof = p == 1 ? nE : 2 * nE + 2 * nF;
-  h->n_edges = nE;
-  h->n_faces = nF;
-  if (h->ndof >= ((int64_t)1 << 31)) {
-    h->err = "hc_create: more than 2^31 - 1 dofs per problem is not supported";
-    return HC_ENOTSUP;
-  }
-  edofs.resize(ne * L);
-  for (int64_t e = 0; e < ne; ++e) {
-    int32_t* dd = &edofs[e * L];
-    for (int k = 0; k < 6; ++k) {
-      const uint64_t key =
-          (uint64_t)sorted_verts[4 * e + kEdges[k][0]] * (uint64_t)nv + (uint64_t)sorted_verts[4 * e + kEdges[k][1]];
-      const int64_t g = std::lower_bound(ekeys.begin(), ekeys.end(), key) - ekeys.begin();
-      if (p == 1) dd[k] = (int32_t)g;
-      else {
-        dd[2 * k] = (int32_t)(2 * g);
-        dd[2 * k + 1] = (int32_t)(2 * g + 1);
-      }
-    }
-    if (p == 2)
-      for (int f = 0; f < 4; ++f) {
-        const std::array<int32_t, 3> key{sorted_verts[4 * e + kFaces[f][0]], sorted_verts[4 * e + kFaces[f][1]],
-                                         sorted_verts[4 * e + kFaces[f][2]]};
-        const int64_t g = std::lower_bound(fkeys.begin(), fkeys.end(), key) - fkeys.begin();
-        dd[12 + 2 * f] = (int32_t)(2 * nE + 2 * g);
-        dd[12 + 2 * f + 1] = (int32_t)(2 * nE + 2 * g + 1);
-      }
-  }
-  // essential dofs from marked boundary triangles
-  h->ess_host.assign(h->ndof, 0);
-  if (d->ess_mask) {
-    for (int64_t i = 0; i < h->ndof; ++i) h->ess_host[i] = d->ess_mask[i] ? 1 : 0;
-    h->explicit_mask = true;
-  } else if (d->n_bdr > 0 && d->bdr_tris && d->bdr_attr) {
-    for (int64_t b = 0; b < d->n_bdr; ++b) {
-      const int a = d->bdr_attr[b];
-      if (a < 1 || a > 31 || !((d->ess_attr_bits >> (a - 1)) & 1)) continue;
-      int64_t s[3] = {d->bdr_tris[3 * b], d->bdr_tris[3 * b + 1], d->bdr_tris[3 * b + 2]};
-      std::sort(s, s + 3);
-      const int pr[3][2] = {{0, 1}, {0, 2}, {1, 2}};
-      for (auto& q : pr) {
-        const uint64_t key = (uint64_t)s[q[0]] * (uint64_t)nv + (uint64_t)s[q[1]];
-        auto it = std::lower_bound(ekeys.begin(), ekeys.end(), key);
-        if (it == ekeys.end() || *it != key) {
-          h->err = "hc_create: boundary triangle edge is not an edge of the mesh";
-          return HC_EINVAL;
-        }
-        const int64_t g = it - ekeys.begin();
-        if (p == 1) h->ess_host[g] = 1;
-        else h->ess_host[2 * g] = h->ess_host[2 * g + 1] = 1;
-      }
-      if (p == 2) {
-        const std::array<int32_t, 3> key{(int32_t)s[0], (int32_t)s[1], (int32_t)s[2]};
-        auto it = std::lower_bound(fkeys.begin(), fkeys.end(), key);
-        if (it == fkeys.end() || *it != key) {
-          h->err = "hc_create: boundary triangle is not a face of the mesh";
-          return HC_EINVAL;
-        }
-        const int64_t g = it - fkeys.begin();
-        h->ess_host[2 * nE + 2 * g] = h->ess_host[2 * nE + 2 * g + 1] = 1;
-      }
-    }
-  }
+  edofs.swap(T.edofs);
+  sorted_verts.swap(T.sorted_verts);
+  h->ess_host.swap(T.ess);
+  h->ndof = T.ndof;
+  h->n_edges = T.n_edges;
+  h->n_faces = T.n_faces;
+  h->explicit_mask = T.explicit_mask;
   return HC_OK;
 }
 
