@@ -221,8 +221,8 @@ inline HCsr spgemm(const HCsr& A, const HCsr& B) {
 }
 
 // inv = (S A S)^-1 with S = diag^-1/2, sc = S (both FP32, for the device), by a
-// Cholesky factor L of S A S (row-major, contiguous inner products, one host
-// thread: n^3 / 3 multiply-adds, about 0.3 s at n = 1,500), the rows
+// Cholesky factor L of S A S (row-major, contiguous inner products, rows below
+// each column block on host threads), the rows
 // of L^-1's transpose (row j = column j of L^-1, computed independently on
 // host threads) and inv[i][j] = sum_k L^-1[k][i] L^-1[k][j] (threads over i).
 // Returns false if S A S is not positive definite.
@@ -233,20 +233,38 @@ inline bool dense_scaled_inverse(const HCsr& A, const std::vector<double>& dg, s
   for (int i = 0; i < n; ++i) s[i] = 1.0 / std::sqrt(std::fabs(dg[i]));
   for (int i = 0; i < n; ++i)
     for (int k = A.rp[i]; k < A.rp[i + 1]; ++k) M[(size_t)i * n + A.ci[k]] = s[i] * A.va[k] * s[A.ci[k]];
-  // Cholesky, lower triangle in place (row j of L from rows < j)
-  for (int j = 0; j < n; ++j) {
-    const double* rj = &M[(size_t)j * n];
-    double d = rj[j];
-    for (int k = 0; k < j; ++k) d -= rj[k] * rj[k];
-    if (!(d > 1e-12)) return false;
-    d = std::sqrt(d);
-    M[(size_t)j * n + j] = d;
-    for (int i = j + 1; i < n; ++i) {
-      double* ri = &M[(size_t)i * n];
-      double v = ri[j];
-      for (int k = 0; k < j; ++k) v -= ri[k] * rj[k];
-      ri[j] = v / d;
+  // Cholesky, lower triangle in place, by column blocks of 64: the block's own
+  // rows in order, then every row below it on host threads.  Each entry is
+  // L[i][j] = (M[i][j] - sum_{k<j} L[i][k] L[j][k]) / L[j][j] with the sum in
+  // ascending k, as in the column-by-column algorithm.
+  constexpr int kBlock = 64;
+  for (int j0 = 0; j0 < n; j0 += kBlock) {
+    const int j1 = std::min(n, j0 + kBlock);
+    for (int j = j0; j < j1; ++j) {
+      const double* rj = &M[(size_t)j * n];
+      double d = rj[j];
+      for (int k = 0; k < j; ++k) d -= rj[k] * rj[k];
+      if (!(d > 1e-12)) return false;
+      d = std::sqrt(d);
+      M[(size_t)j * n + j] = d;
+      for (int i = j + 1; i < j1; ++i) {
+        double* ri = &M[(size_t)i * n];
+        double v = ri[j];
+        for (int k = 0; k < j; ++k) v -= ri[k] * rj[k];
+        ri[j] = v / d;
+      }
     }
+    parallel_for(n - j1, [&](int64_t lo, int64_t hi) {
+      for (int64_t ii = lo; ii < hi; ++ii) {
+        double* ri = &M[(size_t)(j1 + ii) * n];
+        for (int j = j0; j < j1; ++j) {
+          const double* rj = &M[(size_t)j * n];
+          double v = ri[j];
+          for (int k = 0; k < j; ++k) v -= ri[k] * rj[k];
+          ri[j] = v / rj[j];
+        }
+      }
+    }, 16);
   }
   // LiT[j][k] = (L^-1)[k][j], k >= j: forward substitution L y = e_j
   std::vector<double> LiT((size_t)n * n, 0.0);
