@@ -149,13 +149,17 @@ inline bool build_aux_structure(int p, int64_t ne, int64_t N, int64_t n_edges, c
   A.n = A.m = nfree;
   {
     std::vector<uint64_t> keys;
-    keys.reserve(ne * 6);
-    for (int64_t e = 0; e < ne; ++e)
-      for (auto& q : kHEdges) {
-        const int a = fmap[sv[4 * e + q[0]]], b = fmap[sv[4 * e + q[1]]];
-        if (a >= 0 && b >= 0) keys.push_back((uint64_t)std::min(a, b) * (uint64_t)nfree + (uint64_t)std::max(a, b));
-      }
+    keys.assign(ne * 6, ~(uint64_t)0);  // ~0: an edge with a fixed vertex (sorted last, dropped)
+    parallel_for(ne, [&](int64_t lo_e, int64_t hi_e) {
+      for (int64_t e = lo_e; e < hi_e; ++e)
+        for (int k = 0; k < 6; ++k) {
+          const int a = fmap[sv[4 * e + kHEdges[k][0]]], b = fmap[sv[4 * e + kHEdges[k][1]]];
+          if (a >= 0 && b >= 0)
+            keys[6 * e + k] = (uint64_t)std::min(a, b) * (uint64_t)nfree + (uint64_t)std::max(a, b);
+        }
+    });
     parallel_sort(keys);
+    while (!keys.empty() && keys.back() == ~(uint64_t)0) keys.pop_back();
     keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
     A.rp.assign(nfree + 1, 0);
     for (int i = 0; i < nfree; ++i) A.rp[i + 1] = 1;
@@ -175,18 +179,26 @@ inline bool build_aux_structure(int p, int64_t ne, int64_t N, int64_t n_edges, c
     }
     for (int i = 0; i < nfree; ++i) std::sort(A.ci.begin() + A.rp[i], A.ci.begin() + A.rp[i + 1]);
     const int tri[4][4] = {{0, 1, 2, 3}, {1, 4, 5, 6}, {2, 5, 7, 8}, {3, 6, 8, 9}};
-    for (int64_t e = 0; e < ne; ++e)
-      for (int a = 0; a < 4; ++a) {
-        const int i = fmap[sv[4 * e + a]];
-        if (i < 0) continue;
-        for (int b = 0; b < 4; ++b) {
-          const int j = fmap[sv[4 * e + b]];
-          if (j < 0) continue;
-          const int* lo = &A.ci[A.rp[i]];
-          const int* hi = &A.ci[A.rp[i + 1]];
-          A.va[std::lower_bound(lo, hi, j) - &A.ci[0]] += Ae[e * nout + tri[a][b]];
+    // CSR positions of every element's 16 entries on host threads (-1: fixed
+    // vertex), then the sums in element order
+    std::vector<int> pos16(ne * 16, -1);
+    parallel_for(ne, [&](int64_t lo_e, int64_t hi_e) {
+      for (int64_t e = lo_e; e < hi_e; ++e)
+        for (int a = 0; a < 4; ++a) {
+          const int i = fmap[sv[4 * e + a]];
+          if (i < 0) continue;
+          for (int b = 0; b < 4; ++b) {
+            const int j = fmap[sv[4 * e + b]];
+            if (j < 0) continue;
+            const int* lo = &A.ci[A.rp[i]];
+            const int* hi = &A.ci[A.rp[i + 1]];
+            pos16[e * 16 + 4 * a + b] = (int)(std::lower_bound(lo, hi, j) - &A.ci[0]);
+          }
         }
-      }
+    });
+    for (int64_t e = 0; e < ne; ++e)
+      for (int ab = 0; ab < 16; ++ab)
+        if (pos16[e * 16 + ab] >= 0) A.va[pos16[e * 16 + ab]] += Ae[e * nout + tri[ab / 4][ab % 4]];
   }
 
   // order 2: D_L^-1 on the nodal rows (vertex block diagonal, edge-bubble diagonal)
