@@ -149,6 +149,42 @@ class CpuBaseline:
                 "sub-problem (%d dofs, nnz %d), %d reps in %.1f s" % (self.P.ndof, self.nnz, reps, el))
 
 
+class TetCpuBaseline(CpuBaseline):
+    """FP64 CSR SpMV of the eliminated tet operator (oracle assembly) on the
+    Kuhn n^3 sub-problem of the tets workload (same jitter and coefficient
+    distributions), one SpMV per right-hand side, all host threads."""
+
+    def __init__(self, n_sample=24, nthreads=None):
+        import oracle
+
+        from hephaestus_gb300 import meshes
+
+        self.nthreads = nthreads or os.cpu_count()
+        self.n = n_sample
+        v, t, bt, ba = meshes.kuhn_mesh(n_sample, jitter=0.15, seed=0)
+        rng = np.random.default_rng(0)
+        ne = len(t)
+        P = oracle.Problem.tet(v, t, 2)
+        P.set_coef(0.01 * meshes.loguniform(ne, 1.0, 1e3, rng), meshes.loguniform(ne, 1e-2, 1e6, rng))
+        P.assemble()
+        P.set_ess(P.tet_ess_mask(bt, ba, 0x3F))
+        self.ne = ne
+        self.L = oracle.lib()
+        self.nnz = self.L.orc_build_eliminated(P.h)
+        self.P = P
+        self.x = np.random.default_rng(1).standard_normal(P.ndof)
+        self.y = np.empty_like(self.x)
+        self.px = self.x.ctypes.data_as(oracle.C.c_void_p)
+        self.py = self.y.ctypes.data_as(oracle.C.c_void_p)
+        self.L.orc_spmv_eliminated(P.h, self.px, self.py, self.nthreads)  # warm-up
+
+    def sample(self):
+        reps, el = self.last
+        return ("FP64 CSR SpMV (32-bit columns) of the eliminated operator on the Kuhn %d^3 tet ND p=2 "
+                "sub-problem (%d tets, %d dofs, nnz %d), one SpMV per right-hand side, %d in %.1f s"
+                % (self.n, self.ne, self.P.ndof, self.nnz, reps, el))
+
+
 # ----------------------------------------------------------------------------
 def dist_init():
     import torch
@@ -519,12 +555,18 @@ def run_tets(args):
         out[name] = {"ms_per_apply": ms, "gdof_rhs_per_s": op.ndof * nrhs / (ms * 1e-3) / 1e9,
                      "alg_bytes": alg, "achieved_gbs": alg / (ms * 1e-3) / 1e9}
     solves = tet_solves(args, op, nrhs) if args.solves > 0 else None
+    cpu = None
+    if not args.no_cpu:
+        cb = TetCpuBaseline()
+        g_cpu = cb.measure(args.cpu_seconds)
+        cpu = {"value": g_cpu, "unit": "GDoF*RHS/s", "cores": cb.nthreads, "kind": "port",
+               "sample": cb.sample() + "; oracle restatement, not MFEM/hypre (not buildable here)"}
     line = {"metric": "GDoF/s x RHS, tet Nedelec p=2 element-matrix apply, 16 RHS",
             "value": out["fp32"]["gdof_rhs_per_s"], "unit": "GDoF*RHS/s", "n_gpus": 1, "higher_is_better": True,
             "config": {"workload": "tets48: Kuhn 48^3 (%d tets), jitter 0.15h, ND p=2, %d dofs, 16 RHS" % (ne, op.ndof),
                        "l2": "flushed between steps"},
             "fp32": out["fp32"], "fp64": out["fp64"], "bf16_matrices": out["bf16_matrices"],
-            "setup_seconds": setup_s, "solves": solves}
+            "setup_seconds": setup_s, "solves": solves, "cpu_baseline": cpu}
     print(json.dumps(line))
 
 

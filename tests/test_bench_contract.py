@@ -24,3 +24,15 @@ def test_reference_arm_prints_the_contract_line():
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
+
+
+def test_tet_cpu_baseline_measures_the_oracle_operator():
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    cb = bench.TetCpuBaseline(n_sample=6)
+    g = cb.measure(0.2)
+    assert g > 0 and cb.P.ndof > 0
+    assert "Kuhn 6^3" in cb.sample()
