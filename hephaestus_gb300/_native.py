@@ -18,6 +18,7 @@ STATUS_NAMES = ["OK", "EINVAL", "ENOMEM", "ECUDA", "NOT_CONVERGED", "BREAKDOWN",
 HC_HEX, HC_TET = 0, 1
 HC_FP64, HC_FP32, HC_MIXED, HC_BF16 = 0, 1, 2, 3
 HC_PRECOND_NONE, HC_PRECOND_JACOBI, HC_PRECOND_CHEBYSHEV, HC_PRECOND_AUX = 0, 1, 2, 3
+HC_FIELD_ELEM, HC_FIELD_QUAD = 0, 1
 
 
 class NativeUnavailable(RuntimeError):
@@ -133,6 +134,15 @@ _SIGS = {
     "hc_solve_multi": (C.c_int, [C.c_void_p, C.POINTER(SolveParams), C.c_int32, C.c_void_p, C.c_void_p,
                                  C.POINTER(SolveInfo)]),
     "hc_load_coil": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    "hc_quad_points_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "hc_load_field_device": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
+    "hc_curl_load_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hc_magnetic_field_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.POINTER(SolveInfo)]),
+    "hc_tet_curl_points_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "hc_be_rhs_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hc_be_update_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hc_be_steps_device": (C.c_int, [C.c_void_p, C.POINTER(SolveParams), C.c_int32, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_void_p, C.POINTER(SolveInfo)]),
     "hc_load_coil_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
 }
 

@@ -228,6 +228,9 @@ static hc_status create_tet(const hc_problem_desc* desc, hcop_t** out) {
   if (need > fr) return fail_create(h, "hc_create: problem exceeds free device memory", HC_ENOMEM);
   if (!tables_ready()) return fail_create(h, "hc_create: constant table upload failed", HC_ECUDA);
   if (!alloc_common(h)) return fail_create(h, "hc_create: device allocation failed", HC_ENOMEM);
+  if (dmalloc(h, (void**)&h->nu, h->ne * sizeof(double)) != cudaSuccess)
+    return fail_create(h, "hc_create: device allocation failed", HC_ENOMEM);
+  cudaMemcpyAsync(h->nu, desc->nu, h->ne * sizeof(double), cudaMemcpyHostToDevice, h->stream);
   cudaMemcpyAsync(h->ess, h->ess_host.data(), N, cudaMemcpyHostToDevice, h->stream);
   cudaError_t e = tet_setup_device(h, desc, edofs, sv);
   if (e == cudaErrorInvalidValue && h->err.empty())
@@ -287,7 +290,8 @@ void hc_destroy(hcop_t* h) {
   auxmg_free(h);
   multi_free(h);
   tetaux_free(h);
-  for (void* p : {(void*)h->fac, (void*)h->facf, (void*)h->ess, (void*)h->diag, (void*)h->dinv, (void*)h->dinvf,
+  if (h->mass_child) hc_destroy(h->mass_child);
+  for (void* p : {(void*)h->nu, (void*)h->fac, (void*)h->facf, (void*)h->ess, (void*)h->diag, (void*)h->dinv, (void*)h->dinvf,
                   (void*)h->sdinv, (void*)h->sdinvf, (void*)h->scal, (void*)h->partials, h->work, (void*)h->xbuf,
                   (void*)h->ybuf, (void*)h->verts, (void*)h->tet_edofs, (void*)h->tet_sv, (void*)h->tetK64, (void*)h->tetK32,
                   h->tetK16, (void*)h->tab})
@@ -445,7 +449,7 @@ hc_status hc_create(const hc_problem_desc* desc, hcop_t** out) {
   if (!alloc((void**)&h->fac, fac.size() * 8) || !alloc((void**)&h->facf, facf.size() * 4) ||
       !alloc((void**)&h->ess, N) || !alloc((void**)&h->diag, N * 8) || !alloc((void**)&h->dinv, N * 8) ||
       !alloc((void**)&h->dinvf, N * 4) || !alloc((void**)&h->sdinv, N * 8) || !alloc((void**)&h->sdinvf, N * 4) ||
-      !alloc((void**)&h->xbuf, N * 8) || !alloc((void**)&h->ybuf, N * 8))
+      !alloc((void**)&h->xbuf, N * 8) || !alloc((void**)&h->ybuf, N * 8) || !alloc((void**)&h->nu, ne * 8))
     return fail_create(h, "hc_create: device allocation failed", HC_ENOMEM);
   {
     std::vector<int> tab;
@@ -462,6 +466,7 @@ hc_status hc_create(const hc_problem_desc* desc, hcop_t** out) {
   cudaMemcpyAsync(h->fac, fac.data(), fac.size() * 8, cudaMemcpyHostToDevice, cs);
   cudaMemcpyAsync(h->facf, facf.data(), facf.size() * 4, cudaMemcpyHostToDevice, cs);
   cudaMemcpyAsync(h->ess, h->ess_host.data(), N, cudaMemcpyHostToDevice, cs);
+  cudaMemcpyAsync(h->nu, desc->nu, ne * sizeof(double), cudaMemcpyHostToDevice, cs);
   cudaMemsetAsync(h->diag, 0, N * 8, cs);
   const HexDev d = h->hexdev();
   if (hex_diag(d, h->diag, cs) != cudaSuccess)
@@ -702,6 +707,88 @@ hc_status hc_load_coil_device(hcop_t* h, const hc_coil* coil, int q, double* b) 
   const double cv[7] = {coil->I0, coil->xc, coil->yc, coil->r0, coil->r1, coil->z0, coil->z1};
   HC_CUDA_TRY(h, hex_load_coil(h->hexdev(), h->verts, cv, q, xq.data(), wq.data(), bc.data(), bo.data(), b,
                                h->stream));
+  return HC_OK;
+}
+
+// q-point Gauss-Legendre rule on [0,1] and the hex's 1-D bases at its points
+struct HexRule {
+  std::vector<double> xq, wq, bc, bo;
+};
+static HexRule hex_rule(const hcop* h, int q) {
+  HexRule r;
+  r.xq.resize(q);
+  r.wq.resize(q);
+  r.bc.resize(q * (h->p + 1));
+  r.bo.resize(q * h->p);
+  gl01(q, r.xq.data(), r.wq.data());
+  if (h->type != HC_HEX) return r;
+  double xc[kMaxP + 1], xo[kMaxP], wo[kMaxP], d1[kMaxP + 1];
+  gll01(h->p + 1, xc);
+  gl01(h->p, xo, wo);
+  for (int k = 0; k < q; ++k) {
+    lagrange(xc, h->p + 1, r.xq[k], &r.bc[k * (h->p + 1)], d1);
+    lagrange(xo, h->p, r.xq[k], &r.bo[k * h->p], d1);
+  }
+  return r;
+}
+
+hc_status hc_quad_points_device(hcop_t* h, int q, double* xyz) {
+  if (!h || !xyz) return HC_EINVAL;
+  if (q < 1 || q > 8) {
+    h->err = "hc_quad_points_device: 1 <= q <= 8";
+    return HC_EINVAL;
+  }
+  const HexRule r = hex_rule(h, q);
+  if (h->type == HC_TET) {
+    HC_CUDA_TRY(h, tet_quad_points(h, q, r.xq.data(), xyz, h->stream));
+  } else {
+    HC_CUDA_TRY(h, hex_quad_points(h->hexdev(), h->verts, q, r.xq.data(), r.wq.data(), r.bc.data(), r.bo.data(), xyz,
+                                   h->stream));
+  }
+  return HC_OK;
+}
+
+hc_status hc_load_field_device(hcop_t* h, int mode, int q, const double* J, double* b) {
+  if (!h || !J || !b) return HC_EINVAL;
+  if ((mode != HC_FIELD_ELEM && mode != HC_FIELD_QUAD) || q < 1 || q > 8) {
+    h->err = "hc_load_field_device: mode must be HC_FIELD_ELEM or HC_FIELD_QUAD and 1 <= q <= 8";
+    return HC_EINVAL;
+  }
+  const HexRule r = hex_rule(h, q);
+  const int per_point = mode == HC_FIELD_QUAD ? 1 : 0;
+  if (h->type == HC_TET) {
+    HC_CUDA_TRY(h, tet_load_field(h, per_point, J, q, r.xq.data(), r.wq.data(), b, h->stream));
+  } else {
+    HC_CUDA_TRY(h, hex_load_field(h->hexdev(), h->verts, per_point, J, q, r.xq.data(), r.wq.data(), r.bc.data(),
+                                  r.bo.data(), b, h->stream));
+  }
+  return HC_OK;
+}
+
+hc_status hc_curl_load_device(hcop_t* h, const double* A, double* b) {
+  if (!h || !A || !b) return HC_EINVAL;
+  if (h->type == HC_TET) {
+    // curl A (degree p - 1) . w_i (degree p) on affine tets: 4 points per
+    // direction of the collapsed rule are exact
+    const HexRule r = hex_rule(h, 4);
+    HC_CUDA_TRY(h, tet_curl_load(h, A, 4, r.xq.data(), r.wq.data(), b, h->stream));
+  } else {
+    HC_CUDA_TRY(h, hex_curl_load(h->hexdev(), h->nu, A, b, h->stream));
+  }
+  return HC_OK;
+}
+
+hc_status hc_tet_curl_points_device(hcop_t* h, const double* A, int npts, const double* xi, double* B) {
+  if (!h || !A || !xi || !B) return HC_EINVAL;
+  if (h->type != HC_TET) {
+    h->err = "hc_tet_curl_points_device: tet meshes only (hex grids: hc_curl_device)";
+    return HC_ENOTSUP;
+  }
+  if (npts < 1 || npts > 16) {
+    h->err = "hc_tet_curl_points_device: 1 <= npts <= 16";
+    return HC_EINVAL;
+  }
+  HC_CUDA_TRY(h, tet_curl_points(h, A, npts, xi, B, h->stream));
   return HC_OK;
 }
 

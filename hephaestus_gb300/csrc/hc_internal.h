@@ -109,6 +109,8 @@ struct hcop {
   void* mwork = nullptr;               // multi-RHS block PCG work space, hc_multi.cu
   void* taux = nullptr;                // tet auxiliary-space preconditioner, hc_tetaux.cu
   int64_t n_vert = 0;                  // tet meshes: vertices
+  double* nu = nullptr;                // per-element nu (FP64), for nu-weighted post-processing
+  hcop* mass_child = nullptr;          // unit-coefficient Nedelec mass on the same space (hc_fields.cu)
 
   hc::HexDev hexdev() const {
     hc::HexDev d;
@@ -166,6 +168,15 @@ void hex_rt_layout(const HexDev& d, int64_t* off1, int64_t* off2, int64_t* n);
 cudaError_t hex_curl(const HexDev& d, const double* A, double* B, cudaStream_t s);
 cudaError_t hex_load_coil(const HexDev& d, const double* V, const double coil[7], int q, const double* xq,
                           const double* wq, const double* bc, const double* bo, double* b, cudaStream_t s);
+// points of the q^3 Gauss-Legendre rule per element (ne * q^3 * 3)
+cudaError_t hex_quad_points(const HexDev& d, const double* V, int q, const double* xq, const double* wq,
+                            const double* bc, const double* bo, double* xyz, cudaStream_t s);
+// b = (J, w_i) for a source given per element (per_point = 0) or at the rule's points (1)
+cudaError_t hex_load_field(const HexDev& d, const double* V, int per_point, const double* src, int q,
+                           const double* xq, const double* wq, const double* bc, const double* bo, double* b,
+                           cudaStream_t s);
+// b_i = (nu curl A, w_i) with per-element nu
+cudaError_t hex_curl_load(const HexDev& d, const double* nu, const double* A, double* b, cudaStream_t s);
 
 // ---- hc_tet.cu ----
 hc_status tet_topology(hcop* h, const hc_problem_desc* d, std::vector<int32_t>& edofs,
@@ -180,6 +191,16 @@ cudaError_t tet_apply_launch_bf16(const hcop* h, const float* x, float* y, int n
 // b = coil load (I0, xc, yc, r0, r1, z0, z1) with a q^3 collapsed Gauss-Legendre rule per tet (1 <= q <= 8)
 cudaError_t tet_load_coil(const hcop* h, const double coil[7], int q, const double* xq, const double* wq, double* b,
                           cudaStream_t s);
+// points of the collapsed q^3 rule per tet (ne * q^3 * 3)
+cudaError_t tet_quad_points(const hcop* h, int q, const double* xq, double* xyz, cudaStream_t s);
+// b = (J, w_i) for a source given per element (per_point = 0) or at the rule's points (1)
+cudaError_t tet_load_field(const hcop* h, int per_point, const double* src, int q, const double* xq,
+                           const double* wq, double* b, cudaStream_t s);
+// b_i = (nu curl A, w_i) with per-element nu (collapsed rule, q points per direction)
+cudaError_t tet_curl_load(const hcop* h, const double* A, int q, const double* xq, const double* wq, double* b,
+                          cudaStream_t s);
+// B = curl A at npts reference points (<= 16) of every tet (ne * npts * 3)
+cudaError_t tet_curl_points(const hcop* h, const double* A, int npts, const double* xi, double* B, cudaStream_t s);
 // pq = p.q over all dofs, then alpha = rz / pq (PCG mode of operators without a fused energy)
 template <typename T>
 cudaError_t dot_alpha(int64_t n, const T* p, const T* q, KrylovScalars* S, double* partials, cudaStream_t s);

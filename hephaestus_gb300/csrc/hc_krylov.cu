@@ -771,8 +771,10 @@ hc_status mixed_device(hcop* h, const hc_solve_params* prm, const double* b, dou
       }
       c64.lmax = h->lmax64;
     }
-    c64.rtol = prm->rtol;
-    c64.atol = prm->atol;
+    // aim below the tolerance: the polish stops on its recursive residual,
+    // the status is judged on the true residual below
+    c64.rtol = 0.5 * prm->rtol;
+    c64.atol = 0.5 * prm->atol;
     c64.maxit = prm->maxit - iters;
     int it = 0, ap = 0;
     const hc_status pst = pcg_run<double>(h, c64, b, x, wk64, &it, &ap);
@@ -782,8 +784,9 @@ hc_status mixed_device(hcop* h, const hc_solve_params* prm, const double* b, dou
     if (pst == HC_ECUDA || pst == HC_ENOMEM) return pst;
     st = residual(&rn2, &bn2);
     if (st != HC_OK) return st;
-    // the FP64 Krylov's own verdict (recursive residual), as for a plain FP64 solve
-    result = std::isfinite(std::sqrt(rn2)) ? pst : HC_BREAKDOWN;
+    if (!std::isfinite(std::sqrt(rn2))) result = HC_BREAKDOWN;
+    else if (pst == HC_BREAKDOWN) result = pst;
+    else result = std::sqrt(rn2) <= tol ? HC_OK : HC_NOT_CONVERGED;
   }
   if (info) {
     info->status = result;

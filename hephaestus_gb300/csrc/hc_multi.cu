@@ -655,7 +655,10 @@ hc_status multi_solve_device(hcop* h, const hc_solve_params* prm, int R, const d
     double* wk64 = (double*)((char*)w->vec + off);
     int used = 0;
     for (int k = 0; k < R; ++k) used = std::max(used, total[k]);
-    st = mpcg_run<double>(h, R, prm->rtol, prm->atol, std::max(1, prm->maxit - used), B, X, wk64, h->dinv, aux);
+    // aim below the tolerance: the polish stops on its recursive residual,
+    // the status below is judged on the true one
+    st = mpcg_run<double>(h, R, 0.5 * prm->rtol, 0.5 * prm->atol, std::max(1, prm->maxit - used), B, X, wk64, h->dinv,
+                          aux);
     if (st != HC_OK) return st;
     for (int k = 0; k < R; ++k) {
       total[k] += w->hS->it[k];
@@ -666,7 +669,7 @@ hc_status multi_solve_device(hcop* h, const hc_solve_params* prm, int R, const d
   }
   hc_status worst = HC_OK;
   for (int k = 0; k < R; ++k) {
-    const bool ok = std::isfinite(rn[k]) && rn[k] <= tol[k] * (stalled ? 1.01 : 1.0);
+    const bool ok = std::isfinite(rn[k]) && rn[k] <= tol[k];
     info[k].status = std::isfinite(rn[k]) ? (ok ? HC_OK : HC_NOT_CONVERGED) : HC_BREAKDOWN;
     info[k].iterations = total[k];
     info[k].outer_iterations = outer[k];

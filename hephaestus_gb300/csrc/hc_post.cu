@@ -155,8 +155,8 @@ __global__ void hex_load_coil_kernel(HexDev d, const double* __restrict__ V, Coi
   scatter<double, P, 2>(d, b, ex, ey, ez, false, be2);
 }
 
-cudaError_t hex_load_coil(const HexDev& d, const double* V, const double coil[7], int q, const double* xq,
-                          const double* wq, const double* bc, const double* bo, double* b, cudaStream_t s) {
+static LoadTab make_load_tab(const HexDev& d, int q, const double* xq, const double* wq, const double* bc,
+                             const double* bo) {
   LoadTab t;
   std::memset(&t, 0, sizeof(t));
   t.q = q;
@@ -166,6 +166,168 @@ cudaError_t hex_load_coil(const HexDev& d, const double* V, const double coil[7]
     for (int j = 0; j <= d.p; ++j) t.bc[k][j] = bc[k * (d.p + 1) + j];
     for (int j = 0; j < d.p; ++j) t.bo[k][j] = bo[k * d.p + j];
   }
+  return t;
+}
+
+// Affine map of element e: corner v0, Jacobian J (columns = edge vectors),
+// inverse Ji, det.
+struct HexMap {
+  double v0[3], J[9], Ji[9], det;
+};
+__device__ __forceinline__ void hex_map(const HexDev& d, const double* __restrict__ V, int ex, int ey, int ez,
+                                        HexMap& m) {
+  auto vtx = [&](int a, int bb, int c) {
+    return V + 3 * ((ex + a) + (int64_t)(d.nx + 1) * ((ey + bb) + (int64_t)(d.ny + 1) * (ez + c)));
+  };
+  const double *v0 = vtx(0, 0, 0), *vx = vtx(1, 0, 0), *vy = vtx(0, 1, 0), *vz = vtx(0, 0, 1);
+  for (int r = 0; r < 3; ++r) {
+    m.v0[r] = v0[r];
+    m.J[3 * r] = vx[r] - v0[r];
+    m.J[3 * r + 1] = vy[r] - v0[r];
+    m.J[3 * r + 2] = vz[r] - v0[r];
+  }
+  const double* J = m.J;
+  m.det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) + J[2] * (J[3] * J[7] - J[4] * J[6]);
+  double* Ji = m.Ji;
+  Ji[0] = (J[4] * J[8] - J[5] * J[7]) / m.det;
+  Ji[1] = (J[2] * J[7] - J[1] * J[8]) / m.det;
+  Ji[2] = (J[1] * J[5] - J[2] * J[4]) / m.det;
+  Ji[3] = (J[5] * J[6] - J[3] * J[8]) / m.det;
+  Ji[4] = (J[0] * J[8] - J[2] * J[6]) / m.det;
+  Ji[5] = (J[2] * J[3] - J[0] * J[5]) / m.det;
+  Ji[6] = (J[3] * J[7] - J[4] * J[6]) / m.det;
+  Ji[7] = (J[1] * J[6] - J[0] * J[7]) / m.det;
+  Ji[8] = (J[0] * J[4] - J[1] * J[3]) / m.det;
+}
+
+// ---- points of the q^3 Gauss-Legendre rule, x = v0 + J xi -------------------------
+__global__ void hex_quad_points_kernel(HexDev d, const double* __restrict__ V, LoadTab t, double* __restrict__ xyz) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.ne) return;
+  const int ex = (int)(e % d.nx), ey = (int)((e / d.nx) % d.ny), ez = (int)(e / ((int64_t)d.nx * d.ny));
+  HexMap m;
+  hex_map(d, V, ex, ey, ez, m);
+  const int q = t.q, q3 = q * q * q;
+  for (int kz = 0; kz < q; ++kz)
+    for (int ky = 0; ky < q; ++ky)
+      for (int kx = 0; kx < q; ++kx) {
+        const double xi[3] = {t.x[kx], t.x[ky], t.x[kz]};
+        double* out = xyz + 3 * (e * q3 + kx + q * (ky + q * kz));
+        for (int r = 0; r < 3; ++r) out[r] = m.v0[r] + m.J[3 * r] * xi[0] + m.J[3 * r + 1] * xi[1] + m.J[3 * r + 2] * xi[2];
+      }
+}
+
+// ---- b = (J, w_i) for a caller-supplied source ------------------------------------
+// per_point = 0: J is one vector per element; 1: J at the q^3 points of the rule.
+// Covariant Piola: (j, w) = int (J^-1 j) . w_ref |det J|.
+template <int P>
+__global__ void hex_load_field_kernel(HexDev d, const double* __restrict__ V, LoadTab t, int per_point,
+                                      const double* __restrict__ src, double* __restrict__ b) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.ne) return;
+  constexpr int C = P + 1, O = P, NDC = O * C * C;
+  const int ex = (int)(e % d.nx), ey = (int)((e / d.nx) % d.ny), ez = (int)(e / ((int64_t)d.nx * d.ny));
+  HexMap m;
+  hex_map(d, V, ex, ey, ez, m);
+  const double adet = fabs(m.det);
+  double be0[NDC], be1[NDC], be2[NDC];
+  for (int i = 0; i < NDC; ++i) be0[i] = be1[i] = be2[i] = 0.0;
+  const int q = t.q, q3 = q * q * q;
+  for (int kz = 0; kz < q; ++kz)
+    for (int ky = 0; ky < q; ++ky)
+      for (int kx = 0; kx < q; ++kx) {
+        const double* jc = per_point ? src + 3 * (e * q3 + kx + q * (ky + q * kz)) : src + 3 * e;
+        const double wq = t.w[kx] * t.w[ky] * t.w[kz] * adet;
+        double f[3];
+        for (int r = 0; r < 3; ++r) f[r] = wq * (m.Ji[3 * r] * jc[0] + m.Ji[3 * r + 1] * jc[1] + m.Ji[3 * r + 2] * jc[2]);
+        for (int c = 0; c < C; ++c)
+          for (int bb = 0; bb < C; ++bb)
+            for (int a = 0; a < O; ++a)
+              be0[a + O * (bb + C * c)] += f[0] * t.bo[kx][a] * t.bc[ky][bb] * t.bc[kz][c];
+        for (int c = 0; c < C; ++c)
+          for (int bb = 0; bb < O; ++bb)
+            for (int a = 0; a < C; ++a)
+              be1[a + C * (bb + O * c)] += f[1] * t.bc[kx][a] * t.bo[ky][bb] * t.bc[kz][c];
+        for (int c = 0; c < O; ++c)
+          for (int bb = 0; bb < C; ++bb)
+            for (int a = 0; a < C; ++a)
+              be2[a + C * (bb + C * c)] += f[2] * t.bc[kx][a] * t.bc[ky][bb] * t.bo[kz][c];
+      }
+  scatter<double, P, 0>(d, b, ex, ey, ez, false, be0);
+  scatter<double, P, 1>(d, b, ex, ey, ez, false, be1);
+  scatter<double, P, 2>(d, b, ex, ey, ez, false, be2);
+}
+
+// ---- b_i = (nu curl A, w_i) ---------------------------------------------------------
+// curl A is the Raviart-Thomas field J r / det J (r the element-local curl of
+// the reference dofs) and w = J^-T w_ref, so the Piola factors cancel:
+// (curl A, w)_e = int r . w_ref over the reference cube.  Component c pairs RT
+// component c (closed in c, open across) with Nedelec component c (open in c,
+// closed across): one mixed 1-D mass per direction, exact.
+template <int P>
+__global__ void hex_curl_load_kernel(HexDev d, const double* __restrict__ nu, const double* __restrict__ A,
+                                     double* __restrict__ b) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.ne) return;
+  constexpr int C = P + 1, O = P, NDC = O * C * C, RTC = C * O * O;
+  const int ex = (int)(e % d.nx), ey = (int)((e / d.nx) % d.ny), ez = (int)(e / ((int64_t)d.nx * d.ny));
+  double u0[NDC], u1[NDC], u2[NDC], r0[RTC], r1[RTC], r2[RTC];
+  gather<double, P, 0>(d, A, ex, ey, ez, false, u0);
+  gather<double, P, 1>(d, A, ex, ey, ez, false, u1);
+  gather<double, P, 2>(d, A, ex, ey, ez, false, u2);
+  curl_nd<double, P>(u0, u1, u2, r0, r1, r2);
+  const double s = nu[e];
+  kron3_acc<double, P, NdT<0, 0>::v, RtT<0, 0>::v, NdT<0, 1>::v, RtT<0, 1>::v, NdT<0, 2>::v, RtT<0, 2>::v, false>(
+      r0, u0, s);
+  kron3_acc<double, P, NdT<1, 0>::v, RtT<1, 0>::v, NdT<1, 1>::v, RtT<1, 1>::v, NdT<1, 2>::v, RtT<1, 2>::v, false>(
+      r1, u1, s);
+  kron3_acc<double, P, NdT<2, 0>::v, RtT<2, 0>::v, NdT<2, 1>::v, RtT<2, 1>::v, NdT<2, 2>::v, RtT<2, 2>::v, false>(
+      r2, u2, s);
+  scatter<double, P, 0>(d, b, ex, ey, ez, false, u0);
+  scatter<double, P, 1>(d, b, ex, ey, ez, false, u1);
+  scatter<double, P, 2>(d, b, ex, ey, ez, false, u2);
+}
+
+cudaError_t hex_quad_points(const HexDev& d, const double* V, int q, const double* xq, const double* wq,
+                            const double* bc, const double* bo, double* xyz, cudaStream_t s) {
+  const LoadTab t = make_load_tab(d, q, xq, wq, bc, bo);
+  const int blocks = (int)((d.ne + 127) / 128);
+  hex_quad_points_kernel<<<blocks, 128, 0, s>>>(d, V, t, xyz);
+  return cudaGetLastError();
+}
+
+cudaError_t hex_load_field(const HexDev& d, const double* V, int per_point, const double* src, int q,
+                           const double* xq, const double* wq, const double* bc, const double* bo, double* b,
+                           cudaStream_t s) {
+  const LoadTab t = make_load_tab(d, q, xq, wq, bc, bo);
+  cudaError_t e = cudaMemsetAsync(b, 0, d.ndof * sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  const int blocks = (int)((d.ne + 127) / 128);
+  switch (d.p) {
+    case 1: hex_load_field_kernel<1><<<blocks, 128, 0, s>>>(d, V, t, per_point, src, b); break;
+    case 2: hex_load_field_kernel<2><<<blocks, 128, 0, s>>>(d, V, t, per_point, src, b); break;
+    case 3: hex_load_field_kernel<3><<<blocks, 128, 0, s>>>(d, V, t, per_point, src, b); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t hex_curl_load(const HexDev& d, const double* nu, const double* A, double* b, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(b, 0, d.ndof * sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  const int blocks = (int)((d.ne + 127) / 128);
+  switch (d.p) {
+    case 1: hex_curl_load_kernel<1><<<blocks, 128, 0, s>>>(d, nu, A, b); break;
+    case 2: hex_curl_load_kernel<2><<<blocks, 128, 0, s>>>(d, nu, A, b); break;
+    case 3: hex_curl_load_kernel<3><<<blocks, 128, 0, s>>>(d, nu, A, b); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t hex_load_coil(const HexDev& d, const double* V, const double coil[7], int q, const double* xq,
+                          const double* wq, const double* bc, const double* bo, double* b, cudaStream_t s) {
+  const LoadTab t = make_load_tab(d, q, xq, wq, bc, bo);
   cudaError_t e = cudaMemsetAsync(b, 0, d.ndof * sizeof(double), s);
   if (e != cudaSuccess) return e;
   const CoilDev cd{coil[0], coil[1], coil[2], coil[3], coil[4], coil[5], coil[6]};

@@ -727,6 +727,219 @@ __global__ void __launch_bounds__(128) tet_load_coil_kernel(int64_t ne, int p, c
     if (be[i] != 0.0) atomicAdd(b + edofs[e * L + i], be[i]);
 }
 
+// ---- fields on tets: quadrature points, (J, w_i), (nu curl A, w_i), curl at points ------
+// Geometry of tet e on its sorted vertices: corner, gradients of the
+// barycentrics, |det J|.
+struct TetGeom {
+  double v[4][3];
+  double gl[4][3];
+  double adet;
+};
+__device__ __forceinline__ void tet_geom(const double* __restrict__ V, const int32_t* __restrict__ sv, int64_t e,
+                                         TetGeom& g) {
+  for (int k = 0; k < 4; ++k)
+    for (int r = 0; r < 3; ++r) g.v[k][r] = V[3 * (int64_t)sv[4 * e + k] + r];
+  double J[9];
+  for (int c = 0; c < 3; ++c)
+    for (int r = 0; r < 3; ++r) J[3 * r + c] = g.v[c + 1][r] - g.v[0][r];
+  const double det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) +
+                     J[2] * (J[3] * J[7] - J[4] * J[6]);
+  g.gl[1][0] = (J[4] * J[8] - J[5] * J[7]) / det;
+  g.gl[1][1] = (J[2] * J[7] - J[1] * J[8]) / det;
+  g.gl[1][2] = (J[1] * J[5] - J[2] * J[4]) / det;
+  g.gl[2][0] = (J[5] * J[6] - J[3] * J[8]) / det;
+  g.gl[2][1] = (J[0] * J[8] - J[2] * J[6]) / det;
+  g.gl[2][2] = (J[2] * J[3] - J[0] * J[5]) / det;
+  g.gl[3][0] = (J[3] * J[7] - J[4] * J[6]) / det;
+  g.gl[3][1] = (J[1] * J[6] - J[0] * J[7]) / det;
+  g.gl[3][2] = (J[0] * J[4] - J[1] * J[3]) / det;
+  for (int r = 0; r < 3; ++r) g.gl[0][r] = -(g.gl[1][r] + g.gl[2][r] + g.gl[3][r]);
+  g.adet = fabs(det);
+}
+// physical value (val) and curl (cur) of basis function I at barycentrics lam
+__device__ __forceinline__ void tet_basis_eval(int p, int I, const TetGeom& g, const double lam[4], double val[3],
+                                               double cur[3]) {
+  VTerm vt[2];
+  CTerm ct[3];
+  int nv, nc;
+  basis_terms(p, I, vt, &nv, ct, &nc);
+  for (int r = 0; r < 3; ++r) val[r] = cur[r] = 0.0;
+  for (int k = 0; k < nv; ++k) {
+    const double m = vt[k].c * (vt[k].l0 >= 0 ? lam[vt[k].l0] : 1.0) * lam[vt[k].l1];
+    for (int r = 0; r < 3; ++r) val[r] += m * g.gl[vt[k].g][r];
+  }
+  for (int k = 0; k < nc; ++k) {
+    const double m = ct[k].c * (ct[k].l >= 0 ? lam[ct[k].l] : 1.0);
+    const double* a = g.gl[ct[k].u];
+    const double* b = g.gl[ct[k].v];
+    cur[0] += m * (a[1] * b[2] - a[2] * b[1]);
+    cur[1] += m * (a[2] * b[0] - a[0] * b[2]);
+    cur[2] += m * (a[0] * b[1] - a[1] * b[0]);
+  }
+}
+__device__ __forceinline__ void duffy_lam(double u, double v, double t, double lam[4]) {
+  lam[1] = u;
+  lam[2] = v * (1 - u);
+  lam[3] = t * (1 - u) * (1 - v);
+  lam[0] = 1.0 - lam[1] - lam[2] - lam[3];
+}
+
+__global__ void tet_quad_points_kernel(int64_t ne, const double* __restrict__ V, const int32_t* __restrict__ sv,
+                                       TetQuad Q, double* __restrict__ xyz) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  TetGeom g;
+  tet_geom(V, sv, e, g);
+  const int q = Q.q, q3 = q * q * q;
+  for (int ia = 0; ia < q; ++ia)
+    for (int ib = 0; ib < q; ++ib)
+      for (int ic = 0; ic < q; ++ic) {
+        double lam[4];
+        duffy_lam(Q.x[ia], Q.x[ib], Q.x[ic], lam);
+        double* out = xyz + 3 * (e * q3 + ic + q * (ib + q * ia));
+        for (int r = 0; r < 3; ++r)
+          out[r] = lam[0] * g.v[0][r] + lam[1] * g.v[1][r] + lam[2] * g.v[2][r] + lam[3] * g.v[3][r];
+      }
+}
+
+// mode 0: b = (J, w_i), J per element (per_point = 0) or per point; mode 1:
+// b = (nu curl A, w_i)
+template <int L>
+__global__ void __launch_bounds__(128) tet_field_load_kernel(int64_t ne, int p, const double* __restrict__ V,
+                                                             const int32_t* __restrict__ sv,
+                                                             const int32_t* __restrict__ edofs, TetQuad Q, int mode,
+                                                             int per_point, const double* __restrict__ src,
+                                                             const double* __restrict__ nu, double* __restrict__ b) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  TetGeom g;
+  tet_geom(V, sv, e, g);
+  double ae[L];
+  if (mode == 1) {
+    for (int i = 0; i < L; ++i) ae[i] = src[edofs[e * L + i]];
+  }
+  double be[L];
+#pragma unroll
+  for (int i = 0; i < L; ++i) be[i] = 0.0;
+  const int q = Q.q, q3 = q * q * q;
+  for (int ia = 0; ia < q; ++ia)
+    for (int ib = 0; ib < q; ++ib)
+      for (int ic = 0; ic < q; ++ic) {
+        const double u = Q.x[ia], v = Q.x[ib];
+        double lam[4];
+        duffy_lam(u, v, Q.x[ic], lam);
+        const double wq = Q.w[ia] * Q.w[ib] * Q.w[ic] * (1 - u) * (1 - u) * (1 - v) * g.adet;
+        double f[3];
+        if (mode == 0) {
+          const double* jc = per_point ? src + 3 * (e * q3 + ic + q * (ib + q * ia)) : src + 3 * e;
+          for (int r = 0; r < 3; ++r) f[r] = wq * jc[r];
+        } else {
+          double cu[3] = {0.0, 0.0, 0.0};
+          for (int I = 0; I < L; ++I) {
+            double vv[3], cc[3];
+            tet_basis_eval(p, I, g, lam, vv, cc);
+            for (int r = 0; r < 3; ++r) cu[r] += ae[I] * cc[r];
+          }
+          const double s = wq * nu[e];
+          for (int r = 0; r < 3; ++r) f[r] = s * cu[r];
+        }
+        for (int I = 0; I < L; ++I) {
+          double vv[3], cc[3];
+          tet_basis_eval(p, I, g, lam, vv, cc);
+          be[I] += f[0] * vv[0] + f[1] * vv[1] + f[2] * vv[2];
+        }
+      }
+#pragma unroll
+  for (int i = 0; i < L; ++i)
+    if (be[i] != 0.0) atomicAdd(b + edofs[e * L + i], be[i]);
+}
+
+struct TetPoints {
+  int n;
+  double xi[16][3];
+};
+template <int L>
+__global__ void tet_curl_points_kernel(int64_t ne, int p, const double* __restrict__ V, const int32_t* __restrict__ sv,
+                                       const int32_t* __restrict__ edofs, TetPoints P, const double* __restrict__ A,
+                                       double* __restrict__ B) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  TetGeom g;
+  tet_geom(V, sv, e, g);
+  double ae[L];
+  for (int i = 0; i < L; ++i) ae[i] = A[edofs[e * L + i]];
+  for (int k = 0; k < P.n; ++k) {
+    const double lam[4] = {1.0 - P.xi[k][0] - P.xi[k][1] - P.xi[k][2], P.xi[k][0], P.xi[k][1], P.xi[k][2]};
+    double cu[3] = {0.0, 0.0, 0.0};
+    for (int I = 0; I < L; ++I) {
+      double vv[3], cc[3];
+      tet_basis_eval(p, I, g, lam, vv, cc);
+      for (int r = 0; r < 3; ++r) cu[r] += ae[I] * cc[r];
+    }
+    for (int r = 0; r < 3; ++r) B[3 * (e * P.n + k) + r] = cu[r];
+  }
+}
+
+static TetQuad make_tet_quad(int q, const double* xq, const double* wq) {
+  TetQuad Q;
+  std::memset(&Q, 0, sizeof(Q));
+  Q.q = q;
+  for (int k = 0; k < 8; ++k) {
+    Q.x[k] = k < q ? xq[k] : 0.0;
+    Q.w[k] = (k < q && wq) ? wq[k] : 0.0;
+  }
+  return Q;
+}
+
+cudaError_t tet_quad_points(const hcop* h, int q, const double* xq, double* xyz, cudaStream_t s) {
+  if (!h->verts || !h->tet_sv || q < 1 || q > 8) return cudaErrorInvalidValue;
+  const TetQuad Q = make_tet_quad(q, xq, nullptr);
+  tet_quad_points_kernel<<<(unsigned)((h->ne + 127) / 128), 128, 0, s>>>(h->ne, h->verts, h->tet_sv, Q, xyz);
+  return cudaGetLastError();
+}
+
+static cudaError_t tet_field_launch(const hcop* h, int mode, int per_point, const double* src, int q,
+                                    const double* xq, const double* wq, double* b, cudaStream_t s) {
+  if (!h->verts || !h->tet_sv || q < 1 || q > 8) return cudaErrorInvalidValue;
+  const TetQuad Q = make_tet_quad(q, xq, wq);
+  cudaError_t e = cudaMemsetAsync(b, 0, h->ndof * sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  const unsigned blocks = (unsigned)((h->ne + 127) / 128);
+  if (h->p == 1)
+    tet_field_load_kernel<6><<<blocks, 128, 0, s>>>(h->ne, 1, h->verts, h->tet_sv, h->tet_edofs, Q, mode, per_point,
+                                                    src, h->nu, b);
+  else
+    tet_field_load_kernel<20><<<blocks, 128, 0, s>>>(h->ne, 2, h->verts, h->tet_sv, h->tet_edofs, Q, mode, per_point,
+                                                     src, h->nu, b);
+  return cudaGetLastError();
+}
+
+cudaError_t tet_load_field(const hcop* h, int per_point, const double* src, int q, const double* xq,
+                           const double* wq, double* b, cudaStream_t s) {
+  return tet_field_launch(h, 0, per_point, src, q, xq, wq, b, s);
+}
+
+cudaError_t tet_curl_load(const hcop* h, const double* A, int q, const double* xq, const double* wq, double* b,
+                          cudaStream_t s) {
+  if (!h->nu) return cudaErrorInvalidValue;
+  return tet_field_launch(h, 1, 0, A, q, xq, wq, b, s);
+}
+
+cudaError_t tet_curl_points(const hcop* h, const double* A, int npts, const double* xi, double* B, cudaStream_t s) {
+  if (!h->verts || !h->tet_sv || npts < 1 || npts > 16) return cudaErrorInvalidValue;
+  TetPoints P;
+  std::memset(&P, 0, sizeof(P));
+  P.n = npts;
+  for (int k = 0; k < npts; ++k)
+    for (int r = 0; r < 3; ++r) P.xi[k][r] = xi[3 * k + r];
+  const unsigned blocks = (unsigned)((h->ne + 127) / 128);
+  if (h->p == 1)
+    tet_curl_points_kernel<6><<<blocks, 128, 0, s>>>(h->ne, 1, h->verts, h->tet_sv, h->tet_edofs, P, A, B);
+  else
+    tet_curl_points_kernel<20><<<blocks, 128, 0, s>>>(h->ne, 2, h->verts, h->tet_sv, h->tet_edofs, P, A, B);
+  return cudaGetLastError();
+}
+
 cudaError_t tet_load_coil(const hcop* h, const double coil[7], int q, const double* xq, const double* wq, double* b,
                           cudaStream_t s) {
   if (!h->verts || !h->tet_sv || q < 1 || q > 8) return cudaErrorInvalidValue;

@@ -336,6 +336,72 @@ class HCurlOperator:
                                             _dev_ptr(b, "float64")), self.h)
         return b
 
+    # -- sources and fields (DivFreeSource load, CurlAuxSolver, ScaledCurlVectorGridFunctionAux) --
+    def QuadPointsDevice(self, q):
+        """Physical points of the q^3 rule the load entry points use, a
+        (ne, q^3, 3) float64 CUDA tensor (hex: kx + q (ky + q kz); tet:
+        collapsed rule, ic + q (ib + q ia))."""
+        import torch
+
+        xyz = torch.empty(self.ne, q ** 3, 3, dtype=torch.float64, device="cuda")
+        N.check(N.lib().hc_quad_points_device(self.h, int(q), _dev_ptr(xyz, "float64")), self.h)
+        return xyz
+
+    def LoadFieldDevice(self, J, b, q=None):
+        """b = (J, w_i) for a caller-supplied source: J of shape (ne, 3) (one
+        vector per element) or (ne, q^3, 3) (values at QuadPointsDevice(q))."""
+        per_point = J.dim() == 3
+        if per_point:
+            q = round(int(J.shape[1]) ** (1.0 / 3.0))
+            if q ** 3 != int(J.shape[1]):
+                raise ValueError("J must be (ne, q^3, 3)")
+        else:
+            q = int(q or self.order + 1)
+        if int(J.shape[0]) != self.ne or int(J.shape[-1]) != 3:
+            raise ValueError("J must have ne = %d rows of 3-vectors" % self.ne)
+        mode = N.HC_FIELD_QUAD if per_point else N.HC_FIELD_ELEM
+        N.check(N.lib().hc_load_field_device(self.h, mode, int(q), _dev_ptr(J, "float64"), _dev_ptr(b, "float64")),
+                self.h)
+        return b
+
+    def CurlLoadDevice(self, A, b):
+        """b_i = (nu curl A, w_i) with the operator's per-element nu."""
+        N.check(N.lib().hc_curl_load_device(self.h, _dev_ptr(A, "float64"), _dev_ptr(b, "float64")), self.h)
+        return b
+
+    def MagneticFieldDevice(self, A, H, rtol=1e-12):
+        """H = nu curl A projected into this Nedelec space (M H = (nu curl A, w),
+        Jacobi PCG); H holds the initial guess.  Returns the solve report."""
+        info = N.SolveInfo()
+        st = N.lib().hc_magnetic_field_device(self.h, _dev_ptr(A, "float64"), _dev_ptr(H, "float64"), float(rtol),
+                                              C.byref(info))
+        N.check(st, self.h)
+        return {"status": N.STATUS_NAMES[info.status], "iterations": info.iterations,
+                "rel_residual": info.rel_residual}
+
+    def TetCurlPointsDevice(self, A, xi):
+        """curl A at reference points xi (npts x 3, simplex of the sorted
+        element vertices) of every tet: (ne, npts, 3) float64 CUDA tensor."""
+        import torch
+
+        xi = np.ascontiguousarray(xi, dtype=np.float64).reshape(-1, 3)
+        B = torch.empty(self.ne, xi.shape[0], 3, dtype=torch.float64, device="cuda")
+        N.check(N.lib().hc_tet_curl_points_device(self.h, _dev_ptr(A, "float64"), int(xi.shape[0]), _ptr(xi),
+                                                  _dev_ptr(B, "float64")), self.h)
+        return B
+
+    # -- backward-Euler steps on device state --
+    def BeRhsDevice(self, f, A, b):
+        """b = P (f - C_nu A) (one step's right-hand side)."""
+        N.check(N.lib().hc_be_rhs_device(self.h, _dev_ptr(f, "float64"), _dev_ptr(A, "float64"),
+                                         _dev_ptr(b, "float64")), self.h)
+        return b
+
+    def BeUpdateDevice(self, A, dA):
+        """A += dt dA."""
+        N.check(N.lib().hc_be_update_device(self.h, _dev_ptr(A, "float64"), _dev_ptr(dA, "float64")), self.h)
+        return A
+
     # -- frequency domain: C_nu + i omega M_sigma (ComplexMaxwellOperator, eps = 0) --
     def MultComplex(self, omega, x):
         """y = J x for the eliminated complex operator, complex host vectors."""
@@ -437,6 +503,25 @@ class GpuHCurlPCGSolver:
         self._check(st)
         out = []
         for i in infos:
+            self.info = i
+            out.append(self.result)
+        return out
+
+    def StepsDevice(self, f, A, dA, b, nsteps):
+        """nsteps backward-Euler steps on device state (hc_be_steps_device):
+        per step b = P (f - C_nu A), dA = 0, solve J dA = b with these
+        options, A += dt dA.  A is updated in place; returns the per-step
+        result dicts of the steps taken (the last one is the first non-OK)."""
+        op = self.op
+        infos = (N.SolveInfo * int(nsteps))()
+        st = N.lib().hc_be_steps_device(op.h, C.byref(self.p), int(nsteps), _dev_ptr(f, "float64"),
+                                        _dev_ptr(A, "float64"), _dev_ptr(dA, "float64"), _dev_ptr(b, "float64"),
+                                        infos)
+        self._check(st)
+        out = []
+        for i in infos:
+            if i.status < 0:
+                break
             self.info = i
             out.append(self.result)
         return out

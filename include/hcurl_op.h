@@ -281,6 +281,62 @@ hc_status hc_solve_complex_batch(int32_t n, hcop_t* const* hs, const hc_solve_pa
                                  const double* const* br, const double* const* bi, double* const* xr,
                                  double* const* xi, hc_solve_info* info);
 
+/* ---- sources and fields around the solve ----------------------------------- */
+/* Points of the q^3 rule the load entry points integrate with (1 <= q <= 8):
+ * HC_HEX the tensor Gauss-Legendre rule per element, point kx + q (ky + q kz);
+ * HC_TET the collapsed (Duffy) Gauss-Legendre rule, point ic + q (ib + q ia)
+ * with barycentrics l1 = u_ia, l2 = u_ib (1 - l1), l3 = u_ic (1 - l1 - l2) on
+ * the element's vertices sorted by global id.  xyz: n_elem * q^3 * 3 device
+ * doubles, physical coordinates.                                            */
+hc_status hc_quad_points_device(hcop_t* h, int q, double* xyz);
+/* b = (J, w_i) for a source J the caller supplies (VectorFEDomainLFIntegrator
+ * of DivFreeSource::Apply, src/sources/div_free_source.cpp:77-80):
+ *   HC_FIELD_ELEM: J holds one vector per element (n_elem * 3), constant there;
+ *   HC_FIELD_QUAD: J holds the vector at every point of hc_quad_points_device
+ *                  (n_elem * q^3 * 3), integrated with that rule.
+ * Device pointers; b is overwritten.                                        */
+enum { HC_FIELD_ELEM = 0, HC_FIELD_QUAD = 1 };
+hc_status hc_load_field_device(hcop_t* h, int mode, int q, const double* J, double* b);
+/* Right-hand side of ScaledCurlVectorGridFunctionAux's projection of
+ * H = nu curl A into this Nedelec space, b_i = (nu curl A, w_i), with the
+ * handle's per-element nu (MixedVectorCurlIntegrator(nu),
+ * src/auxsolvers/scaled_curl_vector_gridfunction_aux.cpp:21-27).  Device.   */
+hc_status hc_curl_load_device(hcop_t* h, const double* A, double* b);
+/* H = nu curl A projected into this Nedelec space: solves M H = b with the
+ * unit-coefficient Nedelec mass M (no essential dofs) by Jacobi PCG to rtol,
+ * as ScaledVectorGridFunctionAux::Solve does
+ * (src/auxsolvers/scaled_vector_gridfunction_aux.cpp:73-99; the reference
+ * registers H = nu curl A this way, src/formulations/HCurl/a_formulation.cpp:78-86).
+ * The mass operator is built on the first call and kept by the handle.
+ * Device pointers; H holds the initial guess.                               */
+hc_status hc_magnetic_field_device(hcop_t* h, const double* A, double* H, double rtol, hc_solve_info* info);
+/* B = curl A at npts reference points xi (npts * 3, coordinates in the
+ * simplex of the element's vertices sorted by global id: x = v0 + sum_k
+ * xi_k (v_k - v0)) of every tet: B is n_elem * npts * 3 physical values
+ * (CurlAuxSolver's field, src/auxsolvers/curl_aux.cpp:25-30, sampled
+ * pointwise).  Tet meshes; device pointers for A and B, host xi.            */
+hc_status hc_tet_curl_points_device(hcop_t* h, const double* A, int npts, const double* xi, double* B);
+
+/* ---- backward-Euler time stepping on device state -------------------------- */
+/* b = P (f - C_nu A): one step's right-hand side, the source load f plus
+ * WeakCurlCurlKernel's -C_nu A_n (src/kernels/weak_curl_curl_kernel.cpp:27-31),
+ * essential rows set to zero (homogeneous A x n = 0, as FormLinearSystem
+ * leaves them).  Structured hex grids; device pointers.                    */
+hc_status hc_be_rhs_device(hcop_t* h, const double* f, const double* A, double* b);
+/* A += dt dA: BackwardEulerSolver's update of the state
+ * (src/problem_builders/time_domain_problem_builder.cpp:59-64).  Device.    */
+hc_status hc_be_update_device(hcop_t* h, double* A, const double* dA);
+/* nsteps backward-Euler steps of TimeDomainEquationSystemProblemOperator::
+ * ImplicitSolve (time_domain_equation_system_problem_operator.cpp:31-51):
+ * per step b = P (f - C_nu A), dA = 0, solve J dA = b with prm, A += dt dA.
+ * f, A, dA, b are device vectors (A is the state, updated in place; dA and
+ * b are work vectors that hold the last step's values on return).  info
+ * (nsteps entries) receives one report per step taken, status -1 for steps
+ * not taken; the loop stops at the first step whose solve is not HC_OK and
+ * returns its status.  Structured hex grids.                               */
+hc_status hc_be_steps_device(hcop_t* h, const hc_solve_params* prm, int32_t nsteps, const double* f, double* A,
+                             double* dA, double* b, hc_solve_info* info);
+
 /* ---- linear solve --------------------------------------------------------- */
 /* Solve J x = b for x (x holds the initial guess on entry).  Replaces the
  * HyprePCG solve of HCurlFormulation::ConstructJacobianSolver

@@ -51,6 +51,9 @@ def lib():
             "orc_cheb_apply": (None, [vp, i32, dbl, dbl, vp, vp, i32]),
             "orc_load_coil": (None, [vp, dbl, dbl, dbl, dbl, dbl, dbl, dbl, i32, vp]),
             "orc_load_mms": (None, [vp, dbl, dbl, i32, vp]),
+            "orc_load_elem_field": (None, [vp, vp, i32, vp]),
+            "orc_load_affine": (None, [vp, vp, vp, i32, vp]),
+            "orc_curl_load": (None, [vp, vp, vp, i32, vp]),
             "orc_l2err_mms": (dbl, [vp, vp, dbl, i32]),
             "orc_eval": (None, [vp, vp, i64, vp, vp, vp]),
         }
@@ -192,6 +195,26 @@ class Problem:
     def load_coil(self, I0=1.0, xc=0.5, yc=0.5, r0=0.2, r1=0.35, z0=0.3, z1=0.7, q=None):
         b = np.empty(self.ndof)
         lib().orc_load_coil(self.h, I0, xc, yc, r0, r1, z0, z1, q or 4, _p(b))
+        return b
+
+    def load_elem_field(self, J, q=4):
+        J = np.ascontiguousarray(J, dtype=np.float64)
+        b = np.empty(self.ndof)
+        lib().orc_load_elem_field(self.h, _p(J), q, _p(b))
+        return b
+
+    def load_affine(self, a, B, q=4):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        B = np.ascontiguousarray(B, dtype=np.float64)
+        b = np.empty(self.ndof)
+        lib().orc_load_affine(self.h, _p(a), _p(B), q, _p(b))
+        return b
+
+    def curl_load(self, nu, A, q=6):
+        nu = np.ascontiguousarray(nu, dtype=np.float64)
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        b = np.empty(self.ndof)
+        lib().orc_curl_load(self.h, _p(nu), _p(A), q, _p(b))
         return b
 
     def load_mms(self, t, var_scale=0.5, q=6):

@@ -1088,6 +1088,59 @@ void orc_load_coil(void* h, double I0, double xc, double yc, double r0, double r
 void orc_load_mms(void* h, double t, double s, int q, double* b) {
   load_generic(*static_cast<Prob*>(h), q, [=](const double* x, double* f) { mms_source(x, t, s, f); }, b);
 }
+// b_i = (J, w_i) for a source constant on each element (J: ne x 3), the
+// VectorFEDomainLFIntegrator load of DivFreeSource::Apply
+// (src/sources/div_free_source.cpp:77-80) for an element-wise source.
+void orc_load_elem_field(void* h, const double* J, int q, double* b) {
+  Prob& P = *static_cast<Prob*>(h);
+  std::vector<double> xi, w;
+  P.ref_quad(q, xi, w);
+  const int L = P.L;
+  std::vector<double> val(L * 3), cu(L * 3);
+  std::fill(b, b + P.ndof, 0.0);
+  for (i64 e = 0; e < P.ne; ++e)
+    for (size_t k = 0; k < w.size(); ++k) {
+      double x[3], ad;
+      P.eval_phys(e, &xi[3 * k], x, &ad, val.data(), cu.data());
+      const double* f = J + 3 * e;
+      const double wq = w[k] * ad;
+      for (int i = 0; i < L; ++i)
+        b[P.edofs[e * L + i]] += wq * (f[0] * val[3 * i] + f[1] * val[3 * i + 1] + f[2] * val[3 * i + 2]);
+    }
+}
+// b_i = (J, w_i) for the affine source J(x) = a + B x (B row-major 3x3).
+void orc_load_affine(void* h, const double* a, const double* B, int q, double* b) {
+  const double a0 = a[0], a1 = a[1], a2 = a[2];
+  double Bm[9];
+  std::memcpy(Bm, B, sizeof(Bm));
+  load_generic(*static_cast<Prob*>(h), q,
+               [=](const double* x, double* f) {
+                 const double aa[3] = {a0, a1, a2};
+                 for (int r = 0; r < 3; ++r) f[r] = aa[r] + Bm[3 * r] * x[0] + Bm[3 * r + 1] * x[1] + Bm[3 * r + 2] * x[2];
+               },
+               b);
+}
+// b_i = (nu curl A, w_i) with nu constant per element: the right-hand side of
+// ScaledCurlVectorGridFunctionAux's projection (MixedVectorCurlIntegrator(nu),
+// src/auxsolvers/scaled_curl_vector_gridfunction_aux.cpp:21-27), by quadrature.
+void orc_curl_load(void* h, const double* nu, const double* A, int q, double* b) {
+  Prob& P = *static_cast<Prob*>(h);
+  std::vector<double> xi, w;
+  P.ref_quad(q, xi, w);
+  const int L = P.L;
+  std::vector<double> val(L * 3), cu(L * 3);
+  std::fill(b, b + P.ndof, 0.0);
+  for (i64 e = 0; e < P.ne; ++e)
+    for (size_t k = 0; k < w.size(); ++k) {
+      double x[3], ad, c[3] = {0, 0, 0};
+      P.eval_phys(e, &xi[3 * k], x, &ad, val.data(), cu.data());
+      for (int i = 0; i < L; ++i)
+        for (int r = 0; r < 3; ++r) c[r] += A[P.edofs[e * L + i]] * cu[3 * i + r];
+      const double wq = w[k] * ad * nu[e];
+      for (int i = 0; i < L; ++i)
+        b[P.edofs[e * L + i]] += wq * (c[0] * val[3 * i] + c[1] * val[3 * i + 1] + c[2] * val[3 * i + 2]);
+    }
+}
 double orc_l2err_mms(void* h, const double* A, double t, int q) {
   Prob& P = *static_cast<Prob*>(h);
   std::vector<double> xi, w;

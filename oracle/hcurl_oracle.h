@@ -108,6 +108,12 @@ void    orc_cheb_apply(void* h, int degree, double lmax, double ratio, const dou
  * with q points per direction per hex (or q^3 collapsed points per tet).    */
 void    orc_load_coil(void* h, double I0, double xc, double yc, double r0, double r1, double z0,
                       double z1, int q, double* b);
+/* b_i = (J, w_i) for J constant per element (ne x 3), and for the affine
+ * J(x) = a + B x (B row-major 3x3); the same q-point rules as orc_load_coil. */
+void    orc_load_elem_field(void* h, const double* J, int q, double* b);
+void    orc_load_affine(void* h, const double* a, const double* B, int q, double* b);
+/* b_i = (nu curl A, w_i), nu constant per element (ne values).             */
+void    orc_curl_load(void* h, const double* nu, const double* A, int q, double* b);
 /* Source of test_aform_source.cpp:39-49 at time t.                          */
 void    orc_load_mms(void* h, double t, double var_scale, int q, double* b);
 /* L2 norm of (A_h - A_exact(t)), A_exact = t sin(pi y) sin(pi z) e_x.     */

@@ -14,7 +14,9 @@ import numpy as np
 sys.path.insert(0, os.path.join(os.path.dirname(__file__), "..", ".."))
 from hephaestus_gb300.meshes import read_mfem_tet_mesh  # noqa: E402
 
-src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/data/beam-tet.mesh"
+if len(sys.argv) != 2:
+    sys.exit("usage: python tests/golden/make_beam_tet.py <reference checkout>/data/beam-tet.mesh")
+src = sys.argv[1]
 verts, tets, btris, battr, eattr = read_mfem_tet_mesh(src)
 out = os.path.join(os.path.dirname(__file__), "beam_tet.npz")
 np.savez(out, verts=verts, tets=tets, btris=btris, battr=battr, eattr=eattr)

@@ -70,6 +70,15 @@ def test_null_arguments_return_einval():
     assert L.hc_num_dofs(None) == -1
     assert L.hc_last_error(None, None, 0) == N.HC_EINVAL
     L.hc_destroy(None)  # no-op
+    # sources, fields and time stepping
+    assert L.hc_quad_points_device(None, 2, None) == N.HC_EINVAL
+    assert L.hc_load_field_device(None, N.HC_FIELD_ELEM, 2, None, None) == N.HC_EINVAL
+    assert L.hc_curl_load_device(None, None, None) == N.HC_EINVAL
+    assert L.hc_magnetic_field_device(None, None, None, 1e-12, None) == N.HC_EINVAL
+    assert L.hc_tet_curl_points_device(None, None, 1, None, None) == N.HC_EINVAL
+    assert L.hc_be_rhs_device(None, None, None, None) == N.HC_EINVAL
+    assert L.hc_be_update_device(None, None, None) == N.HC_EINVAL
+    assert L.hc_be_steps_device(None, None, 1, None, None, None, None, None) == N.HC_EINVAL
 
 
 def test_mfem_shim_compiles_against_stub():

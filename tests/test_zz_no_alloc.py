@@ -35,6 +35,61 @@ def test_curl_static_matches_curl_twice(nx, ny, nz, p):
         assert np.abs(B - ref).max() <= 1e-13 * scale, call
 
 
+def _cudart():
+    """The CUDA runtime as a shared library (the device's default memory pool
+    is one per device, shared by every runtime instance in the process)."""
+    import os
+
+    for name in ("libcudart.so", "libcudart.so.13", "/usr/local/cuda/lib64/libcudart.so"):
+        try:
+            return C.CDLL(name)
+        except OSError:
+            continue
+    cuda_home = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    return C.CDLL(os.path.join(cuda_home, "lib64", "libcudart.so"))
+
+
+def test_curl_static_allocates_nothing_in_the_call():
+    """After the first call (which looks the static area up), a call leaves
+    the default pool's used-memory high-water mark and the device's free
+    memory unchanged: the library's per-handle work memory is stream-ordered
+    from that pool, so a per-call allocation would raise the high-water mark
+    even if it were freed again inside the call."""
+    import torch
+
+    cr = _cudart()
+    USED_CURRENT, USED_HIGH = 7, 8  # cudaMemPoolAttrUsedMemCurrent / UsedMemHigh (driver_types.h)
+    nx = ny = nz = 12
+    op = HCurlOperator(nx, ny, nz, 2, np.ones(nx * ny * nz), None, ess_attr_bits=0)
+    L = N.lib()
+    nrt = L.hc_num_rt_dofs(op.h)
+    A = np.random.default_rng(3).standard_normal(op.ndof)
+    B = np.empty(nrt)
+    N.check(L.hc_curl_static(op.h, _p(A), _p(B)), op.h)  # set-up call
+    torch.cuda.synchronize()
+    dev = C.c_int(0)
+    assert cr.cudaGetDevice(C.byref(dev)) == 0
+    pool = C.c_void_p()
+    assert cr.cudaDeviceGetDefaultMemPool(C.byref(pool), dev) == 0
+
+    def attr(a):
+        v = C.c_uint64(0)
+        assert cr.cudaMemPoolGetAttribute(pool, a, C.byref(v)) == 0
+        return v.value
+
+    zero = C.c_uint64(0)
+    assert cr.cudaMemPoolSetAttribute(pool, USED_HIGH, C.byref(zero)) == 0  # reset the mark to the current use
+    used0, high0 = attr(USED_CURRENT), attr(USED_HIGH)
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(2):
+        N.check(L.hc_curl_static(op.h, _p(A), _p(B)), op.h)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert attr(USED_CURRENT) == used0
+    assert attr(USED_HIGH) == high0
+    assert free1 == free0
+
+
 def test_curl_static_rejects_grids_beyond_the_scratch():
     n, p = 48, 2   # 3 * 97 * 96 * 96 = 2,681,856 RT dofs > 2^20
     op = HCurlOperator(n, n, n, p, np.ones(n ** 3), None, ess_attr_bits=0)
