@@ -134,6 +134,16 @@ _SIGS = {
     "hc_solve_multi": (C.c_int, [C.c_void_p, C.POINTER(SolveParams), C.c_int32, C.c_void_p, C.c_void_p,
                                  C.POINTER(SolveInfo)]),
     "hc_load_coil": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    "hc_hex_elem_dofs": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
+    "hc_tet_elem_dofs": (C.c_int, [C.c_int32, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]),
+    "hc_dofmap_create": (C.c_int, [C.c_int64, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p,
+                                   C.POINTER(C.c_void_p)]),
+    "hc_dofmap_to_lib": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hc_dofmap_from_lib": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hc_dofmap_ess_mask": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "hc_dofmap_size": (C.c_int64, [C.c_void_p]),
+    "hc_dofmap_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
+    "hc_dofmap_destroy": (None, [C.c_void_p]),
     "hc_quad_points_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "hc_load_field_device": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     "hc_curl_load_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),

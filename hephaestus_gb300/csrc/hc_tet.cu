@@ -493,6 +493,182 @@ __global__ void __launch_bounds__(256, 3) tet_apply_tiles20(int64_t ne, const in
   }
 }
 
+// ---- tensor-core form: order 2, 16 right-hand sides, BF16 element matrices ----------------
+// One warp per element and step: Y_e^T (16 x 20) = X_e^T (16 x 20) K_e^T with
+// mma.sync m16n8k16 + m16n8k8 (BF16 operands, FP32 accumulation): M = the 16
+// right-hand sides, K = the element's 20 dofs (16 + 8, the last 4 zero), N =
+// its 20 output rows (three tiles of 8).  The B fragments are read straight
+// from the BF16 element matrix in HBM (32-bit loads, every entry once); the A
+// fragments come from the element's X rows staged in shared memory, split
+// into BF16 hi + lo parts (two MMAs) so that the result carries the rounding
+// of the BF16 matrix alone.  Y_e goes through shared memory to 128-bit atomic
+// adds, one per 4 columns of a row.  Staging is the cp.async pipeline of
+// tet_apply_tiles20: X rows of the next element and dof indices of the one
+// after land while the current element computes.
+constexpr int kTcW = 8;    // warps per block
+constexpr int kTcXS = 20;  // row stride (floats) of the staged blocks: conflict-free fragment reads
+
+__device__ __forceinline__ void split_bf16(float v0, float v1, uint32_t& hi, uint32_t& lo) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);  // .x (low half) = v0
+  const __nv_bfloat162 l = __floats2bfloat162_rn(v0 - __low2float(h), v1 - __high2float(h));
+  hi = *reinterpret_cast<const uint32_t*>(&h);
+  lo = *reinterpret_cast<const uint32_t*>(&l);
+}
+__device__ __forceinline__ void mma_16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+__device__ __forceinline__ void mma_1688(float (&d)[4], const uint32_t (&a)[2], uint32_t b0) {
+  asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5}, {%6}, {%0,%1,%2,%3};\n"
+               : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+               : "r"(a[0]), "r"(a[1]), "r"(b0));
+}
+
+__global__ void __launch_bounds__(32 * kTcW) tet_apply_mma16(int64_t ne, const int32_t* __restrict__ edofs,
+                                                             const __nv_bfloat16* __restrict__ K,
+                                                             const uint8_t* __restrict__ ess, int masked, float scale,
+                                                             const float* __restrict__ x, float* __restrict__ y,
+                                                             const int* done) {
+  if (done && *done) return;
+  constexpr int L = 20, R = 16;
+  __shared__ __align__(16) float xs_all[kTcW][2][L][kTcXS];  // X rows: [dof j][rhs r]
+  __shared__ __align__(16) float ds_all[kTcW][L][kTcXS];     // Y_e rows for the scatter
+  __shared__ __align__(16) int sdof_all[kTcW][3][L];
+  __shared__ unsigned char sess_all[kTcW][3][L];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane >> 2, tig = lane & 3;
+  const int64_t wstride = (int64_t)gridDim.x * kTcW;
+  const int64_t first = (int64_t)blockIdx.x * kTcW + wid;
+  if (first >= ne) return;  // uniform over the warp: warps share no state
+
+  auto copy_dofs = [&](int64_t e, int ds) {
+    if (e < ne && lane < L) cp_async4(&sdof_all[wid][ds][lane], edofs + e * L + lane);
+  };
+  auto copy_x = [&](int64_t e, int ds, int xb) {  // 20 rows x 4 chunks of 16 bytes
+    if (e >= ne) return;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int q = lane + 32 * k;
+      if (q < 4 * L) {
+        const int j = q >> 2, c4 = q & 3;
+        cp_async16(&xs_all[wid][xb][j][4 * c4], x + (int64_t)sdof_all[wid][ds][j] * R + 4 * c4);
+      }
+    }
+  };
+  auto mask_rows = [&](int64_t e, int ds, int xb) {  // after the copies landed
+    if (e >= ne) return;
+    unsigned char f[3] = {0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int q = lane + 32 * k;
+      if (q < 4 * L && masked) f[k] = ess[sdof_all[wid][ds][q >> 2]];
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int q = lane + 32 * k;
+      if (q < 4 * L) {
+        const int j = q >> 2, c4 = q & 3;
+        if (f[k]) *reinterpret_cast<float4*>(&xs_all[wid][xb][j][4 * c4]) = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (c4 == 0) sess_all[wid][ds][j] = f[k];
+      }
+    }
+  };
+
+  copy_dofs(first, 0);
+  copy_dofs(first + wstride, 1);
+  cp_async_commit_wait();
+  __syncwarp();
+  copy_x(first, 0, 0);
+  cp_async_commit_wait();
+  __syncwarp();
+  mask_rows(first, 0, 0);
+  __syncwarp();
+  int it = 0;
+  for (int64_t e = first; e < ne; e += wstride, ++it) {
+    const int d0 = it % 3, d1 = (it + 1) % 3, d2 = (it + 2) % 3, xb = it & 1;
+    copy_x(e + wstride, d1, xb ^ 1);
+    copy_dofs(e + 2 * wstride, d2);
+    const float* xs = &xs_all[wid][xb][0][0];
+    // A fragments: A[r][j] = X[dof j][r]; k16 over j < 16, k8 over 16 <= j < 24 (j >= 20 zero)
+    uint32_t ah[4], al[4], bh[2] = {0u, 0u}, bl[2] = {0u, 0u};
+    split_bf16(xs[(2 * tig) * kTcXS + g], xs[(2 * tig + 1) * kTcXS + g], ah[0], al[0]);
+    split_bf16(xs[(2 * tig) * kTcXS + g + 8], xs[(2 * tig + 1) * kTcXS + g + 8], ah[1], al[1]);
+    split_bf16(xs[(2 * tig + 8) * kTcXS + g], xs[(2 * tig + 9) * kTcXS + g], ah[2], al[2]);
+    split_bf16(xs[(2 * tig + 8) * kTcXS + g + 8], xs[(2 * tig + 9) * kTcXS + g + 8], ah[3], al[3]);
+    if (tig < 2) {
+      split_bf16(xs[(16 + 2 * tig) * kTcXS + g], xs[(17 + 2 * tig) * kTcXS + g], bh[0], bl[0]);
+      split_bf16(xs[(16 + 2 * tig) * kTcXS + g + 8], xs[(17 + 2 * tig) * kTcXS + g + 8], bh[1], bl[1]);
+    }
+    const uint32_t* Ke = reinterpret_cast<const uint32_t*>(K + e * (L * L));  // 200 words, 4-byte aligned
+    float acc[3][4];
+#pragma unroll
+    for (int nt = 0; nt < 3; ++nt) {
+      acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+      const int row = 8 * nt + g;  // output row i = B column n
+      uint32_t b0 = 0u, b1 = 0u, b2 = 0u;
+      if (row < L) {
+        const uint32_t* Kr = Ke + row * (L / 2);  // B[j][i] = K_e[i][j]: pairs along j
+        b0 = __ldg(Kr + tig);                     // j = 2 tig, 2 tig + 1
+        b1 = __ldg(Kr + 4 + tig);                 // j = 2 tig + 8, + 9
+        if (tig < 2) b2 = __ldg(Kr + 8 + tig);    // j = 16 + 2 tig, + 1
+      }
+      mma_16816(acc[nt], ah, b0, b1);
+      mma_16816(acc[nt], al, b0, b1);
+      mma_1688(acc[nt], bh, b2);
+      mma_1688(acc[nt], bl, b2);
+    }
+    // D[r][i] = Y_e[i][r]: rows r = g, g + 8; columns i = 8 nt + 2 tig, + 1
+    float* ds = &ds_all[wid][0][0];
+#pragma unroll
+    for (int nt = 0; nt < 3; ++nt) {
+      const int i0 = 8 * nt + 2 * tig;
+      if (i0 < L) {
+        ds[i0 * kTcXS + g] = acc[nt][0];
+        ds[(i0 + 1) * kTcXS + g] = acc[nt][1];
+        ds[i0 * kTcXS + g + 8] = acc[nt][2];
+        ds[(i0 + 1) * kTcXS + g + 8] = acc[nt][3];
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int q = lane + 32 * k;
+      if (q < 4 * L) {
+        const int j = q >> 2, c4 = q & 3;
+        if (!sess_all[wid][d0][j]) {
+          const float4 v = *reinterpret_cast<const float4*>(&ds[j * kTcXS + 4 * c4]);
+          atomicAdd(reinterpret_cast<float4*>(y + (int64_t)sdof_all[wid][d0][j] * R) + c4,
+                    make_float4(scale * v.x, scale * v.y, scale * v.z, scale * v.w));
+        }
+      }
+    }
+    cp_async_commit_wait();  // X rows of the next element, dofs of the one after
+    __syncwarp();
+    mask_rows(e + wstride, d1, xb ^ 1);
+    __syncwarp();  // flags and rows visible; this element's buffers free
+  }
+}
+
+static bool tet_mma16_launch(const hcop* h, const __nv_bfloat16* K, const float* x, float* y, int nrhs, bool masked,
+                             float scale, const int* done, cudaStream_t s) {
+  if (h->p != 2 || nrhs != 16 || ((uintptr_t)x | (uintptr_t)y) % 16 != 0) return false;
+  static int resident = 0;  // blocks resident on the device: warps stride over the elements
+  if (!resident) {
+    int dev = 0, nsm = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, tet_apply_mma16, 32 * kTcW, 0);
+    resident = std::max(1, occ) * std::max(1, nsm);
+  }
+  const int64_t b = (h->ne + kTcW - 1) / kTcW;
+  const unsigned blocks = (unsigned)std::min<int64_t>(b, resident);
+  tet_apply_mma16<<<blocks, 32 * kTcW, 0, s>>>(h->ne, h->tet_edofs, K, h->ess, masked ? 1 : 0, scale, x, y, done);
+  return true;
+}
+
 template <typename TK>
 static bool tet_tiles20_launch(const hcop* h, const TK* K, const float* x, float* y, int nrhs, bool masked,
                                float scale, const int* done, cudaStream_t s) {
@@ -565,6 +741,7 @@ template cudaError_t tet_apply_launch<float>(const hcop*, const float*, const fl
 cudaError_t tet_apply_launch_bf16(const hcop* h, const float* x, float* y, int nrhs, bool masked, cudaStream_t s) {
   const __nv_bfloat16* K = static_cast<const __nv_bfloat16*>(h->tetK16);
   if (h->p == 1) return tet_rows_launch<float, 6, __nv_bfloat16>(h, K, x, y, nrhs, masked, 1.0f, nullptr, s);
+  if (tet_mma16_launch(h, K, x, y, nrhs, masked, 1.0f, nullptr, s)) return cudaGetLastError();
   if (tet_tiles20_launch<__nv_bfloat16>(h, K, x, y, nrhs, masked, 1.0f, nullptr, s)) return cudaGetLastError();
   return tet_rows_launch<float, 20, __nv_bfloat16>(h, K, x, y, nrhs, masked, 1.0f, nullptr, s);
 }

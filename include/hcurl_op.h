@@ -337,6 +337,41 @@ hc_status hc_be_update_device(hcop_t* h, double* A, const double* dA);
 hc_status hc_be_steps_device(hcop_t* h, const hc_solve_params* prm, int32_t nsteps, const double* f, double* A,
                              double* dA, double* b, hc_solve_info* info);
 
+/* ---- dof correspondence with a caller's numbering (the MFEM shim) ------------
+ * The reference passes vectors in MFEM's true-dof numbering of its ND space
+ * (EquationSystem::FormLinearSystem / Mult, equation_system.cpp:117-210).
+ * Where the caller's local basis on each element is this library's -- MFEM's
+ * default ND hex basis read in MFEM's lexicographic element order, and the
+ * order-1 (Whitney) tet basis -- the numberings differ by a signed
+ * permutation, built here from both sides' element dof lists.  Host code: no
+ * device is needed.                                                          */
+typedef struct hc_dofmap hc_dofmap_t;
+/* This library's dofs of every element of a structured hex grid in the
+ * lexicographic local order (x-component dofs (p, p+1, p+1) x fastest, then
+ * y, then z): n_elem * 3 p (p+1)^2 entries, elements x fastest.            */
+hc_status hc_hex_elem_dofs(int32_t order, int32_t nx, int32_t ny, int32_t nz, int64_t* out);
+/* This library's dofs of every tet (order 1: the 6 edges (01,02,03,12,13,23)
+ * of the element's vertices sorted by global id; order 2: 20 dofs) and the
+ * dof count; numbering as hc_create gives a tet mesh.                       */
+hc_status hc_tet_elem_dofs(int32_t order, int64_t n_vert, int64_t n_elem, const int64_t* elem_verts, int64_t* out,
+                           int64_t* n_dof);
+/* Map from element dof lists: lib_elem_dofs from the calls above,
+ * caller_elem_dofs the caller's global dof of the same element and local
+ * function (MFEM's encoding: d for +, -1 - d when the element's function is
+ * minus the global one).  Fails (HC_EINVAL, reason in hc_dofmap_last_error)
+ * unless the correspondence is one to one with one sign per dof.            */
+hc_status hc_dofmap_create(int64_t n_dof, int64_t n_elem, int32_t ldofs, const int64_t* lib_elem_dofs,
+                           const int32_t* caller_elem_dofs, hc_dofmap_t** out);
+/* x_lib = S P x_caller, x_caller = (S P)^T x_lib (host vectors, not aliased) */
+hc_status hc_dofmap_to_lib(const hc_dofmap_t* m, const double* x_caller, double* x_lib);
+hc_status hc_dofmap_from_lib(const hc_dofmap_t* m, const double* x_lib, double* x_caller);
+/* ess_mask (library numbering, n_dof bytes) from the caller's ess_tdof_list
+ * (GetEssentialTrueDofs, boundary_conditions.cpp:32-51).                    */
+hc_status hc_dofmap_ess_mask(const hc_dofmap_t* m, int64_t n_ess, const int32_t* ess_tdofs, uint8_t* mask);
+int64_t hc_dofmap_size(const hc_dofmap_t* m);
+hc_status hc_dofmap_last_error(char* buf, size_t n);
+void hc_dofmap_destroy(hc_dofmap_t* m);
+
 /* ---- linear solve --------------------------------------------------------- */
 /* Solve J x = b for x (x holds the initial guess on entry).  Replaces the
  * HyprePCG solve of HCurlFormulation::ConstructJacobianSolver

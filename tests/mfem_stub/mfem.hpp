@@ -40,6 +40,47 @@ private:
   int h_, w_;
   std::vector<double> d_;
 };
+template <typename T>
+class Array {
+public:
+  int Size() const { return (int)d_.size(); }
+  void SetSize(int n) { d_.resize(n); }
+  T& operator[](int i) { return d_[i]; }
+  const T& operator[](int i) const { return d_[i]; }
+
+private:
+  std::vector<T> d_;
+};
+struct Geometry {
+  enum Type { TETRAHEDRON = 4 };
+  template <int G>
+  struct Constants;
+};
+template <>
+struct Geometry::Constants<Geometry::TETRAHEDRON> {
+  static constexpr int Edges[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+};
+class FiniteElement {
+public:
+  virtual ~FiniteElement() = default;
+};
+class VectorTensorFiniteElement : public FiniteElement {
+public:
+  const Array<int>& GetDofMap() const { return dof_map_; }
+
+private:
+  Array<int> dof_map_;
+};
+class FiniteElementSpace {
+public:
+  int GetNE() const { return 0; }
+  void GetElementDofs(int, Array<int>& dofs) const { dofs.SetSize(0); }
+  const FiniteElement* GetFE(int) const { return nullptr; }
+};
+class Mesh {
+public:
+  void GetElementVertices(int, Array<int>& v) const { v.SetSize(4); }
+};
 class Operator {
 public:
   virtual ~Operator() = default;

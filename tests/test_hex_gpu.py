@@ -100,6 +100,47 @@ def test_curl_of_gradient_vanishes_on_device(p):
     assert np.linalg.norm(y) < 1e-11 * np.linalg.norm(g) * np.abs(op._nu).max() * 10
 
 
+@pytest.mark.parametrize("p", [1, 2])
+def test_apply_parity_across_block_boundaries(p):
+    """A grid whose apply spans several thread blocks in x (> 32 elements), y
+    and z, so that dofs shared between blocks are combined across them:
+    masked and unmasked forms, overwrite (y = J x) and accumulate
+    (y += P K P x) forms, FP64 and FP32, against the oracle."""
+    import torch
+
+    nx, ny, nz = 37, 9, 11
+    rng = np.random.default_rng(11)
+    ne = nx * ny * nz
+    nu = meshes.loguniform(ne, 1.0, 1e3, rng)
+    sigma = meshes.loguniform(ne, 1e-2, 1e6, rng)
+    op = HCurlOperator(nx, ny, nz, p, nu, sigma, dt=0.01, ess_attr_bits=0x2D)
+    ref = oracle.Problem.hex(nx, ny, nz, p)
+    ref.set_coef(0.01 * nu, sigma)
+    ref.assemble()
+    ref.set_ess(op.ess_mask())
+    x = rng.standard_normal(op.ndof)
+    yf = ref.apply(x)
+    assert np.linalg.norm(op.ApplyForm(x) - yf) / np.linalg.norm(yf) < TOL64
+    ym = ref.apply_masked(x)
+    assert np.linalg.norm(op.Mult(x) - ym) / np.linalg.norm(ym) < TOL64
+    free = op.ess_mask() == 0
+    for dt in (torch.float64, torch.float32):
+        xd = torch.tensor(x, dtype=dt, device="cuda")
+        yd = torch.empty_like(xd)
+        op.MultDevice(xd, yd)
+        y0 = rng.standard_normal(op.ndof)
+        ya = torch.tensor(y0, dtype=dt, device="cuda")
+        op.AddMultDevice(xd, ya)  # y0 + P K P x on free rows, y0 on essential rows
+        torch.cuda.synchronize()
+        tol = TOL64 if dt == torch.float64 else TOL32
+        xr = x if dt == torch.float64 else x.astype(np.float32).astype(np.float64)
+        want = ref.apply_masked(xr)
+        assert np.linalg.norm(yd.double().cpu().numpy() - want) / np.linalg.norm(want) < tol
+        want_add = y0 + np.where(free, want, 0.0)
+        got = ya.double().cpu().numpy()
+        assert np.linalg.norm(got - want_add) / np.linalg.norm(want_add) < tol
+
+
 def test_symmetry_and_linearity_fp64():
     op, _, rng = _pair(6, 2)
     x, z = rng.standard_normal(op.ndof), rng.standard_normal(op.ndof)
