@@ -402,7 +402,7 @@ def run_ours(args):
 
 
 XERR_BAR = 1e-10          # ||x - x_FP64|| / ||x_FP64|| every credited solve must meet
-RTOL_LADDER = (1e-10, 1e-11, 1e-12, 1e-13)
+RTOL_LADDER = (1e-10, 1e-11, 1e-12, 1e-13, 5e-14)
 
 
 def _true_relres(op, b, x, cols=False):
@@ -450,16 +450,20 @@ def _fp64_truth(solve, apply, b, steps=3):
 
 def _arm_at_bar(solve, truth_err, ladder):
     """Loosest tolerance of the ladder at which one (untimed) solve meets the
-    accuracy bar against the FP64 truth; (rtol, x-err, report) or the
-    tightest tried when none meets it."""
-    last = None
+    accuracy bar against the FP64 truth; (rtol, x-err, report).  When none
+    does (the bar lies below what the arm reaches on this problem), the
+    tolerance of its most accurate converged solve."""
+    best = None
     for rtol in ladder:
         rep = solve(rtol)
         err = truth_err()
-        last = (rtol, err, rep)
-        if np.max(err) <= XERR_BAR:
-            break
-    return last
+        reps = rep if isinstance(rep, list) else [rep]
+        ok = all(r["status"] == "OK" for r in reps)
+        if np.max(err) <= XERR_BAR and ok:
+            return rtol, err, rep
+        if ok and (best is None or np.max(err) < np.max(best[1])):
+            best = (rtol, err, rep)
+    return best if best is not None else (rtol, err, rep)
 
 
 def measure_solves(op, k, rtol, inner=3e-4):
@@ -568,12 +572,111 @@ def run_batch(args):
         "mixed": {"solves_per_s": ok["mixed"] / times["mixed"], "seconds": times["mixed"], "converged": ok["mixed"],
                   "within_1e-10_of_fp64": good},
         "speedup_mixed_over_fp64": (ok["mixed"] / times["mixed"]) / max(ok["fp64"] / times["fp64"], 1e-30),
+        "mdofs_solved_per_s": {p: sum(pb.ndof for pb, r in zip(probs, res[p]) if r["status"] == "OK") / times[p] / 1e6
+                               for p in res},
         "rel_err_mixed_vs_fp64": {"max": max(rel), "median": float(np.median(rel))},
         "iterations": {p: [r["iterations"] for r in res[p]] for p in res},
         "setup_seconds": setup_s,
     }
+    # e2e: the same batch with its right-hand sides copied from pinned host
+    # memory and its solutions copied back, inside the timed region
+    db.set_params(dict(base, Precision="mixed"))
+    db.zero()
+    hb = [(b[0].cpu().pin_memory(), b[1].cpu().pin_memory()) for b in db.rhs]
+    hx = [(torch.empty_like(b[0]), torch.empty_like(b[1])) for b in hb]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for st, (br, bi), (hr, hi) in zip(db.streams, db.rhs, hb):
+        with torch.cuda.stream(st):
+            br.copy_(hr, non_blocking=True)
+            bi.copy_(hi, non_blocking=True)
+    res_e2e = db.solve()
+    for st, (xr, xi), (hr, hi) in zip(db.streams, db.sols, hx):
+        with torch.cuda.stream(st):
+            hr.copy_(xr, non_blocking=True)
+            hi.copy_(xi, non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    ok_e2e = sum(r["status"] == "OK" for r in res_e2e)
+    nbytes = int(sum(2 * p.ndof * 8 for p in probs))
+    line["e2e"] = {"value": ok_e2e / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": nbytes,
+                   "d2h_bytes_per_step": nbytes,
+                   "path": "pinned host b -> device, hc_solve_complex_batch, device x -> pinned host"}
     db.close()
+    line["roofline"] = batch_roofline()
+    line["cpu_baseline"] = None if args.no_cpu else batch_cpu_baseline(probs)
     print(json.dumps(line))
+
+
+def batch_roofline(n=24, p=2, omega=1e3, reps=10):
+    """The fused complex apply (FP32 planar re/im, the kernel every inner COCG
+    iteration runs) on a mid-size member, CUDA events, L2 flushed."""
+    import torch
+
+    from hephaestus_gb300 import HCurlOperator, meshes
+
+    rng = np.random.default_rng(6)
+    op = HCurlOperator(n, n, n, p, meshes.loguniform(n ** 3, 1.0, 1e3, rng), meshes.loguniform(n ** 3, 1e-2, 1e6, rng),
+                       dt=1.0, ess_attr_bits=0x3F)
+    xr = torch.randn(op.ndof, device="cuda")
+    xi = torch.randn_like(xr)
+    yr, yi = torch.empty_like(xr), torch.empty_like(xr)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        op.MultComplexDevice(omega, xr, xi, yr, yi)
+    ts = []
+    for _ in range(reps):
+        flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        op.MultComplexDevice(omega, xr, xi, yr, yi)
+        b.record()
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b))
+    ms = float(np.mean(ts))
+    alg = op.ndof * 4 * 4 + op.ne * 12 * 8  # x re/im read, y re/im written (FP32); 12 FP64 values per element
+    hbm, src = hbm_peak()
+    op.close()
+    return {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+            "frac": alg / (ms * 1e-3) / 1e9 / hbm, "traffic": None,
+            "kernel": "masked init + hex_apply_tiled_cplx<float,p=2> on a 24^3 member (%d complex dofs)" % op.ndof,
+            "kernel_ms": ms, "alg_bytes_per_launch": alg, "peak_source": src}
+
+
+def batch_cpu_baseline(probs, dof_budget=60000):
+    """SuperLU solves (the reference's direct solver for this operator) of the
+    smallest members, up to dof_budget complex dofs together, with the
+    oracle's matrices, one host thread; reported as solved dofs per second."""
+    import oracle
+    from hephaestus_gb300 import meshes
+    from oracle import complex_ref as CR
+
+    small, tot = [], 0
+    for pb in sorted(probs, key=lambda p: p.ndof):
+        if small and tot + pb.ndof > dof_budget:
+            break
+        small.append(pb)
+        tot += pb.ndof
+    t0 = time.perf_counter()
+    for pb in small:
+        rng = np.random.default_rng(pb.seed)
+        ne = pb.n ** 3
+        nu = meshes.loguniform(ne, 1.0, 1e3, rng)
+        sigma = meshes.loguniform(ne, 1e-2, 1e6, rng)
+        I0 = float(rng.uniform(0.5, 2.0))
+        P = oracle.Problem.hex(pb.n, pb.n, pb.n, pb.p)
+        ess = P.hex_ess_mask(0x3F)
+        Cn, M = CR.forms(P, nu, sigma)
+        J = CR.eliminated(Cn, M, pb.omega, ess)
+        b = P.load_coil(I0=I0, q=pb.p + 2)
+        b[ess != 0] = 0.0
+        CR.direct_solve(J, b)
+    el = time.perf_counter() - t0
+    return {"value": tot / el / 1e6, "unit": "M complex dofs solved/s", "cores": 1, "kind": "port",
+            "solves_per_s": len(small) / el,
+            "sample": "%d smallest members (%s complex dofs): oracle assembly + SuperLU solve each, %.1f s; oracle "
+                      "restatement, not MFEM" % (len(small), "/".join(str(p.ndof) for p in small), el)}
 
 
 def run_serve(args):
@@ -594,14 +697,22 @@ def run_serve(args):
         ex(r, 0)
     mean_service = (time.perf_counter() - t0) / len(cal)
     rate = 0.8 / mean_service
+    kept = {}
+    sample = lambda r: r.rid % 40 == 0  # noqa: E731  results compared between the precisions
     for prec in ("fp64", "mixed"):
         reqs = SV.make_stream(args.requests, rate=rate, seed=7)
-        ex = SV.GpuExecutor(args.slots, precision=prec, rtol=args.solve_rtol, keep=False, inner_rtol=args.inner_rtol)
+        ex = SV.GpuExecutor(args.slots, precision=prec, rtol=args.solve_rtol, keep=sample, inner_rtol=args.inner_rtol)
         done, wall = SV.run_stream(reqs, ex, budget_bytes=budget, slots=args.slots)
         steps = sum(r.steps for r in done)
         st = SV.latency_stats(done)
+        kept[prec] = ex.kept
         out[prec] = {"requests": len(done), "steps": steps, "wall_s": wall, "solves_per_s": steps / wall,
                      "ok": sum(r.result["status"] == "OK" for r in done), **st}
+    diffs = [float(np.linalg.norm(kept["mixed"][k] - kept["fp64"][k]) / max(np.linalg.norm(kept["fp64"][k]), 1e-300))
+             for k in kept["fp64"] if k in kept["mixed"]]
+    # dominant kernel: the FP32 masked apply on a mid-size request (40^3 hexes, p = 2)
+    roof = serve_roofline()
+    cpu = None if args.no_cpu else serve_cpu_baseline(args)
     line = {
         "metric": "serving: p50/p99 latency and solves/s, transient A-formulation steps (mixed vs FP64)",
         "value": out["mixed"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
@@ -610,8 +721,83 @@ def run_serve(args):
                                (args.requests, rate, mean_service),
                    "slots": args.slots, "hbm_budget_bytes": budget, "rtol": args.solve_rtol},
         "fp64": out["fp64"], "mixed": out["mixed"],
+        "rel_err_mixed_vs_fp64": {"requests_compared": len(diffs), "max": max(diffs) if diffs else None,
+                                  "median": float(np.median(diffs)) if diffs else None},
+        "roofline": roof, "cpu_baseline": cpu,
     }
     print(json.dumps(line))
+
+
+def serve_roofline(n=40, p=2, reps=10):
+    """FP32 masked apply (the kernel every inner iteration runs) on one
+    mid-size request's operator, CUDA events around each launch, L2 flushed."""
+    import torch
+
+    from hephaestus_gb300 import HCurlOperator, meshes
+
+    rng = np.random.default_rng(5)
+    op = HCurlOperator(n, n, n, p, meshes.loguniform(n ** 3, 1.0, 1e3, rng), meshes.loguniform(n ** 3, 1e-2, 1e6, rng),
+                       dt=DT, ess_attr_bits=0x3F)
+    x = torch.randn(op.ndof, device="cuda")
+    y = torch.empty_like(x)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        op.MultDevice(x, y)
+    ts = []
+    for _ in range(reps):
+        flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        op.MultDevice(x, y)
+        b.record()
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b))
+    ms = float(np.mean(ts))
+    alg = algorithmic_bytes(op.ndof, op.ne, 4, 12, 8)
+    hbm, src = hbm_peak()
+    op.close()
+    return {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+            "frac": alg / (ms * 1e-3) / 1e9 / hbm, "traffic": None,
+            "kernel": "k_init_masked + hex_apply_tiled<float,p=2> on a 40^3 request (%d dofs)" % op.ndof,
+            "kernel_ms": ms, "alg_bytes_per_launch": alg, "peak_source": src}
+
+
+def serve_cpu_baseline(args, count=2):
+    """The oracle's FP64 backward-Euler step (CSR assembly + sparse direct solve)
+    on the smallest requests of the same stream, one host thread (SuperLU)."""
+    import oracle
+    from hephaestus_gb300 import serve as SV
+
+    reqs = sorted(SV.make_stream(args.requests, rate=1.0, seed=7), key=lambda r: r.ndof)[:count]
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as sla
+
+    t0 = time.perf_counter()
+    steps = 0
+    for r in reqs:
+        nu, sigma, I0 = SV.GpuExecutor.fields(r)
+        ref = oracle.Problem.hex(r.n, r.n, r.n, r.p)
+        ref.set_coef(DT * nu, sigma)
+        ref.assemble()
+        m = ref.hex_ess_mask(0x3F)
+        ref.set_ess(m)
+        K = ref.csr()
+        free = (m == 0).astype(np.float64)
+        J = (sp.diags(free) @ K @ sp.diags(free) + sp.diags(1.0 - free)).tocsc()
+        lu = sla.splu(J)
+        f = ref.load_coil(I0=I0, q=r.p + 2)
+        A = np.zeros(ref.ndof)
+        for _ in range(r.steps):
+            b = f - ref.apply_curlcurl(A) / DT
+            b[m != 0] = 0.0
+            A = A + DT * lu.solve(b)
+            steps += 1
+    el = time.perf_counter() - t0
+    return {"value": steps / el, "unit": "solves/s", "cores": 1, "kind": "port",
+            "sample": "%d smallest requests of the stream (%s dofs), oracle CSR assembly + SuperLU direct solve per "
+                      "request, %d steps in %.1f s; oracle restatement, not MFEM/hypre"
+                      % (len(reqs), "/".join(str(r.ndof) for r in reqs), steps, el)}
 
 
 def run_tets(args):
@@ -771,8 +957,38 @@ def tet_solves(args, op, nrhs):
                      "rel_err_vs_fp64_truth_per_column": [float(v) for v in err],
                      "rel_err_vs_fp64_truth_max": float(np.max(err))}
         out[prec]["meets_1e-10"] = bool(np.max(err) <= XERR_BAR and all(r["status"] == "OK" for r in res))
+    sols_mixed = X.clone()
+    # the plain FP64 single-solve path (the drop-in: hc_solve_device, one
+    # column at a time, same preconditioner) at the FP64 block arm's tolerance
+    s1 = solver("fp64", out["fp64"]["rtol"])
+    x1 = torch.zeros(op.ndof, dtype=torch.float64, device="cuda")
+    b1 = B[:, 0].contiguous()
+    s1.MultDevice(b1, x1)  # warm-up
+    X1 = torch.empty_like(B)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    e = torch.cuda.Event(enable_timing=True)
+    a.record()
+    its1 = []
+    for k in range(nrhs):
+        b1 = B[:, k].contiguous()
+        x1.zero_()
+        s1.MultDevice(b1, x1)
+        its1.append(s1.result["iterations"])
+        X1[:, k] = x1
+    e.record()
+    torch.cuda.synchronize()
+    ms1 = a.elapsed_time(e)
+    err1 = _xerr(X1, truth, cols=True)
+    out["fp64_single"] = {"solves_per_s": nrhs / (ms1 * 1e-3), "ms_per_solve": ms1 / nrhs, "rtol": out["fp64"]["rtol"],
+                          "iterations_max": max(its1), "rel_err_vs_fp64_truth_max": float(np.max(err1)),
+                          "path": "hc_solve_device per column (tet AUX, block PCG with one column)"}
     out["rel_err_mixed_vs_fp64_max"] = out["mixed"]["rel_err_vs_fp64_truth_max"]
+    out["rel_err_mixed_vs_fp64_arm_max"] = float(np.max(_xerr(sols_mixed, X1, cols=True)))
     out["speedup_mixed_over_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+    out["speedup_mixed_batched_over_fp64_single"] = out["mixed"]["solves_per_s"] / out["fp64_single"]["solves_per_s"]
+    out["mixed_as_accurate_as_fp64"] = bool(out["mixed"]["rel_err_vs_fp64_truth_max"] <=
+                                            max(out["fp64"]["rel_err_vs_fp64_truth_max"], XERR_BAR))
     out["speedup_credited"] = bool(out["fp64"]["meets_1e-10"] and out["mixed"]["meets_1e-10"])
     out["rhs"] = "%d loop coils, I0 ~ U[0.5, 2], centre (0.5, 0.5) + U[-0.1, 0.1]^2, seeded" % nrhs
     out["preconditioner"] = ("Jacobi + gradient-space correction (PG) V (PG)^T, V = one smoothed-aggregation AMG "

@@ -79,8 +79,25 @@ __global__ void k_init_masked_multi(int64_t n, int nrhs, const uint8_t* __restri
                                     T* __restrict__ y) {
   GS_LOOP(i, n * nrhs) y[i] = ess[i / nrhs] ? x[i] : T(0);
 }
+// 16-byte chunks of a [dof][rhs] block with 4 | nrhs (a power of two): the
+// row of chunk i is i >> shift, no division per element
+template <typename T>
+__global__ void k_init_masked_multi_v(int64_t nchunks, int shift, const uint8_t* __restrict__ ess,
+                                      const uint4* __restrict__ x, uint4* __restrict__ y) {
+  GS_LOOP(i, nchunks) y[i] = ess[i >> shift] ? x[i] : make_uint4(0u, 0u, 0u, 0u);
+}
 template <typename T>
 cudaError_t init_masked_multi(int64_t n, int nrhs, const uint8_t* ess, const T* x, T* y, cudaStream_t s) {
+  const int per = (int)(16 / sizeof(T));  // values per 16-byte chunk
+  if (nrhs % per == 0 && ((uintptr_t)x | (uintptr_t)y) % 16 == 0 && (nrhs & (nrhs - 1)) == 0) {
+    int shift = 0;
+    while ((1 << shift) < nrhs / per) ++shift;
+    const int64_t nch = n * (nrhs / per);
+    const int64_t blocks = std::min<int64_t>((nch + 255) / 256, 152 * 16);
+    k_init_masked_multi_v<T><<<(unsigned)std::max<int64_t>(1, blocks), 256, 0, s>>>(
+        nch, shift, ess, reinterpret_cast<const uint4*>(x), reinterpret_cast<uint4*>(y));
+    return cudaGetLastError();
+  }
   k_init_masked_multi<T><<<vgrid(n * nrhs), kRedThreads, 0, s>>>(n, nrhs, ess, x, y);
   return cudaGetLastError();
 }

@@ -527,7 +527,7 @@ __device__ __forceinline__ void mma_1688(float (&d)[4], const uint32_t (&a)[2], 
                : "r"(a[0]), "r"(a[1]), "r"(b0));
 }
 
-__global__ void __launch_bounds__(32 * kTcW) tet_apply_mma16(int64_t ne, const int32_t* __restrict__ edofs,
+__global__ void __launch_bounds__(32 * kTcW, 5) tet_apply_mma16(int64_t ne, const int32_t* __restrict__ edofs,
                                                              const __nv_bfloat16* __restrict__ K,
                                                              const uint8_t* __restrict__ ess, int masked, float scale,
                                                              const float* __restrict__ x, float* __restrict__ y,

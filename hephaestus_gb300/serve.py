@@ -207,7 +207,8 @@ def latency_stats(reqs):
 class GpuExecutor:
     """Runs one request on the GPU: builds the operator for its seeded fields,
     then takes its time steps with device-resident A, b, dA on a dedicated
-    stream (one per worker)."""
+    stream (one per worker).  keep: False, True, or a predicate on the
+    request -- the final A of kept requests is copied to the host (kept)."""
 
     def __init__(self, slots, precision="mixed", precond="aux", rtol=1e-12, dt=0.01, keep=False, inner_rtol=3e-4):
         import torch
@@ -222,7 +223,9 @@ class GpuExecutor:
         self.kept = {}
         self.inner_rtol = inner_rtol
 
-    def fields(self, req):
+    @staticmethod
+    def fields(req):
+        """Seeded per-element nu, sigma and the coil current of a request."""
         from . import meshes
 
         rng = np.random.default_rng(req.seed)
@@ -257,7 +260,7 @@ class GpuExecutor:
                 last = steps[-1] if steps else {"status": "EINVAL", "rel_residual": float("nan")}
                 res = {"status": last["status"], "iterations": [r["iterations"] for r in steps],
                        "rel_residual": last["rel_residual"]}
-                if self.keep:
+                if self.keep and (not callable(self.keep) or self.keep(req)):
                     self.kept[req.rid] = A.cpu().numpy()
                 return res
             finally:

@@ -206,3 +206,48 @@ def test_batch_of_uneven_problems_matches_each_alone():
         assert res[k]["status"] == "OK", (k, res[k])
         x = sols[k][0].cpu().numpy() + 1j * sols[k][1].cpu().numpy()
         assert np.linalg.norm(x - refs[k]) / np.linalg.norm(refs[k]) < 1e-9, (k, res[k])
+
+
+def test_config4_sized_batch_equals_each_member_alone():
+    """Members drawn as config 4 draws them (nu = 10^U(0,3), sigma = 10^U(-2,6),
+    coil right-hand side), including a 32^3 order-2 member (300 k complex dofs):
+    solved together (hc_solve_complex_batch, each on its own stream) and each
+    alone (the same graph-driven solve), mixed precision with the
+    auxiliary-space preconditioner; the small member is also checked against
+    the oracle's SuperLU solve."""
+    import torch
+
+    from hephaestus_gb300 import batch as B
+    from hephaestus_gb300.operator import solve_complex_batch
+
+    probs = [B.Problem(32, 2, 3.0e4, 101), B.Problem(12, 3, 2.0e3, 102), B.Problem(9, 1, 4.0e2, 103)]
+    params = {"Tolerance": 1e-10, "AbsTolerance": 0.0, "MaxIter": 20000, "Precision": "mixed",
+              "Preconditioner": "aux", "InnerTolerance": 3e-4}
+    db = B.DeviceBatch(probs, params)
+    try:
+        res = db.solve()
+        assert all(r["status"] == "OK" for r in res), res
+        together = db.solutions()
+        for k in range(len(probs)):
+            db.zero()
+            res1 = solve_complex_batch([db.solvers[k]], [db.rhs[k]], [db.sols[k]])
+            assert res1[0]["status"] == "OK", res1
+            xr, xi = db.sols[k]
+            ar, ai = together[k]
+            d = torch.sqrt(torch.sum((xr - ar) ** 2 + (xi - ai) ** 2)) / torch.sqrt(torch.sum(xr ** 2 + xi ** 2))
+            assert float(d) <= 1e-10, (k, float(d))
+        # the 9^3 order-1 member against SuperLU on the oracle's matrices
+        pb = probs[2]
+        rng = np.random.default_rng(pb.seed)
+        ne = pb.n ** 3
+        nu = meshes.loguniform(ne, 1.0, 1e3, rng)
+        sigma = meshes.loguniform(ne, 1e-2, 1e6, rng)
+        P = oracle.Problem.hex(pb.n, pb.n, pb.n, pb.p)
+        Cn, M = CR.forms(P, nu, sigma)
+        J = CR.eliminated(Cn, M, pb.omega, db.ops[2].ess_mask())
+        b = db.rhs[2][0].cpu().numpy()
+        x_ref = CR.direct_solve(J, b)
+        x = together[2][0].cpu().numpy() + 1j * together[2][1].cpu().numpy()
+        assert np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref) < 1e-8
+    finally:
+        db.close()
