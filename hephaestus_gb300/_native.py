@@ -16,7 +16,7 @@ HEADER = os.path.join(os.path.dirname(_HERE), "include", "hcurl_op.h")
 HC_OK, HC_EINVAL, HC_ENOMEM, HC_ECUDA, HC_NOT_CONVERGED, HC_BREAKDOWN, HC_TIMEOUT, HC_ENOTSUP = range(8)
 STATUS_NAMES = ["OK", "EINVAL", "ENOMEM", "ECUDA", "NOT_CONVERGED", "BREAKDOWN", "TIMEOUT", "ENOTSUP"]
 HC_HEX, HC_TET = 0, 1
-HC_FP64, HC_FP32, HC_MIXED, HC_BF16 = 0, 1, 2, 3
+HC_FP64, HC_FP32, HC_MIXED, HC_BF16, HC_MIXED_RR = 0, 1, 2, 3, 4
 HC_PRECOND_NONE, HC_PRECOND_JACOBI, HC_PRECOND_CHEBYSHEV, HC_PRECOND_AUX = 0, 1, 2, 3
 HC_FIELD_ELEM, HC_FIELD_QUAD = 0, 1
 
@@ -108,6 +108,7 @@ _SIGS = {
     "hc_solve_device": (C.c_int, [C.c_void_p, C.POINTER(SolveParams), C.c_void_p, C.c_void_p,
                                   C.POINTER(SolveInfo)]),
     "hc_lanczos_lmax": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
+    "hc_precond_apply_device": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "hc_mult_multi_device": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     "hc_elem_type": (C.c_int32, [C.c_void_p]),
     "hc_tet_element_matrix": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),

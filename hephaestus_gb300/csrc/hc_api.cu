@@ -815,8 +815,8 @@ static hc_status check_params(hcop* h, const hc_solve_params* p) {
     h->err = "null solve parameters";
     return HC_EINVAL;
   }
-  if (p->precision != HC_FP64 && p->precision != HC_MIXED) {
-    h->err = "precision must be HC_FP64 or HC_MIXED";
+  if (p->precision != HC_FP64 && p->precision != HC_MIXED && p->precision != HC_MIXED_RR) {
+    h->err = "precision must be HC_FP64, HC_MIXED or HC_MIXED_RR";
     return HC_EINVAL;
   }
   if (p->precond < HC_PRECOND_NONE || p->precond > HC_PRECOND_AUX) {
@@ -830,6 +830,29 @@ static hc_status check_params(hcop* h, const hc_solve_params* p) {
   if (!(p->rtol >= 0.0) || !(p->atol >= 0.0) || p->maxit < 1) {
     h->err = "rtol, atol must be >= 0 and maxit >= 1";
     return HC_EINVAL;
+  }
+  return HC_OK;
+}
+
+hc_status hc_precond_apply_device(hcop_t* h, int32_t precond, const double* r, double* z) {
+  if (!h || !r || !z) return HC_EINVAL;
+  if (precond != HC_PRECOND_JACOBI && precond != HC_PRECOND_AUX) {
+    h->err = "hc_precond_apply_device: precond must be HC_PRECOND_JACOBI or HC_PRECOND_AUX";
+    return HC_EINVAL;
+  }
+  if (precond == HC_PRECOND_AUX && h->type != HC_HEX) {
+    h->err = "hc_precond_apply_device: HC_PRECOND_AUX is built for hex handles here";
+    return HC_ENOTSUP;
+  }
+  if (precond == HC_PRECOND_AUX) {
+    const hc_status st = auxmg_setup(h);
+    if (st != HC_OK) return st;
+  }
+  HC_CUDA_TRY(h, jacobi_apply(h->ndof, h->dinv, r, z, h->stream));
+  if (precond == HC_PRECOND_AUX) {
+    const float coef[4] = {1.0f, 0.0f, 0.0f, 0.0f};
+    const cudaError_t e = auxmg_apply<double, 1>(h, r, nullptr, z, nullptr, coef, nullptr, h->stream);
+    HC_CUDA_TRY(h, e);
   }
   return HC_OK;
 }
@@ -848,6 +871,10 @@ hc_status hc_solve_device(hcop_t* h, const hc_solve_params* prm, const double* b
   if (!info) info = &loc;
   std::memset(info, 0, sizeof(*info));
   if (prm->precond == HC_PRECOND_AUX && h->type == HC_TET) {  // one-column block PCG with the tet AMG
+    if (prm->precision == HC_MIXED_RR) {
+      h->err = "hc_solve_device: HC_MIXED_RR is not built for tet AUX solves (use HC_MIXED)";
+      return HC_ENOTSUP;
+    }
     if ((reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(x)) % 16 != 0) {
       h->err = "hc_solve_device: b and x must be 16-byte aligned for tet AUX solves";
       return HC_EINVAL;
@@ -859,6 +886,7 @@ hc_status hc_solve_device(hcop_t* h, const hc_solve_params* prm, const double* b
     if (st != HC_OK) return st;
   }
   if (prm->precision == HC_MIXED) return mixed_device(h, prm, b, x, info);
+  if (prm->precision == HC_MIXED_RR) return mixed_rr_device(h, prm, b, x, info);
   SolveCfg cfg;
   cfg.precond = prm->precond;
   cfg.cheb_degree = prm->cheb_degree;

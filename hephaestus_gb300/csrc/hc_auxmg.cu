@@ -24,6 +24,7 @@
 // vectors.  c = 1 for K = dt C + M_sigma, c = 1/(i omega) for C + i omega M_sigma.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -77,12 +78,22 @@ struct AuxLevel {
 struct AuxGraph {
   cudaGraphExec_t exec = nullptr;
   const void* key[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-  int nv = 0, tsize = 0;
+  int nv = 0, tsize = 0, coop = 0;
   float coef[4] = {0, 0, 0, 0};
+};
+
+// Grid barrier of the cooperative V-cycle (device memory, zeroed at setup).
+struct CoopBar {
+  unsigned count;  // arrivals at the current barrier
+  unsigned gen;    // barriers completed
+  int err;         // 1: a wait gave up (sticky; the V-cycle then returns NaN)
 };
 
 struct AuxMG {
   int p = 1, nlev = 0;
+  CoopBar* bar = nullptr;  // cooperative V-cycle state, nullptr: per-step kernels
+  int coop_blocks = 0;     // co-resident blocks of the cooperative V-cycle (per NV: [NV - 1])
+  int coop_blocks2 = 0;
   std::vector<AuxGraph> graphs;   // at most kAuxGraphs, oldest replaced first
   int next_graph = 0;
   cudaStream_t cap = nullptr;     // private stream the captures are made on
@@ -196,10 +207,20 @@ static inline NodeGrid node_grid(int nx, int ny, int nz) {
   if (i > (d).nx) return;                                                   \
   const int n = i + ((d).nx + 1) * (j + ((d).ny + 1) * k)
 
+// Loads of level vectors.  COH (the cooperative V-cycle, where one launch
+// writes a vector in one step and other blocks read it in a later one): L2
+// loads (ld.global.cg), never the per-SM read-only or L1 copies, which are
+// not kept coherent with other SMs' writes within a launch.
+template <bool COH>
+__device__ __forceinline__ float vld(const float* p) {
+  if constexpr (COH) return __ldcg(p);
+  else return *p;
+}
+
 // (L v)_n: all 27 coefficient and value loads issued together; the stencil of
 // a boundary node has zero coefficients outside the grid, whose loads are
 // redirected to the node itself
-template <int NV>
+template <int NV, bool COH = false>
 __device__ __forceinline__ void st_row(const Dims& d, const float* __restrict__ St, const float* __restrict__ v,
                                        int nn, int n, int i, int j, int k, float (&acc)[NV]) {
   const int sx = d.nx + 1, sxy = (d.nx + 1) * (d.ny + 1);
@@ -212,58 +233,74 @@ __device__ __forceinline__ void st_row(const Dims& d, const float* __restrict__ 
     const int m = in ? n + dx + sx * dy + sxy * dz : n;
     const float c = St[q * nn + n];
 #pragma unroll
-    for (int w = 0; w < NV; ++w) acc[w] += c * v[w * nn + m];
+    for (int w = 0; w < NV; ++w) acc[w] = __fmaf_rn(c, vld<COH>(v + w * nn + m), acc[w]);
   }
 }
 
 // One fused Chebyshev step (Saad Alg. 12.1): t = L d_in, r -= t,
 // d_out = c1 d_in + c2 D^-1 r, x += (add_in ? d_in : 0) + d_out.
 // d_in is read at stencil neighbours and never written here.
+template <int NV, bool COH = false>
+__device__ __forceinline__ void cheb_fused_at(const Dims& d, const float* __restrict__ St,
+                                              const float* __restrict__ dinv, const float* __restrict__ din,
+                                              float* __restrict__ dout, float* __restrict__ r,
+                                              float* __restrict__ x, float c1, float c2, int add_in, int n, int i,
+                                              int j, int k) {
+  const int nn = (int)d.nodes();
+  float t[NV];
+  st_row<NV, COH>(d, St, din, nn, n, i, j, k, t);
+  const float dv = dinv[n];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    const int id = q * nn + n;
+    const float ri = __fsub_rn(vld<COH>(r + id), t[q]);
+    const float di = vld<COH>(din + id);
+    const float dn = __fmaf_rn(c1, di, __fmul_rn(__fmul_rn(c2, dv), ri));
+    r[id] = ri;
+    dout[id] = dn;
+    x[id] = __fadd_rn(vld<COH>(x + id), __fadd_rn(add_in ? di : 0.0f, dn));
+  }
+}
 template <int NV>
 __global__ void k_cheb_fused(Dims d, const float* __restrict__ St, const float* __restrict__ dinv,
                              const float* __restrict__ din, float* __restrict__ dout, float* __restrict__ r,
                              float* __restrict__ x, float c1, float c2, int add_in, const int* __restrict__ done) {
   if (done && *done) return;
   NODE_IJK(d, i, j, k, n);
+  cheb_fused_at<NV>(d, St, dinv, din, dout, r, x, c1, c2, add_in, n, i, j, k);
+}
+// r = b - L x (zero at fixed nodes), d = D^-1 r / theta; x untouched
+template <int NV, bool COH = false>
+__device__ __forceinline__ void cheb_resid_at(const Dims& d, const float* __restrict__ St,
+                                              const float* __restrict__ dinv, const float* __restrict__ b,
+                                              const float* __restrict__ x, float* __restrict__ r,
+                                              float* __restrict__ dv, float inv_theta, int n, int i, int j, int k) {
   const int nn = (int)d.nodes();
   float t[NV];
-  st_row<NV>(d, St, din, nn, n, i, j, k, t);
-  const float dv = dinv[n];
+  st_row<NV, COH>(d, St, x, nn, n, i, j, k, t);
+  const float di = dinv[n];
 #pragma unroll
   for (int q = 0; q < NV; ++q) {
     const int id = q * nn + n;
-    const float ri = r[id] - t[q];
-    const float di = din[id];
-    const float dn = c1 * di + c2 * dv * ri;
+    const float ri = di != 0.0f ? __fsub_rn(vld<COH>(b + id), t[q]) : 0.0f;
     r[id] = ri;
-    dout[id] = dn;
-    x[id] += (add_in ? di : 0.0f) + dn;
+    dv[id] = __fmul_rn(__fmul_rn(di, ri), inv_theta);
   }
 }
-// r = b - L x (zero at fixed nodes), d = D^-1 r / theta; x untouched
 template <int NV>
 __global__ void k_cheb_resid(Dims d, const float* __restrict__ St, const float* __restrict__ dinv,
                              const float* __restrict__ b, const float* __restrict__ x, float* __restrict__ r,
                              float* __restrict__ dv, float inv_theta, const int* __restrict__ done) {
   if (done && *done) return;
   NODE_IJK(d, i, j, k, n);
-  const int nn = (int)d.nodes();
-  float t[NV];
-  st_row<NV>(d, St, x, nn, n, i, j, k, t);
-  const float di = dinv[n];
-#pragma unroll
-  for (int q = 0; q < NV; ++q) {
-    const int id = q * nn + n;
-    const float ri = di != 0.0f ? b[id] - t[q] : 0.0f;
-    r[id] = ri;
-    dv[id] = di * ri * inv_theta;
-  }
+  cheb_resid_at<NV>(d, St, dinv, b, x, r, dv, inv_theta, n, i, j, k);
 }
 // x += d (a one-step smoother from a nonzero start)
 template <int NV>
 __global__ void k_add(int nn, const float* __restrict__ d, float* __restrict__ x, const int* __restrict__ done) {
   if (done && *done) return;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NV * nn; i += gridDim.x * blockDim.x) x[i] += d[i];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NV * nn; i += gridDim.x * blockDim.x)
+    x[i] = __fadd_rn(x[i], d[i]);
 }
 
 // coarse element matrices: K_C = sum over children W^T K_child W (index-space trilinear W)
@@ -342,18 +379,17 @@ template <int NV>
 __device__ __forceinline__ void cheb_start_at(const ChebStart& cs, int nn, int n, float dinv, const float (&b)[NV]) {
 #pragma unroll
   for (int v = 0; v < NV; ++v) {
-    const float dv = dinv * b[v] * cs.inv_theta;
+    const float dv = __fmul_rn(__fmul_rn(dinv, b[v]), cs.inv_theta);
     cs.r[v * nn + n] = b[v];
     cs.d[v * nn + n] = dv;
     cs.x[v * nn + n] = dv;
   }
 }
 
-template <int NV>
-__global__ void k_restrict(Dims fd, Dims cd, const float* __restrict__ rf, const float* __restrict__ dinvc,
-                           float* __restrict__ bc, ChebStart cs, const int* __restrict__ done) {
-  if (done && *done) return;
-  NODE_IJK(cd, I, J, K, n);
+template <int NV, bool COH = false>
+__device__ __forceinline__ void restrict_at(const Dims& fd, const Dims& cd, const float* __restrict__ rf,
+                                            const float* __restrict__ dinvc, float* __restrict__ bc,
+                                            const ChebStart& cs, int n, int I, int J, int K) {
   const int nc = (int)cd.nodes(), nf = (int)fd.nodes();
   const int sx = fd.nx + 1, sxy = (fd.nx + 1) * (fd.ny + 1);
   float acc[NV];
@@ -362,15 +398,22 @@ __global__ void k_restrict(Dims fd, Dims cd, const float* __restrict__ rf, const
 #pragma unroll
     for (int q = 0; q < 27; ++q) {
       const int fi = 2 * I - 1 + q % 3, fj = 2 * J - 1 + (q / 3) % 3, fk = 2 * K - 1 + q / 9;
-      const float w = w1d(fi, I, fd.nx) * w1d(fj, J, fd.ny) * w1d(fk, K, fd.nz);
+      const float w = __fmul_rn(__fmul_rn(w1d(fi, I, fd.nx), w1d(fj, J, fd.ny)), w1d(fk, K, fd.nz));
       const int g = w != 0.0f ? fi + sx * fj + sxy * fk : 0;
 #pragma unroll
-      for (int v = 0; v < NV; ++v) acc[v] += w * rf[v * nf + g];
+      for (int v = 0; v < NV; ++v) acc[v] = __fmaf_rn(w, vld<COH>(rf + v * nf + g), acc[v]);
     }
   }
 #pragma unroll
   for (int v = 0; v < NV; ++v) bc[v * nc + n] = acc[v];
   cheb_start_at<NV>(cs, nc, n, dinvc[n], acc);
+}
+template <int NV>
+__global__ void k_restrict(Dims fd, Dims cd, const float* __restrict__ rf, const float* __restrict__ dinvc,
+                           float* __restrict__ bc, ChebStart cs, const int* __restrict__ done) {
+  if (done && *done) return;
+  NODE_IJK(cd, I, J, K, n);
+  restrict_at<NV>(fd, cd, rf, dinvc, bc, cs, n, I, J, K);
 }
 // x_f += P x_c at free fine nodes
 __device__ __forceinline__ void coarse_pair(int f, int nf, int& c0, int& c1, float& w0, float& w1) {
@@ -388,11 +431,10 @@ __device__ __forceinline__ void coarse_pair(int f, int nf, int& c0, int& c1, flo
     w0 = w1 = 0.5f;
   }
 }
-template <int NV>
-__global__ void k_prolong_add(Dims fd, Dims cd, const float* __restrict__ xc, const float* __restrict__ dinvf,
-                              float* __restrict__ xf, const int* __restrict__ done) {
-  if (done && *done) return;
-  NODE_IJK(fd, i, j, k, n);
+template <int NV, bool COH = false>
+__device__ __forceinline__ void prolong_add_at(const Dims& fd, const Dims& cd, const float* __restrict__ xc,
+                                               const float* __restrict__ dinvf, float* __restrict__ xf, int n,
+                                               int i, int j, int k) {
   if (dinvf[n] == 0.0f) return;
   const int nc = (int)cd.nodes(), nf = (int)fd.nodes();
   int ci[2], cj[2], ck[2];
@@ -406,13 +448,20 @@ __global__ void k_prolong_add(Dims fd, Dims cd, const float* __restrict__ xc, co
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
     const int a = q & 1, b = (q >> 1) & 1, c = q >> 2;
-    const float w = wi[a] * wj[b] * wk[c];
+    const float w = __fmul_rn(__fmul_rn(wi[a], wj[b]), wk[c]);
     const int g = ci[a] + sx * cj[b] + sxy * ck[c];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) acc[v] += w * xc[v * nc + g];
+    for (int v = 0; v < NV; ++v) acc[v] = __fmaf_rn(w, vld<COH>(xc + v * nc + g), acc[v]);
   }
 #pragma unroll
-  for (int v = 0; v < NV; ++v) xf[v * nf + n] += acc[v];
+  for (int v = 0; v < NV; ++v) xf[v * nf + n] = __fadd_rn(vld<COH>(xf + v * nf + n), acc[v]);
+}
+template <int NV>
+__global__ void k_prolong_add(Dims fd, Dims cd, const float* __restrict__ xc, const float* __restrict__ dinvf,
+                              float* __restrict__ xf, const int* __restrict__ done) {
+  if (done && *done) return;
+  NODE_IJK(fd, i, j, k, n);
+  prolong_add_at<NV>(fd, cd, xc, dinvf, xf, n, i, j, k);
 }
 
 // ---- Nedelec <-> Gauss-Lobatto nodes ----------------------------------------------------
@@ -668,6 +717,7 @@ void auxmg_free(hcop* h) {
   dfree(h, M->qdinv);
   dfree(h, M->g);
   dfree(h, M->phi);
+  dfree(h, M->bar);
   delete M;
   h->aux = nullptr;
 }
@@ -683,6 +733,8 @@ static void face_fixed(int nx, int ny, int nz, int bits, std::vector<uint8_t>& f
         f[i + (size_t)(nx + 1) * (j + (size_t)(ny + 1) * k)] = e;
       }
 }
+
+static void coop_setup(hcop* h, AuxMG* M);
 
 hc_status auxmg_setup(hcop* h) {
   if (h->aux) return HC_OK;
@@ -839,6 +891,7 @@ hc_status auxmg_setup(hcop* h) {
   }
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) return fail(e);
+  coop_setup(h, M);
   return HC_OK;
 }
 
@@ -907,6 +960,210 @@ static void vcycle(const hcop* h, AuxMG* M, int l, const int* done, cudaStream_t
   smooth<NV>(h, L, kAuxDegree, false, done, s);
 }
 
+// ---- the V-cycle as one cooperative launch ------------------------------------------------
+// (The per-node functions above spell their roundings out with __fmaf_rn /
+// __fmul_rn / __fadd_rn, so that the compiler's FMA contraction cannot differ
+// between the kernels that inline them.)
+// The per-step kernels above run one launch per smoothing step, residual,
+// restriction and prolongation (21 launches for four levels), most of them on
+// grids of a few thousand nodes, where launch latency and the drain between
+// dependent kernels cost more than the work.  k_vcycle runs the same steps, in
+// the same order and with the same per-node arithmetic (results are
+// bit-identical), in one cooperative launch of co-resident blocks that meet
+// at a grid barrier between steps.
+constexpr int kVThreads = 512;
+constexpr int kMaxVSteps = 64;
+constexpr unsigned kBarSpins = 1u << 22;  // ~0.3 s of polling before a wait gives up
+enum : int { kOpFused = 0, kOpResid = 1, kOpRestrict = 2, kOpProlong = 3, kOpAdd = 4 };
+
+struct VStep {
+  int op, lev;       // level the step writes (restrict: the fine level it reads)
+  int add_in, swap;  // fused step: add d_in to x; swap: d_in = t, d_out = dv (else the reverse)
+  float c1, c2;      // fused step coefficients; resid: c1 = 1/theta
+};
+struct VLevelDev {
+  Dims d;
+  const float* St;
+  const float* dinv;
+  float *x, *b, *r, *dv, *t;
+  float start_inv_theta;  // 1/theta of the level's first smoothing step (restriction target)
+};
+struct VCycleArgs {
+  int nlev, nsteps;
+  CoopBar* bar;
+  VLevelDev lev[kAuxMaxLevels];
+  VStep step[kMaxVSteps];
+};
+
+// All blocks arrive; the last one opens the next generation.  Waits poll with
+// a bound: a wait that gives up sets bar->err, and every block leaves.
+__device__ __forceinline__ bool coop_sync(CoopBar* bar) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* vg = &bar->gen;
+    volatile int* ve = &bar->err;
+    const unsigned g = *vg;
+    __threadfence();
+    if (atomicAdd(&bar->count, 1u) == gridDim.x - 1) {
+      bar->count = 0u;
+      __threadfence();
+      atomicExch(&bar->gen, g + 1u);
+    } else {
+      unsigned spins = 0;
+      while (*vg == g && *ve == 0) {
+        if (++spins > kBarSpins) {
+          atomicExch(&bar->err, 1);
+          break;
+        }
+        __nanosleep(40);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *(volatile int*)&bar->err == 0;
+}
+
+template <int NV>
+__global__ void __launch_bounds__(kVThreads) k_vcycle(const __grid_constant__ VCycleArgs a,
+                                                      const int* __restrict__ done) {
+  if (done && *done) return;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gs = (int64_t)gridDim.x * blockDim.x;
+  bool ok = *(volatile int*)&a.bar->err == 0;
+  for (int s = 0; s < a.nsteps && ok; ++s) {
+    const VStep& st = a.step[s];
+    const VLevelDev& L = a.lev[st.lev];
+    if (st.op == kOpRestrict) {
+      const VLevelDev& C = a.lev[st.lev + 1];
+      const ChebStart cs{C.r, C.dv, C.x, C.start_inv_theta};
+      const int nx1 = C.d.nx + 1, ny1 = C.d.ny + 1, nn = (int)C.d.nodes();
+      for (int64_t q = gt; q < nn; q += gs) {
+        const int n = (int)q, i = n % nx1, t = n / nx1, j = t % ny1, k = t / ny1;
+        restrict_at<NV, true>(L.d, C.d, L.r, C.dinv, C.b, cs, n, i, j, k);
+      }
+    } else {
+      const int nx1 = L.d.nx + 1, ny1 = L.d.ny + 1, nn = (int)L.d.nodes();
+      const float* din = st.swap ? L.t : L.dv;
+      float* dout = st.swap ? L.dv : L.t;
+      for (int64_t q = gt; q < nn; q += gs) {
+        const int n = (int)q, i = n % nx1, t = n / nx1, j = t % ny1, k = t / ny1;
+        switch (st.op) {
+          case kOpFused:
+            cheb_fused_at<NV, true>(L.d, L.St, L.dinv, din, dout, L.r, L.x, st.c1, st.c2, st.add_in, n, i, j, k);
+            break;
+          case kOpResid: cheb_resid_at<NV, true>(L.d, L.St, L.dinv, L.b, L.x, L.r, L.dv, st.c1, n, i, j, k); break;
+          case kOpProlong: {
+            const VLevelDev& C = a.lev[st.lev + 1];
+            prolong_add_at<NV, true>(L.d, C.d, C.x, L.dinv, L.x, n, i, j, k);
+            break;
+          }
+          default:
+#pragma unroll
+            for (int v = 0; v < NV; ++v)
+              L.x[v * nn + n] = __fadd_rn(vld<true>(L.x + v * nn + n), vld<true>(L.dv + v * nn + n));
+            break;
+        }
+      }
+    }
+    if (s + 1 < a.nsteps) ok = coop_sync(a.bar);
+  }
+  if (!ok && blockIdx.x == 0 && threadIdx.x == 0) {
+    // a barrier wait gave up: the correction is NaN, which the Krylov
+    // reductions turn into HC_BREAKDOWN
+    const int nn = (int)a.lev[0].d.nodes();
+    for (int v = 0; v < NV; ++v) a.lev[0].x[v * nn] = __int_as_float(0x7fc00000);
+  }
+}
+
+// The step list of vcycle(0) (same order and coefficients as the per-step launches).
+static void smooth_steps(const AuxMG* M, int l, int degree, bool from_zero, std::vector<VStep>& out) {
+  const ChebCoef c = cheb_coef(M->lev[l].lmax, degree);
+  if (!from_zero) out.push_back(VStep{kOpResid, l, 0, 0, c.inv_theta, 0.0f});
+  int swap = 0;
+  for (int k = 1; k < degree; ++k) {
+    out.push_back(VStep{kOpFused, l, (!from_zero && k == 1) ? 1 : 0, swap, c.c1[k - 1], c.c2[k - 1]});
+    swap ^= 1;
+  }
+  if (!from_zero && degree == 1) out.push_back(VStep{kOpAdd, l, 0, 0, 0.0f, 0.0f});
+}
+static void vcycle_steps(const AuxMG* M, int l, std::vector<VStep>& out) {
+  if (l == M->nlev - 1) {
+    smooth_steps(M, l, kAuxCoarseDegree, true, out);
+    return;
+  }
+  smooth_steps(M, l, kAuxDegree, true, out);
+  out.push_back(VStep{kOpResid, l, 0, 0, 1.0f, 0.0f});
+  out.push_back(VStep{kOpRestrict, l, 0, 0, 0.0f, 0.0f});
+  vcycle_steps(M, l + 1, out);
+  out.push_back(VStep{kOpProlong, l, 0, 0, 0.0f, 0.0f});
+  smooth_steps(M, l, kAuxDegree, false, out);
+}
+
+// HC_AUX_VCYCLE=kernels in the environment selects the per-step kernels (read
+// at every application, so one handle can run both forms)
+static bool coop_wanted() {
+  const char* env = std::getenv("HC_AUX_VCYCLE");
+  return !(env && std::strcmp(env, "kernels") == 0);
+}
+
+// false: not available (no cooperative support, too many steps); the caller
+// issues the per-step kernels
+template <int NV>
+static bool vcycle_coop(const hcop* h, AuxMG* M, const int* done, cudaStream_t s, cudaError_t* err) {
+  (void)h;
+  const int blocks = NV == 1 ? M->coop_blocks : M->coop_blocks2;
+  if (!M->bar || blocks <= 0 || !coop_wanted()) return false;
+  std::vector<VStep> steps;
+  vcycle_steps(M, 0, steps);
+  if ((int)steps.size() > kMaxVSteps) return false;
+  VCycleArgs a{};
+  a.nlev = M->nlev;
+  a.nsteps = (int)steps.size();
+  a.bar = M->bar;
+  for (int l = 0; l < M->nlev; ++l) {
+    const AuxLevel& L = M->lev[l];
+    a.lev[l] = VLevelDev{L.d, L.St, L.dinv, L.x, L.b, L.r, L.dv, L.t, cheb_coef(L.lmax, 1).inv_theta};
+  }
+  for (int k = 0; k < a.nsteps; ++k) a.step[k] = steps[k];
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)blocks);
+  cfg.blockDim = dim3(kVThreads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  *err = cudaLaunchKernelEx(&cfg, k_vcycle<NV>, a, done);
+  return true;
+}
+
+// Blocks of the cooperative V-cycle: co-resident by construction (occupancy
+// x SMs, at most 2 per SM); 0 when the device cannot launch cooperatively.
+static void coop_setup(hcop* h, AuxMG* M) {
+  M->coop_blocks = M->coop_blocks2 = 0;
+  int dev = 0, coop = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return;
+  int b1 = 0, b2 = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_vcycle<1>, kVThreads, 0) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_vcycle<2>, kVThreads, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  if (b1 < 1 || b2 < 1) return;
+  if (dmalloc(h, (void**)&M->bar, sizeof(CoopBar)) != cudaSuccess) {
+    M->bar = nullptr;
+    cudaGetLastError();
+    return;
+  }
+  if (cudaMemsetAsync(M->bar, 0, sizeof(CoopBar), h->stream) != cudaSuccess) return;
+  M->coop_blocks = sms * std::min(b1, 2);
+  M->coop_blocks2 = sms * std::min(b2, 2);
+}
+
 // z += C G V G^T r   (NV = 1: real r, coefficient c00; NV = 2: planar complex,
 // z_0 += c00 v_0 + c01 v_1, z_1 += c10 v_0 + c11 v_1)
 template <typename T, int NV, int P>
@@ -921,7 +1178,9 @@ static void aux_apply_p(const hcop* h, AuxMG* M, const T* r0, const T* r1, T* z0
   const ChebStart none{nullptr, nullptr, nullptr, 0.0f};
   k_gt<T, NV, P><<<gq.grid, gq.block, 0, s>>>(hd, M->tab, r0, r1, qd, g, P > 1 ? none : start_of(L0), done);
   if (P > 1) k_rq<NV, P><<<g1.grid, g1.block, 0, s>>>(L0.d, M->tab, g, L0.dinv, L0.b, start_of(L0), done);
-  vcycle<NV>(h, M, 0, done, s);
+  cudaError_t ce = cudaSuccess;  // a failed launch is also the thread's last error, read by the caller
+  if (!vcycle_coop<NV>(h, M, done, s, &ce)) vcycle<NV>(h, M, 0, done, s);
+  (void)ce;
   const float* phi = L0.x;  // order 1: phi is the finest Q1 level's x
   if (P > 1) {
     k_pq<NV, P><<<gq.grid, gq.block, 0, s>>>(L0.d, M->tab, g, M->qdinv, L0.x, M->phi, done);
@@ -967,9 +1226,10 @@ cudaError_t auxmg_apply(const hcop* h, const T* r0, const T* r1, T* z0, T* z1, c
     return cudaGetLastError();
   }
   const void* key[5] = {r0, r1, z0, z1, done};
+  const int coop = coop_wanted() ? 1 : 0;
   for (AuxGraph& g : M->graphs) {
-    if (g.exec && g.nv == NV && g.tsize == (int)sizeof(T) && std::memcmp(g.key, key, sizeof(key)) == 0 &&
-        std::memcmp(g.coef, coef, sizeof(g.coef)) == 0)
+    if (g.exec && g.nv == NV && g.tsize == (int)sizeof(T) && g.coop == coop &&
+        std::memcmp(g.key, key, sizeof(key)) == 0 && std::memcmp(g.coef, coef, sizeof(g.coef)) == 0)
       return cudaGraphLaunch(g.exec, s);
   }
   if (!M->cap) {
@@ -1005,6 +1265,7 @@ cudaError_t auxmg_apply(const hcop* h, const T* r0, const T* r1, T* z0, T* z1, c
   std::memcpy(slot->coef, coef, sizeof(slot->coef));
   slot->nv = NV;
   slot->tsize = (int)sizeof(T);
+  slot->coop = coop;
   return cudaGraphLaunch(exec, s);
 }
 

@@ -283,7 +283,12 @@ hc_status lanczos_device(hcop* h, int steps, double* lmax);
 // Mixed precision: FP32 inner PCG in FP64 iterative refinement.
 hc_status mixed_device(hcop* h, const hc_solve_params* prm, const double* b, double* x,
                        hc_solve_info* info);
+// FP32 PCG with FP64 residual replacement (HC_MIXED_RR).
+hc_status mixed_rr_device(hcop* h, const hc_solve_params* prm, const double* b, double* x,
+                          hc_solve_info* info);
 hc_status ensure_work(hcop* h, size_t bytes);
+// z = D^-1 r (FP64, the handle's Jacobi diagonal)
+cudaError_t jacobi_apply(int64_t n, const double* dinv, const double* r, double* z, cudaStream_t s);
 cudaError_t ensure_scalars(hcop* h);
 double vec_norm2_host(hcop* h, const double* x, int64_t n);  // synchronous helper
 

@@ -22,6 +22,10 @@ namespace hc {
 #define GS_LOOP(i, n) \
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
 
+// Vector stride of the Krylov work space: every work vector starts on a
+// 256-byte boundary, so the 16-byte vector kernels apply to all of them.
+static inline int64_t vstride(int64_t n) { return (n + 63) & ~(int64_t)63; }
+
 static inline unsigned vgrid(int64_t n) {
   int64_t b = (n + kRedThreads - 1) / kRedThreads;
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, kRedBlocks));
@@ -286,6 +290,176 @@ __global__ void __launch_bounds__(kRedThreads)
   }
 }
 
+// ---- 16-byte forms of the per-iteration kernels ---------------------------
+// Same arithmetic as k_pcg_update / k_pcg_dir / k_rz_beta, on 16-byte chunks
+// (4 floats or 2 doubles) so that each thread keeps 5-6 wide loads in flight:
+// the scalar forms, one 4-byte load per vector per loop trip, are bound by
+// memory latency at 2 x 152 blocks.  All vectors 16-byte aligned; the last
+// n % W elements go through a scalar tail.
+template <typename T>
+struct Chunk16 {
+  static constexpr int W = (int)(16 / sizeof(T));
+  T v[W];
+  __device__ __forceinline__ void load(const T* __restrict__ p, int64_t c) {
+    const uint4 u = reinterpret_cast<const uint4*>(p)[c];
+    memcpy(v, &u, 16);
+  }
+  __device__ __forceinline__ void store(T* __restrict__ p, int64_t c) const {
+    uint4 u;
+    memcpy(&u, v, 16);
+    reinterpret_cast<uint4*>(p)[c] = u;
+  }
+};
+
+template <typename T, bool JAC>
+__global__ void __launch_bounds__(kRedThreads)
+    k_pcg_update_v(int64_t n, T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
+                   const T* __restrict__ q, const T* __restrict__ dinv, KrylovScalars* S, double* partials,
+                   T* __restrict__ zout) {
+  if (S->done) return;
+  constexpr int W = Chunk16<T>::W;
+  const T a = (T)S->alpha;
+  const int64_t nc = n / W, t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                st = (int64_t)gridDim.x * blockDim.x;
+  const bool needd = zout != nullptr || (JAC && dinv != nullptr);
+  T rrt = T(0), rzt = T(0);
+#pragma unroll 2
+  for (int64_t c = t0; c < nc; c += st) {
+    Chunk16<T> xv, rv, pv, qv, dv;
+    xv.load(x, c);
+    rv.load(r, c);
+    pv.load(p, c);
+    qv.load(q, c);
+    if (needd) dv.load(dinv, c);
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      xv.v[w] += a * pv.v[w];
+      const T ri = rv.v[w] - a * qv.v[w];
+      rv.v[w] = ri;
+      rrt += ri * ri;
+      if (JAC) rzt += ri * ri * (dinv ? dv.v[w] : T(1));
+      if (zout) dv.v[w] *= ri;
+    }
+    xv.store(x, c);
+    rv.store(r, c);
+    if (zout) dv.store(zout, c);
+  }
+  for (int64_t i = nc * W + t0; i < n; i += st) {
+    x[i] += a * p[i];
+    const T ri = r[i] - a * q[i];
+    r[i] = ri;
+    if (zout) zout[i] = dinv[i] * ri;
+    rrt += ri * ri;
+    if (JAC) rzt += ri * ri * (dinv ? dinv[i] : T(1));
+  }
+  double v[2] = {(double)rrt, (double)rzt}, tot[2];
+  block_sum_n<2>(v);
+  if (grid_sum_n<2>(v, partials, &S->counter[2], tot)) {
+    S->rr = tot[0];
+    S->it += 1;
+    if (!isfinite(tot[0])) {
+      S->done = 1;
+      S->status = HC_BREAKDOWN;
+    } else if (tot[0] <= S->tol2) {
+      S->done = 1;
+      S->status = HC_OK;
+    } else if (S->it >= S->maxit) {
+      S->done = 1;
+      S->status = HC_NOT_CONVERGED;
+    }
+    if (JAC) {
+      S->beta = tot[1] / S->rz;
+      S->rz = tot[1];
+    }
+  }
+}
+
+template <typename T, bool JAC>
+__global__ void __launch_bounds__(kRedThreads)
+    k_pcg_dir_v(int64_t n, const T* __restrict__ zr, const T* __restrict__ dinv, T* __restrict__ p,
+                T* __restrict__ q, const uint8_t* __restrict__ ess, KrylovScalars* S, double* partials) {
+  if (S->done) return;
+  constexpr int W = Chunk16<T>::W;
+  const T b = (T)S->beta;
+  const int64_t nc = n / W, t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                st = (int64_t)gridDim.x * blockDim.x;
+  double v[1] = {0.0}, tot[1];
+#pragma unroll 2
+  for (int64_t c = t0; c < nc; c += st) {
+    Chunk16<T> zv, pv, dv;
+    zv.load(zr, c);
+    pv.load(p, c);
+    if (JAC && dinv) dv.load(dinv, c);
+    uint8_t m[W];
+    if constexpr (W == 4) {
+      const uchar4 e4 = reinterpret_cast<const uchar4*>(ess)[c];
+      m[0] = e4.x, m[1] = e4.y, m[2] = e4.z, m[3] = e4.w;
+    } else {
+      const uchar2 e2 = reinterpret_cast<const uchar2*>(ess)[c];
+      m[0] = e2.x, m[1] = e2.y;
+    }
+    Chunk16<T> qv;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      const T z = JAC ? (dinv ? dv.v[w] * zv.v[w] : zv.v[w]) : zv.v[w];
+      const T pi = z + b * pv.v[w];
+      pv.v[w] = pi;
+      qv.v[w] = m[w] ? pi : T(0);
+      if (m[w]) v[0] += (double)pi * (double)pi;
+    }
+    pv.store(p, c);
+    qv.store(q, c);
+  }
+  for (int64_t i = nc * W + t0; i < n; i += st) {
+    const T z = JAC ? (dinv ? dinv[i] * zr[i] : zr[i]) : zr[i];
+    const T pi = z + b * p[i];
+    p[i] = pi;
+    const bool e = ess[i] != 0;
+    q[i] = e ? pi : T(0);
+    if (e) v[0] += (double)pi * (double)pi;
+  }
+  block_sum_n<1>(v);
+  if (grid_sum_n<1>(v, partials, &S->counter[3], tot)) S->pq = tot[0];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+    k_rz_beta_v(int64_t n, const T* __restrict__ r, const T* __restrict__ z, int first, KrylovScalars* S,
+                double* partials) {
+  if (S->done) return;
+  constexpr int W = Chunk16<T>::W;
+  const int64_t nc = n / W, t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                st = (int64_t)gridDim.x * blockDim.x;
+  T acc = T(0);
+#pragma unroll 4
+  for (int64_t c = t0; c < nc; c += st) {
+    Chunk16<T> rv, zv;
+    rv.load(r, c);
+    zv.load(z, c);
+#pragma unroll
+    for (int w = 0; w < W; ++w) acc += rv.v[w] * zv.v[w];
+  }
+  for (int64_t i = nc * W + t0; i < n; i += st) acc += r[i] * z[i];
+  double v[1] = {(double)acc}, tot[1];
+  block_sum_n<1>(v);
+  if (grid_sum_n<1>(v, partials, &S->counter[5], tot)) {
+    S->beta = first ? 0.0 : tot[0] / S->rz;
+    S->rz = tot[0];
+  }
+}
+
+static inline bool al16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// z = D^-1 r with no solver state (hc_precond_apply_device)
+__global__ void k_jacobi(int64_t n, const double* __restrict__ dinv, const double* __restrict__ r,
+                         double* __restrict__ z) {
+  GS_LOOP(i, n) z[i] = dinv[i] * r[i];
+}
+cudaError_t jacobi_apply(int64_t n, const double* dinv, const double* r, double* z, cudaStream_t s) {
+  k_jacobi<<<vgrid(n), kRedThreads, 0, s>>>(n, dinv, r, z);
+  return cudaGetLastError();
+}
+
 // z = D^-1 r (the Jacobi part of the auxiliary-space preconditioner)
 template <typename T>
 __global__ void k_jz(int64_t n, const T* __restrict__ r, const T* __restrict__ dinv, T* __restrict__ z,
@@ -513,7 +687,8 @@ hc_status lanczos_device(hcop* h, int steps, double* lmax, T* wk) {
   HC_CUDA_TRY(h, ensure_scalars(h));
   const int64_t n = h->ndof;
   cudaStream_t s = h->stream;
-  T *v = wk, *vp = wk + n, *w = wk + 2 * n, *tmp = wk + 3 * n;
+  const int64_t np = vstride(n);
+  T *v = wk, *vp = wk + np, *w = wk + 2 * np, *tmp = wk + 3 * np;
   KrylovScalars* S = h->scal;
   const unsigned g = vgrid(n);
   const OpJ<T> op{h, fac_of<T>(h)};
@@ -548,21 +723,33 @@ hc_status lanczos_device(hcop* h, int steps, double* lmax, T* wk) {
 
 template <typename T>
 hc_status lanczos_device(hcop* h, int steps, double* lmax) {
-  hc_status st = ensure_work(h, (size_t)4 * h->ndof * sizeof(T));
+  hc_status st = ensure_work(h, (size_t)4 * vstride(h->ndof) * sizeof(T));
   if (st != HC_OK) return st;
   return lanczos_device<T>(h, steps, lmax, (T*)h->work);
 }
 template hc_status lanczos_device<double>(hcop*, int, double*);
 template hc_status lanczos_device<float>(hcop*, int, double*);
 
+// Host callback of pcg_run at each batch boundary, after the scalars were
+// read back into hs.  Returns kHookGoOn (stop or go on as hs says),
+// kHookResumed (the callback changed the iterate and cleared S->done and
+// hs->done: iterate on) or kHookStop.
+enum { kHookGoOn = 0, kHookResumed = 1, kHookStop = 2 };
+struct ChunkHook {
+  virtual int at_batch(KrylovScalars* hs) = 0;
+  virtual ~ChunkHook() = default;
+};
+
 // Preconditioned CG; wk holds 6 n-vectors of T.
 template <typename T>
-static hc_status pcg_run(hcop* h, const SolveCfg& cfg, const T* b, T* x, T* wk, int* iters, int* applies) {
+static hc_status pcg_run(hcop* h, const SolveCfg& cfg, const T* b, T* x, T* wk, int* iters, int* applies,
+                         ChunkHook* hook = nullptr) {
   HC_CUDA_TRY(h, ensure_scalars(h));
   const int64_t n = h->ndof;
   cudaStream_t s = h->stream;
   KrylovScalars* S = h->scal;
-  T *r = wk, *p = wk + n, *q = wk + 2 * n, *z = wk + 3 * n, *dk = wk + 4 * n, *w = wk + 5 * n;
+  const int64_t np = vstride(n);
+  T *r = wk, *p = wk + np, *q = wk + 2 * np, *z = wk + 3 * np, *dk = wk + 4 * np, *w = wk + 5 * np;
   const unsigned g = vgrid(n);
   const OpJ<T> op{h, fac_of<T>(h)};
   const T* dinv = dinv_of<T>(h);
@@ -636,15 +823,27 @@ static hc_status pcg_run(hcop* h, const SolveCfg& cfg, const T* b, T* x, T* wk, 
   }
   HC_CUDA_TRY(h, cudaGetLastError());
 
+  // 16-byte kernels when every vector they touch is aligned (the work
+  // vectors always are; x is the caller's)
+  const bool wide = al16(x) && al16(dinv) && (reinterpret_cast<uintptr_t>(h->ess) % (16 / sizeof(T))) == 0;
+  const unsigned gv = vgrid((n + Chunk16<T>::W - 1) / Chunk16<T>::W);
   const int chunk = 25;
   int launched = 0;
   for (;;) {
     for (int k = 0; k < chunk && launched < cfg.maxit; ++k, ++launched) {
       HC_CUDA_TRY(h, op.apply(p, q, S, part, s));
       ++napply;
-      if (jac) {
+      if (jac && wide) {
+        k_pcg_update_v<T, true><<<gv, kRedThreads, 0, s>>>(n, x, r, p, q, dj, S, part, nullptr);
+        k_pcg_dir_v<T, true><<<gv, kRedThreads, 0, s>>>(n, r, dj, p, q, h->ess, S, part);
+      } else if (jac) {
         k_pcg_update<T, true><<<g, kRedThreads, 0, s>>>(n, x, r, p, q, dj, S, part);
         k_pcg_dir<T, true><<<g, kRedThreads, 0, s>>>(n, r, dj, p, q, h->ess, S, part);
+      } else if (wide) {
+        k_pcg_update_v<T, false><<<gv, kRedThreads, 0, s>>>(n, x, r, p, q, dinv, S, part, aux ? z : nullptr);
+        HC_CUDA_TRY(h, precond(aux));
+        k_rz_beta_v<T><<<gv, kRedThreads, 0, s>>>(n, r, z, 0, S, part);
+        k_pcg_dir_v<T, false><<<gv, kRedThreads, 0, s>>>(n, z, dinv, p, q, h->ess, S, part);
       } else {
         k_pcg_update<T, false><<<g, kRedThreads, 0, s>>>(n, x, r, p, q, dinv, S, part, aux ? z : nullptr);
         HC_CUDA_TRY(h, precond(aux));
@@ -655,6 +854,11 @@ static hc_status pcg_run(hcop* h, const SolveCfg& cfg, const T* b, T* x, T* wk, 
     HC_CUDA_TRY(h, cudaGetLastError());
     HC_CUDA_TRY(h, cudaMemcpyAsync(hs, S, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, s));
     HC_CUDA_TRY(h, cudaStreamSynchronize(s));
+    if (hook) {
+      const int a = hook->at_batch(hs);
+      if (a == kHookStop) break;
+      if (a == kHookResumed && launched < cfg.maxit) continue;
+    }
     if (hs->done || launched >= cfg.maxit) break;
   }
   *iters = hs->it;
@@ -667,64 +871,132 @@ template <typename T>
 hc_status pcg_device(hcop* h, const SolveCfg& cfg, const T* b, T* x, int* iters, int* applies,
                      double* unused) {
   (void)unused;
-  hc_status st = ensure_work(h, (size_t)6 * h->ndof * sizeof(T));
+  hc_status st = ensure_work(h, (size_t)6 * vstride(h->ndof) * sizeof(T));
   if (st != HC_OK) return st;
   return pcg_run<T>(h, cfg, b, x, (T*)h->work, iters, applies);
 }
 template hc_status pcg_device<double>(hcop*, const SolveCfg&, const double*, double*, int*, int*, double*);
 template hc_status pcg_device<float>(hcop*, const SolveCfg&, const float*, float*, int*, int*, double*);
 
+// r64 = b - J x in FP64; ||r64||^2 and ||b||^2 read back to the host.
+static hc_status resid64(hcop* h, const double* b, const double* x, double* r64, double* rn2, double* bn2) {
+  const int64_t n = h->ndof;
+  cudaStream_t s = h->stream;
+  const OpJ<double> op64{h, h->fac};
+  HC_CUDA_TRY(h, init_masked<double>(n, h->ess, x, r64, s));
+  HC_CUDA_TRY(h, op64.apply(x, r64, nullptr, nullptr, s));
+  k_resid64<<<vgrid(n), kRedThreads, 0, s>>>(n, b, r64, h->scal, h->partials);
+  HC_CUDA_TRY(h, cudaGetLastError());
+  HC_CUDA_TRY(h, cudaMemcpyAsync(h->hscal, h->scal, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, s));
+  HC_CUDA_TRY(h, cudaStreamSynchronize(s));
+  *rn2 = h->hscal->rr;
+  *bn2 = h->hscal->bb;
+  return HC_OK;
+}
+
+// The FP32 inner solver's settings (Chebyshev bound estimated in FP32 once per handle).
+static hc_status inner_cfg(hcop* h, const hc_solve_params* prm, double rtol, float* wk, SolveCfg* in) {
+  in->precond = prm->precond;
+  in->cheb_degree = prm->cheb_degree > 0 ? prm->cheb_degree : 2;
+  in->cheb_ratio = prm->cheb_ratio > 0 ? prm->cheb_ratio : 30.0;
+  in->rtol = rtol;
+  in->atol = 0.0;
+  in->lmax = prm->cheb_lmax;
+  if (in->precond == HC_PRECOND_CHEBYSHEV && in->lmax <= 0) {
+    if (h->lmax32 <= 0) {
+      double lm = 0;
+      const hc_status st = lanczos_device<float>(h, 20, &lm, wk);
+      if (st != HC_OK) return st;
+      h->lmax32 = 1.1 * lm;
+    }
+    in->lmax = h->lmax32;
+  }
+  return HC_OK;
+}
+
+// FP64 polish: PCG on J x = b from the current x, after the FP32 iteration
+// reached its accuracy floor.  The work layout grows to
+// r64 | 8n floats | 6n doubles (the FP64 PCG vectors, also Lanczos space).
+// Returns the solve's status, judged on the true residual (rn2, bn2 out).
+static hc_status polish64(hcop* h, const hc_solve_params* prm, const SolveCfg& in, const double* b, double* x,
+                          double tol, int* iters, int* applies, int* outer, double* rn2, double* bn2) {
+  const int64_t n = h->ndof;
+  const int64_t np = vstride(n);
+  hc_status st = ensure_work(h, (size_t)np * sizeof(double) + (size_t)8 * np * sizeof(float) +
+                                    (size_t)6 * np * sizeof(double));
+  if (st != HC_OK) return st;
+  double* r64 = (double*)h->work;
+  double* wk64 = (double*)((char*)h->work + (size_t)np * sizeof(double) + (size_t)8 * np * sizeof(float));
+  SolveCfg c64;
+  c64.precond = prm->precond;
+  c64.cheb_degree = in.cheb_degree;
+  c64.cheb_ratio = in.cheb_ratio;
+  c64.lmax = prm->cheb_lmax;
+  if (c64.precond == HC_PRECOND_CHEBYSHEV && c64.lmax <= 0) {
+    if (h->lmax64 <= 0) {
+      double lm = 0;
+      st = lanczos_device<double>(h, 20, &lm, wk64);
+      if (st != HC_OK) return st;
+      h->lmax64 = 1.1 * lm;
+    }
+    c64.lmax = h->lmax64;
+  }
+  // aim below the tolerance: the polish stops on its recursive residual,
+  // the status is judged on the true residual below
+  c64.rtol = 0.5 * prm->rtol;
+  c64.atol = 0.5 * prm->atol;
+  c64.maxit = prm->maxit - *iters;
+  int it = 0, ap = 0;
+  const hc_status pst = pcg_run<double>(h, c64, b, x, wk64, &it, &ap);
+  *iters += it;
+  *applies += ap + 1;
+  ++*outer;
+  if (pst == HC_ECUDA || pst == HC_ENOMEM) return pst;
+  st = resid64(h, b, x, r64, rn2, bn2);
+  if (st != HC_OK) return st;
+  if (!std::isfinite(std::sqrt(*rn2))) return HC_BREAKDOWN;
+  if (pst == HC_BREAKDOWN) return pst;
+  return std::sqrt(*rn2) <= tol ? HC_OK : HC_NOT_CONVERGED;
+}
+
+static void fill_info(hc_solve_info* info, hc_status result, int iters, int outer, int applies, double rn2,
+                      double bn2, double lmax) {
+  if (!info) return;
+  info->status = result;
+  info->iterations = iters;
+  info->outer_iterations = outer;
+  info->applies = applies;
+  const double bn = std::sqrt(bn2);
+  info->rel_residual = bn > 0 ? std::sqrt(rn2) / bn : std::sqrt(rn2);
+  info->lmax = lmax;
+}
+
 // FP32 inner PCG inside FP64 iterative refinement.
 hc_status mixed_device(hcop* h, const hc_solve_params* prm, const double* b, double* x, hc_solve_info* info) {
   const int64_t n = h->ndof;
   // layout: r64 (n doubles) | rf, cf (2n floats) | 6n floats of PCG work
-  const size_t bytes = (size_t)n * sizeof(double) + (size_t)8 * n * sizeof(float);
+  const int64_t np = vstride(n);
+  const size_t bytes = (size_t)np * sizeof(double) + (size_t)8 * np * sizeof(float);
   hc_status st = ensure_work(h, bytes);
   if (st != HC_OK) return st;
   HC_CUDA_TRY(h, ensure_scalars(h));
   double* r64 = (double*)h->work;
-  float* rf = (float*)(r64 + n);
-  float* cf = rf + n;
-  float* wk = cf + n;
+  float* rf = (float*)(r64 + np);
+  float* cf = rf + np;
+  float* wk = cf + np;
   cudaStream_t s = h->stream;
   const unsigned g = vgrid(n);
-  const OpJ<double> op64{h, h->fac};
-  KrylovScalars* S = h->scal;
   int applies = 0, iters = 0, outer = 0;
 
   SolveCfg in;
-  in.precond = prm->precond;
-  in.cheb_degree = prm->cheb_degree > 0 ? prm->cheb_degree : 2;
-  in.cheb_ratio = prm->cheb_ratio > 0 ? prm->cheb_ratio : 30.0;
-  in.rtol = prm->inner_rtol > 0 ? prm->inner_rtol : 1e-4;
-  in.atol = 0.0;
-  in.lmax = prm->cheb_lmax;
-  if (in.precond == HC_PRECOND_CHEBYSHEV && in.lmax <= 0) {
-    if (h->lmax32 <= 0) {
-      double lm = 0;
-      st = lanczos_device<float>(h, 20, &lm, wk);
-      if (st != HC_OK) return st;
-      h->lmax32 = 1.1 * lm;
-    }
-    in.lmax = h->lmax32;
-  }
+  st = inner_cfg(h, prm, prm->inner_rtol > 0 ? prm->inner_rtol : 1e-4, wk, &in);
+  if (st != HC_OK) return st;
   const int max_outer = prm->max_outer > 0 ? prm->max_outer : 50;
 
-  auto residual = [&](double* rn2, double* bn2) -> hc_status {
-    HC_CUDA_TRY(h, init_masked<double>(n, h->ess, x, r64, s));
-    HC_CUDA_TRY(h, op64.apply(x, r64, nullptr, nullptr, s));
-    ++applies;
-    k_resid64<<<g, kRedThreads, 0, s>>>(n, b, r64, S, h->partials);
-    HC_CUDA_TRY(h, cudaGetLastError());
-    HC_CUDA_TRY(h, cudaMemcpyAsync(h->hscal, S, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, s));
-    HC_CUDA_TRY(h, cudaStreamSynchronize(s));
-    *rn2 = h->hscal->rr;
-    *bn2 = h->hscal->bb;
-    return HC_OK;
-  };
   double rn2 = 0, bn2 = 0;
-  st = residual(&rn2, &bn2);
+  st = resid64(h, b, x, r64, &rn2, &bn2);
   if (st != HC_OK) return st;
+  ++applies;
   const double bn = std::sqrt(bn2);
   const double tol = std::max(prm->rtol * bn, prm->atol);
   hc_status result = HC_NOT_CONVERGED;
@@ -764,55 +1036,184 @@ hc_status mixed_device(hcop* h, const hc_solve_params* prm, const double* b, dou
     }
     k_axpy_f2d<<<g, kRedThreads, 0, s>>>(n, cf, x, rn);
     HC_CUDA_TRY(h, cudaGetLastError());
-    st = residual(&rn2, &bn2);
+    st = resid64(h, b, x, r64, &rn2, &bn2);
     if (st != HC_OK) return st;
+    ++applies;
   }
-  if (stalled && iters < prm->maxit) {
-    // FP64 polish: PCG on J x = b from the refined x.  Work layout grows to
-    // r64 | 8n floats | 6n doubles (the FP64 PCG vectors, also Lanczos space).
-    st = ensure_work(h, (size_t)n * sizeof(double) + (size_t)8 * n * sizeof(float) + (size_t)6 * n * sizeof(double));
-    if (st != HC_OK) return st;
-    r64 = (double*)h->work;
-    double* wk64 = (double*)((char*)h->work + (size_t)n * sizeof(double) + (size_t)8 * n * sizeof(float));
-    SolveCfg c64;
-    c64.precond = prm->precond;
-    c64.cheb_degree = in.cheb_degree;
-    c64.cheb_ratio = in.cheb_ratio;
-    c64.lmax = prm->cheb_lmax;
-    if (c64.precond == HC_PRECOND_CHEBYSHEV && c64.lmax <= 0) {
-      if (h->lmax64 <= 0) {
-        double lm = 0;
-        st = lanczos_device<double>(h, 20, &lm, wk64);
-        if (st != HC_OK) return st;
-        h->lmax64 = 1.1 * lm;
-      }
-      c64.lmax = h->lmax64;
+  if (stalled && iters < prm->maxit)
+    result = polish64(h, prm, in, b, x, tol, &iters, &applies, &outer, &rn2, &bn2);
+  if (result == HC_ECUDA || result == HC_ENOMEM) return result;
+  fill_info(info, result, iters, outer, applies, rn2, bn2, in.lmax);
+  return result;
+}
+
+// S->rr = rr (the replaced residual's norm); the iteration goes on.
+__global__ void k_resume(KrylovScalars* S, double rr) {
+  S->rr = rr;
+  S->done = 0;
+  S->status = HC_NOT_CONVERGED;
+}
+
+// One FP32 PCG with FP64 residual replacement and grouped solution updates
+// (H. A. van der Vorst and Q. Ye, "Residual replacement strategies for Krylov
+// subspace iterative methods for the convergence of true residuals", SIAM J.
+// Sci. Comput. 22 (2000) 835-852; used for mixed precision as the "reliable
+// updates" of M. A. Clark et al., Comput. Phys. Commun. 181 (2010) 1517-1528).
+// At a batch boundary where the FP32 recursive residual fell by `delta` since
+// the last replacement, or met the tolerance: the FP32 correction (scaled by
+// the initial residual norm) is added to the FP64 solution, b - J x is
+// computed in FP64 and replaces the FP32 recursive residual.  The search
+// direction and r.z are kept: unlike iterative refinement, the Krylov space
+// is not restarted.  Two replacements in a row that do not halve the true
+// residual mark the FP32 accuracy floor of the operator.
+struct ReplaceHook : ChunkHook {
+  hcop* h;
+  const double* b;
+  double* x;
+  double* r64;
+  float* rp;  // the FP32 PCG's residual vector
+  float* cf;  // the FP32 correction since the last replacement
+  double scale, tol, delta2, rr_last, rn_prev;
+  int slow = 0, replacements = 0, applies = 0, since = 0;
+  bool converged = false, stalled = false;
+  bool pending = true;  // cf holds a correction not yet added to x
+  hc_status err = HC_OK;
+  double rn2 = 0, bn2 = 0;
+
+  int at_batch(KrylovScalars* hs) override {
+    if (hs->done && hs->status == HC_BREAKDOWN) return kHookGoOn;
+    // due: converged or capped, the recursive residual fell by delta, or 8
+    // batches (200 iterations) without that (an FP32 iteration that stopped
+    // converging is caught by the stall test below)
+    if (!hs->done && !(hs->rr <= delta2 * rr_last) && ++since < 8) return kHookGoOn;
+    since = 0;
+    const int64_t n = h->ndof;
+    cudaStream_t s = h->stream;
+    const unsigned g = vgrid(n);
+    k_axpy_f2d<<<g, kRedThreads, 0, s>>>(n, cf, x, scale);
+    cudaError_t e = cudaMemsetAsync(cf, 0, n * sizeof(float), s);
+    if (e != cudaSuccess) {
+      h->err = cudaGetErrorString(e);
+      err = HC_ECUDA;
+      return kHookStop;
     }
-    // aim below the tolerance: the polish stops on its recursive residual,
-    // the status is judged on the true residual below
-    c64.rtol = 0.5 * prm->rtol;
-    c64.atol = 0.5 * prm->atol;
-    c64.maxit = prm->maxit - iters;
-    int it = 0, ap = 0;
-    const hc_status pst = pcg_run<double>(h, c64, b, x, wk64, &it, &ap);
-    iters += it;
-    applies += ap;
-    ++outer;
-    if (pst == HC_ECUDA || pst == HC_ENOMEM) return pst;
-    st = residual(&rn2, &bn2);
+    err = resid64(h, b, x, r64, &rn2, &bn2);
+    if (err != HC_OK) return kHookStop;
+    pending = false;
+    ++applies;
+    ++replacements;
+    const double rn = std::sqrt(rn2);
+    if (!std::isfinite(rn)) {
+      err = HC_BREAKDOWN;
+      return kHookStop;
+    }
+    if (rn <= tol) {
+      converged = true;
+      return kHookStop;
+    }
+    if (hs->done && hs->it >= hs->maxit) return kHookStop;
+    slow = rn > 0.5 * rn_prev ? slow + 1 : 0;
+    rn_prev = rn;
+    if (slow >= 2) {
+      stalled = true;
+      return kHookStop;
+    }
+    k_d2f_scaled<<<g, kRedThreads, 0, s>>>(n, r64, rp, 1.0 / scale);
+    const double rr = rn2 / (scale * scale);
+    k_resume<<<1, 1, 0, s>>>(h->scal, rr);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      h->err = cudaGetErrorString(e);
+      err = HC_ECUDA;
+      return kHookStop;
+    }
+    pending = true;
+    hs->rr = rr;
+    hs->done = 0;
+    hs->status = HC_NOT_CONVERGED;
+    rr_last = rr;
+    return kHookResumed;
+  }
+};
+
+hc_status mixed_rr_device(hcop* h, const hc_solve_params* prm, const double* b, double* x, hc_solve_info* info) {
+  const int64_t n = h->ndof;
+  // layout: r64 (n doubles) | rf, cf (2n floats) | 6n floats of PCG work (r first)
+  const int64_t np = vstride(n);
+  const size_t bytes = (size_t)np * sizeof(double) + (size_t)8 * np * sizeof(float);
+  hc_status st = ensure_work(h, bytes);
+  if (st != HC_OK) return st;
+  HC_CUDA_TRY(h, ensure_scalars(h));
+  double* r64 = (double*)h->work;
+  float* rf = (float*)(r64 + np);
+  float* cf = rf + np;
+  float* wk = cf + np;
+  cudaStream_t s = h->stream;
+  int applies = 0, iters = 0, outer = 0;
+
+  double rn2 = 0, bn2 = 0;
+  st = resid64(h, b, x, r64, &rn2, &bn2);
+  if (st != HC_OK) return st;
+  ++applies;
+  const double rn0 = std::sqrt(rn2), bn = std::sqrt(bn2);
+  const double tol = std::max(prm->rtol * bn, prm->atol);
+  SolveCfg in;
+  // the FP32 stopping test, on the recursive residual in units of ||r0||
+  st = inner_cfg(h, prm, rn0 > 0 ? 0.5 * tol / rn0 : 0.0, wk, &in);
+  if (st != HC_OK) return st;
+  if (!std::isfinite(rn0)) {
+    fill_info(info, HC_BREAKDOWN, 0, 0, applies, rn2, bn2, in.lmax);
+    return HC_BREAKDOWN;
+  }
+  if (rn0 <= tol) {
+    fill_info(info, HC_OK, 0, 0, applies, rn2, bn2, in.lmax);
+    return HC_OK;
+  }
+  const double delta = prm->inner_rtol > 0 ? std::min(prm->inner_rtol, 0.5) : 0.1;
+  ReplaceHook hk;
+  hk.h = h;
+  hk.b = b;
+  hk.x = x;
+  hk.r64 = r64;
+  hk.rp = wk;
+  hk.cf = cf;
+  hk.scale = rn0;
+  hk.tol = tol;
+  hk.delta2 = delta * delta;
+  hk.rr_last = 1.0;
+  hk.rn_prev = rn0;
+  k_d2f_scaled<<<vgrid(n), kRedThreads, 0, s>>>(n, r64, rf, 1.0 / rn0);
+  HC_CUDA_TRY(h, cudaMemsetAsync(cf, 0, n * sizeof(float), s));
+  in.maxit = prm->maxit;
+  int it = 0, ap = 0;
+  const hc_status ist = pcg_run<float>(h, in, rf, cf, wk, &it, &ap, &hk);
+  iters += it;
+  applies += ap + hk.applies;
+  outer = hk.replacements;
+  if (hk.err != HC_OK) {
+    if (hk.err == HC_ECUDA || hk.err == HC_ENOMEM) return hk.err;
+    fill_info(info, hk.err, iters, outer, applies, hk.rn2, hk.bn2, in.lmax);
+    return hk.err;
+  }
+  if (ist == HC_ECUDA || ist == HC_ENOMEM) return ist;
+  rn2 = hk.rn2;
+  bn2 = hk.bn2;
+  if (hk.pending) {
+    // the FP32 correction since the last replacement (iteration cap, breakdown)
+    k_axpy_f2d<<<vgrid(n), kRedThreads, 0, s>>>(n, cf, x, rn0);
+    HC_CUDA_TRY(h, cudaGetLastError());
+    st = resid64(h, b, x, r64, &rn2, &bn2);
     if (st != HC_OK) return st;
-    if (!std::isfinite(std::sqrt(rn2))) result = HC_BREAKDOWN;
-    else if (pst == HC_BREAKDOWN) result = pst;
-    else result = std::sqrt(rn2) <= tol ? HC_OK : HC_NOT_CONVERGED;
+    ++applies;
   }
-  if (info) {
-    info->status = result;
-    info->iterations = iters;
-    info->outer_iterations = outer;
-    info->applies = applies;
-    info->rel_residual = bn > 0 ? std::sqrt(rn2) / bn : std::sqrt(rn2);
-    info->lmax = in.lmax;
-  }
+  hc_status result = HC_NOT_CONVERGED;
+  if (!std::isfinite(std::sqrt(rn2))) result = HC_BREAKDOWN;
+  else if (std::sqrt(rn2) <= tol) result = HC_OK;
+  else if (ist == HC_BREAKDOWN) result = HC_BREAKDOWN;
+  else if (hk.stalled && iters < prm->maxit)
+    result = polish64(h, prm, in, b, x, tol, &iters, &applies, &outer, &rn2, &bn2);
+  if (result == HC_ECUDA || result == HC_ENOMEM) return result;
+  fill_info(info, result, iters, outer, applies, rn2, bn2, in.lmax);
   return result;
 }
 

@@ -424,6 +424,12 @@ class HCurlOperator:
                 self.h)
         return yr, yi
 
+    def PrecondApplyDevice(self, r, z, precond="aux"):
+        """z = B r (device FP64 tensors): precond 'jacobi' (D^-1) or 'aux' (D^-1 + G V G^T)."""
+        N.check(N.lib().hc_precond_apply_device(self.h, _PRECOND[precond], _dev_ptr(r, "float64"),
+                                                _dev_ptr(z, "float64")), self.h)
+        return z
+
     def LanczosLmax(self, steps=20):
         v = C.c_double(0)
         N.check(N.lib().hc_lanczos_lmax(self.h, steps, C.byref(v)), self.h)
@@ -432,7 +438,7 @@ class HCurlOperator:
 
 _PRECOND = {"none": N.HC_PRECOND_NONE, "jacobi": N.HC_PRECOND_JACOBI, "chebyshev": N.HC_PRECOND_CHEBYSHEV,
             "aux": N.HC_PRECOND_AUX}
-_PREC = {"fp64": N.HC_FP64, "mixed": N.HC_MIXED}
+_PREC = {"fp64": N.HC_FP64, "mixed": N.HC_MIXED, "mixed_rr": N.HC_MIXED_RR}
 
 
 class GpuHCurlPCGSolver:
@@ -440,10 +446,12 @@ class GpuHCurlPCGSolver:
 
     Options (defaults as DefaultJacobiPCGSolver, hephaestus_solvers.hpp:34-57):
       Tolerance (1e-9), AbsTolerance (1e-16), MaxIter (1000), PrintLevel (ignored),
-    plus: Precision ('fp64' | 'mixed'), Preconditioner ('jacobi' |
+    plus: Precision ('fp64' | 'mixed' | 'mixed_rr': one FP32 PCG with FP64
+    residual replacement), Preconditioner ('jacobi' |
     'chebyshev' | 'aux' | 'none'; 'aux' = Jacobi + the auxiliary-space
     gradient correction, the gradient part of AMS), ChebyshevDegree (2), ChebyshevRatio (30),
-    ChebyshevLmax (0 = estimate), InnerTolerance (1e-4), MaxOuter (50).
+    ChebyshevLmax (0 = estimate), InnerTolerance (1e-4; for 'mixed_rr' the
+    residual reduction between replacements, 0.1), MaxOuter (50).
     """
 
     def __init__(self, params=None, op=None):
@@ -457,7 +465,8 @@ class GpuHCurlPCGSolver:
         self.p.rtol = float(params.get("Tolerance", 1e-9))
         self.p.atol = float(params.get("AbsTolerance", 1e-16))
         self.p.maxit = int(params.get("MaxIter", 1000))
-        self.p.inner_rtol = float(params.get("InnerTolerance", 1e-4))
+        rr = self.p.precision == N.HC_MIXED_RR
+        self.p.inner_rtol = float(params.get("InnerTolerance", 0.1 if rr else 1e-4))
         self.p.max_outer = int(params.get("MaxOuter", 50))
         self.op = op
         self.info = N.SolveInfo()

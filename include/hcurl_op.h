@@ -64,8 +64,12 @@ enum {
   HC_FP64 = 0,   /* plain FP64 operator and PCG (the drop-in path)        */
   HC_FP32 = 1,   /* FP32 operator and vectors, FP64 dots and alpha/beta   */
   HC_MIXED = 2,  /* FP32 inner PCG inside FP64 iterative refinement       */
-  HC_BF16 = 3    /* tet multi-RHS apply: BF16 element matrices, FP32
+  HC_BF16 = 3,   /* tet multi-RHS apply: BF16 element matrices, FP32
                     vectors and accumulation                               */
+  HC_MIXED_RR = 4 /* one FP32 PCG whose recursive residual is replaced by
+                    the FP64 residual b - J x (and its correction added to
+                    the FP64 x) each time it fell by inner_rtol; single
+                    right-hand-side solves (hc_solve_device)               */
 };
 
 /* HC_PRECOND_AUX: Jacobi plus the auxiliary-space gradient correction
@@ -107,14 +111,17 @@ typedef struct {
   double cheb_lmax;         /* upper eigenvalue bound of D^-1 J; <= 0 -> estimate  */
   double rtol, atol;        /* stop when ||b - J x|| <= max(rtol ||b||, atol)      */
   int32_t maxit;            /* max PCG iterations (inner iterations in total)      */
-  double inner_rtol;        /* HC_MIXED: inner FP32 solve tolerance (<= 0 -> 1e-4)  */
+  double inner_rtol;        /* HC_MIXED: inner FP32 solve tolerance (<= 0 -> 1e-4);
+                               HC_MIXED_RR: residual reduction between
+                               replacements (<= 0 -> 0.1, capped at 0.5)      */
   int32_t max_outer;        /* HC_MIXED: max refinement steps (<= 0 -> 50)          */
 } hc_solve_params;
 
 typedef struct {
   int32_t status;           /* hc_status of the solve                              */
   int32_t iterations;       /* total PCG iterations                                */
-  int32_t outer_iterations; /* refinement steps (HC_MIXED), else 1                 */
+  int32_t outer_iterations; /* refinement steps (HC_MIXED), residual replacements
+                               (HC_MIXED_RR), else 1                           */
   int32_t applies;          /* operator applications                               */
   double rel_residual;      /* ||b - J x||_2 / ||b||_2 in FP64 at exit             */
   double lmax;              /* Chebyshev upper bound used                          */
@@ -385,6 +392,12 @@ hc_status hc_solve_device(hcop_t* h, const hc_solve_params* prm, const double* b
 /* Largest eigenvalue estimate of D^-1 J by `steps` Lanczos steps started from
  * v_i = frac(i * 0.6180339887498949) - 1/2.                                */
 hc_status hc_lanczos_lmax(hcop_t* h, int steps, double* lmax);
+/* z = B r for one preconditioner of the PCG above (device FP64 vectors):
+ * HC_PRECOND_JACOBI (B = D^-1) or HC_PRECOND_AUX on hex handles (B = D^-1 +
+ * G V G^T, the gradient part of the HypreAMS application, HypreAMS::Mult as
+ * the reference's PCG calls it, hcurl_formulation.cpp:69-79).  Lets a caller's
+ * own Krylov solver use the library's preconditioner.                      */
+hc_status hc_precond_apply_device(hcop_t* h, int32_t precond, const double* r, double* z);
 
 #ifdef __cplusplus
 }

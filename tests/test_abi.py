@@ -79,6 +79,7 @@ def test_null_arguments_return_einval():
     assert L.hc_be_rhs_device(None, None, None, None) == N.HC_EINVAL
     assert L.hc_be_update_device(None, None, None) == N.HC_EINVAL
     assert L.hc_be_steps_device(None, None, 1, None, None, None, None, None) == N.HC_EINVAL
+    assert L.hc_precond_apply_device(None, N.HC_PRECOND_AUX, None, None) == N.HC_EINVAL
 
 
 def test_mfem_shim_compiles_against_stub():

@@ -146,3 +146,39 @@ def test_aux_cocg_converges_at_low_frequency_where_jacobi_stalls():
         res[pre] = (s.result["status"], s.result["iterations"])
     assert res["aux"][0] == "OK", res
     assert res["jacobi"][0] != "OK" or res["jacobi"][1] > 3 * res["aux"][1], res
+
+
+@pytest.mark.parametrize("n, p", [(40, 2), (24, 1), (17, 3)])
+def test_cooperative_vcycle_equals_per_step_kernels(n, p, monkeypatch):
+    """The Q1 V-cycle as one cooperative launch (grid barriers between steps)
+    runs the same steps with the same per-node arithmetic as the per-step
+    kernels (HC_AUX_VCYCLE=kernels): on one handle, z = B r through
+    hc_precond_apply_device is bit-identical (no atomics on this path), on
+    hierarchies of 3-4 levels and odd grid sizes; and B is D^-1 plus a
+    positive semi-definite correction (r.(z - D^-1 r) >= 0 up to the
+    V-cycle's FP32 rounding)."""
+    import torch
+
+    rng = np.random.default_rng(8 + p)
+    ne = n ** 3
+    op = HCurlOperator(n, n, n, p, meshes.loguniform(ne, 1.0, 1e3, rng), meshes.loguniform(ne, 1e-2, 1e6, rng),
+                       dt=0.01, ess_attr_bits=0x3F)
+    r = torch.tensor(np.random.default_rng(3).standard_normal(op.ndof), device="cuda")
+    r2 = torch.tensor(np.random.default_rng(4).standard_normal(op.ndof), device="cuda")
+    zs = {}
+    for mode in ("coop", "kernels", "coop"):
+        monkeypatch.setenv("HC_AUX_VCYCLE", mode)
+        z, z2 = torch.empty_like(r), torch.empty_like(r)
+        op.PrecondApplyDevice(r, z, "aux")
+        op.PrecondApplyDevice(r2, z2, "aux")
+        torch.cuda.synchronize()
+        zs.setdefault(mode, []).append((z.cpu().numpy(), z2.cpu().numpy()))
+    zj = torch.empty_like(r)
+    op.PrecondApplyDevice(r, zj, "jacobi")
+    for k in (0, 1):
+        a, b = zs["coop"][0][k], zs["kernels"][0][k]
+        d = np.abs(a - b)
+        assert np.array_equal(a, b), (k, int(np.count_nonzero(d)), float(d.max() / np.abs(b).max()), int(np.argmax(d)))
+        assert np.array_equal(a, zs["coop"][1][k])  # replays are reproducible
+    rh, z = r.cpu().numpy(), zs["coop"][0][0]
+    assert rh @ (z - zj.cpu().numpy()) >= -1e-6 * abs(rh @ z)

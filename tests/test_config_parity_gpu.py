@@ -12,7 +12,9 @@
   auxiliary-space preconditioner against the oracle's sparse direct solve;
   and on a 32^3 slice: the oracle's independently assembled operator
   certifies the true residual of the mixed solution, and mixed agrees with
-  the FP64-refined FP64 solution within 1e-10.
+  the FP64-refined FP64 solution within 1e-10.  "mixed" is FP32 PCG inside
+  FP64 iterative refinement, "mixed_rr" one FP32 PCG with FP64 residual
+  replacement.
 * Tets (config 3's mesh family and fields): Kuhn 8^3, p = 2, 16 seeded coil
   right-hand sides solved together (block PCG, mixed precision, tet
   auxiliary-space AMG), column by column against the oracle's direct solve.
@@ -106,13 +108,20 @@ def test_config1_fp64_pcg_matches_oracle_pcg():
     assert _rel(op.Curl(x), op.Curl(xt)) <= 1e-8
 
 
-def test_config1_mixed_meets_the_fp64_floor():
-    """Mixed precision on config 1 (the FP32 inner solves stall on the air
+def _inner(precision):
+    """Inner setting: refinement tolerance, or the residual reduction between
+    replacements of the residual-replacement solve."""
+    return 0.1 if precision == "mixed_rr" else 3e-4
+
+
+@pytest.mark.parametrize("precision", ["mixed", "mixed_rr"])
+def test_config1_mixed_meets_the_fp64_floor(precision):
+    """Mixed precision on config 1 (the FP32 iteration stalls on the air
     region, the FP64 polish finishes) reaches the FP64 true-residual floor,
     certified by the oracle's operator, and the FP64 solution within FP64's
     own spread."""
     op, ref, b = _config1()
-    s = GpuHCurlPCGSolver({"Tolerance": 3e-10, "AbsTolerance": 0.0, "MaxIter": 40000, "Precision": "mixed",
+    s = GpuHCurlPCGSolver({"Tolerance": 3e-10, "AbsTolerance": 0.0, "MaxIter": 40000, "Precision": precision,
                            "Preconditioner": "aux"}, op)
     xm = np.zeros(op.ndof)
     s.Mult(b, xm)
@@ -123,19 +132,20 @@ def test_config1_mixed_meets_the_fp64_floor():
     assert _rel(xm, xt) <= 1e-8, _rel(xm, xt)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_rr"])
 def test_config2_slice10_matches_oracle_direct(precision):
     op, ref, b = _config2_slice(10)
     xd = _direct_refined(R.eliminated(ref), b)
     s = GpuHCurlPCGSolver({"Tolerance": 1e-12, "AbsTolerance": 0.0, "MaxIter": 20000, "Precision": precision,
-                           "Preconditioner": "aux", "InnerTolerance": 3e-4}, op)
+                           "Preconditioner": "aux", "InnerTolerance": _inner(precision)}, op)
     x = np.zeros(op.ndof)
     s.Mult(b, x)
     assert s.result["status"] == "OK", s.result
     assert _rel(x, xd) <= XERR, (_rel(x, xd), s.result)
 
 
-def test_config2_slice32_mixed_certified_by_oracle_operator():
+@pytest.mark.parametrize("precision", ["mixed", "mixed_rr"])
+def test_config2_slice32_mixed_certified_by_oracle_operator(precision):
     """32^3 slice: the mixed solve's true residual, computed with the oracle's
     independently assembled operator, meets its tolerance, and the solution
     is within 1e-10 of the FP64 solution refined in FP64 (true residuals)."""
@@ -155,8 +165,8 @@ def test_config2_slice32_mixed_certified_by_oracle_operator():
         r = torch.empty_like(bd)
         op.MultDevice(xt, r)
         xt += fp64(bd - r, 1e-8)
-    s = GpuHCurlPCGSolver({"Tolerance": 1e-11, "AbsTolerance": 0.0, "MaxIter": 20000, "Precision": "mixed",
-                           "Preconditioner": "aux", "InnerTolerance": 3e-4}, op)
+    s = GpuHCurlPCGSolver({"Tolerance": 1e-11, "AbsTolerance": 0.0, "MaxIter": 20000, "Precision": precision,
+                           "Preconditioner": "aux", "InnerTolerance": _inner(precision)}, op)
     x = torch.zeros_like(bd)
     s.MultDevice(bd, x)
     assert s.result["status"] == "OK", s.result

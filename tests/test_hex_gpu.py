@@ -194,6 +194,40 @@ def test_mixed_precision_reaches_fp64_accuracy():
     assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-10
 
 
+@pytest.mark.parametrize("precond", ["jacobi", "aux"])
+def test_residual_replacement_reaches_fp64_accuracy(precond):
+    """One FP32 PCG with FP64 residual replacement: the solution matches the
+    oracle's FP64 PCG to 1e-10, it replaced its residual more than once, and
+    it needs no more iterations than the FP64 solve (the Krylov space is not
+    restarted)."""
+    op, ref, _ = _pair(6, 2)
+    b = _rhs(op, ref, 2)
+    xr, st, it, rr = ref.pcg(b, precond=1, rtol=1e-14, maxit=200000)
+    res = {}
+    for prec in ("fp64", "mixed_rr"):
+        s = GpuHCurlPCGSolver({"Precision": prec, "Tolerance": 1e-12, "AbsTolerance": 0.0, "MaxIter": 200000,
+                               "Preconditioner": precond}, op)
+        x = np.zeros(op.ndof)
+        s.Mult(b, x)
+        assert s.result["status"] == "OK", s.result
+        assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-10, prec
+        res[prec] = s.result
+    assert res["mixed_rr"]["outer_iterations"] >= 2
+    assert res["mixed_rr"]["iterations"] <= 1.15 * res["fp64"]["iterations"] + 25, res
+
+
+def test_residual_replacement_status_on_iteration_cap():
+    op, ref, _ = _pair(4, 2)
+    b = _rhs(op, ref, 2)
+    s = GpuHCurlPCGSolver({"Precision": "mixed_rr", "Tolerance": 1e-14, "AbsTolerance": 0.0, "MaxIter": 7}, op)
+    x = np.zeros(op.ndof)
+    s.Mult(b, x)
+    assert s.result["status"] == "NOT_CONVERGED" and s.result["iterations"] == 7, s.result
+    # the FP32 correction of those 7 iterations is in x: its true residual is the reported one
+    r = np.linalg.norm(b - op.Mult(x)) / np.linalg.norm(b)
+    assert abs(r - s.result["rel_residual"]) <= 1e-6 * r and r < 1.0
+
+
 def test_lanczos_bound_matches_oracle():
     op, ref, _ = _pair(4, 2)
     lg = op.LanczosLmax(20)

@@ -108,7 +108,7 @@ def test_tet_beam_mesh_matches_oracle():
     assert np.linalg.norm(op.Mult(x) - yr) / np.linalg.norm(yr) < 1e-12
 
 
-@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed_rr"])
 def test_tet_solve_matches_oracle(prec):
     op, ref, rng = _pair(4, 2)
     b = rng.standard_normal(op.ndof)
