@@ -202,6 +202,17 @@ static inline NodeGrid node_grid(int nx, int ny, int nz) {
   const int bx = row_block(w);
   return NodeGrid{dim3((unsigned)((w + bx - 1) / bx), (unsigned)(ny + 1), (unsigned)(nz + 1)), dim3((unsigned)bx)};
 }
+// Transfer kernels on the large grids: KT consecutive z-planes per thread,
+// every load issued before the node's mask is applied, so that a thread keeps
+// several independent gathers in flight (one node per thread and a mask test
+// ahead of the gathers left these kernels bound by two memory latencies per
+// node).
+constexpr int kKT = 4;
+static inline NodeGrid node_grid_kt(int nx, int ny, int nz) {
+  NodeGrid g = node_grid(nx, ny, nz);
+  g.grid.z = (unsigned)((nz + 1 + kKT - 1) / kKT);
+  return g;
+}
 #define NODE_IJK(d, i, j, k, n)                                              \
   const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z; \
   if (i > (d).nx) return;                                                   \
@@ -469,56 +480,71 @@ __global__ void k_prolong_add(Dims fd, Dims cd, const float* __restrict__ xc, co
 // is a template parameter so that element/local splits are shifts and
 // multiplications)
 
-// g = G^T r on the Gauss-Lobatto grid (mx+1, my+1, mz+1), zero where qdinv = 0
+// g = G^T r on the Gauss-Lobatto grid (mx+1, my+1, mz+1), zero where qdinv = 0.
+// Per component c, node index I_c = e P + q lies in one element (0 < q < P) or
+// on the boundary between two (q = 0 of e, q = P of e - 1); both cases are
+// written as two visits with 0/1 weights, so that the gathers carry no branch.
+template <typename T, int NV, int P>
+__device__ __forceinline__ void gt_at(const HexDev& h, const AuxTab& tab, const T* __restrict__ r0,
+                                      const T* __restrict__ r1, int mx, int my, int I, int J, int K,
+                                      float (&acc)[NV]) {
+  const T* rr[2] = {r0, r1};
+  for (int v = 0; v < NV; ++v) acc[v] = 0.0f;
+  const int idx[3] = {I, J, K};
+  const int ne[3] = {h.nx, h.ny, h.nz};
+  const int base[3] = {(int)h.off[0], (int)h.off[1], (int)h.off[2]};
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const int ic = idx[c];
+    // strides of component c's dof array
+    const int n0 = mx + (c != 0), n1 = my + (c != 1);
+    const int s_c = c == 0 ? 1 : (c == 1 ? n0 : n0 * n1);
+    int tt[3] = {I, J, K};
+    tt[c] = 0;
+    const int b0 = base[c] + tt[0] + n0 * (tt[1] + n1 * tt[2]);
+    const int e0 = ic / P, q0 = ic - e0 * P;
+    // visit 1: (e0, q0) inside, else (e0 - 1, P); visit 2: (e0, 0) on a boundary
+    const int ea = q0 != 0 ? e0 : max(e0 - 1, 0), qa = q0 != 0 ? q0 : P;
+    const float ma = (q0 != 0 || ic > 0) ? 1.0f : 0.0f;
+    const int eb = min(e0, ne[c] - 1);
+    const float mb = (q0 == 0 && e0 < ne[c]) ? 1.0f : 0.0f;
+#pragma unroll
+    for (int a2 = 0; a2 < P; ++a2) {
+      const float wa = ma * tab.D[a2][qa], wb = mb * tab.D[a2][0];
+      const int ga = b0 + (ea * P + a2) * s_c, gb = b0 + (eb * P + a2) * s_c;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) acc[v] += wa * (float)rr[v][ga] + wb * (float)rr[v][gb];
+    }
+  }
+}
 template <typename T, int NV, int P>
 __global__ void k_gt(HexDev h, AuxTab tab, const T* __restrict__ r0, const T* __restrict__ r1,
                      const float* __restrict__ qdinv, float* __restrict__ g, ChebStart cs,
                      const int* __restrict__ done) {
   if (done && *done) return;
   const Dims qd{h.nx * P, h.ny * P, h.nz * P};
-  NODE_IJK(qd, I, J, K, n);
-  const int mx = qd.nx, my = qd.ny;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y;
+  if (I > qd.nx) return;
   const int nq = (int)qd.nodes();
-  const T* rr[2] = {r0, r1};
-  float acc[NV];
-  for (int v = 0; v < NV; ++v) acc[v] = 0.0f;
-  if (qdinv[n] != 0.0f) {
-    // component c, open index o = e P + a along c; node index I_c = e P + q
-    const int idx[3] = {I, J, K};
-    const int ne[3] = {h.nx, h.ny, h.nz};
-    const int base[3] = {(int)h.off[0], (int)h.off[1], (int)h.off[2]};
+  float acc[kKT][NV], dq[kKT];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const int ic = idx[c];
-      // strides of component c's dof array
-      const int n0 = mx + (c != 0), n1 = my + (c != 1);
-      const int s_c = c == 0 ? 1 : (c == 1 ? n0 : n0 * n1);
-      int tt[3] = {I, J, K};
-      tt[c] = 0;
-      const int b0 = base[c] + tt[0] + n0 * (tt[1] + n1 * tt[2]);
-      // elements containing node index ic along c: one inside an element,
-      // two (local q = P and q = 0) on an element boundary
-      auto visit = [&](int e, int q) {
-#pragma unroll
-        for (int a2 = 0; a2 < P; ++a2) {
-          const int gdx = b0 + (e * P + a2) * s_c;
-          const float w = tab.D[a2][q];
-#pragma unroll
-          for (int v = 0; v < NV; ++v) acc[v] += w * (float)rr[v][gdx];
-        }
-      };
-      const int e0 = ic / P, q0 = ic - e0 * P;
-      if (q0 != 0) {
-        visit(e0, q0);
-      } else {
-        if (ic > 0) visit(e0 - 1, P);
-        if (e0 < ne[c]) visit(e0, 0);
-      }
-    }
+  for (int t = 0; t < kKT; ++t) {  // gathers of all planes first
+    const int K = min((int)blockIdx.z * kKT + t, qd.nz);
+    gt_at<T, NV, P>(h, tab, r0, r1, qd.nx, qd.ny, I, J, K, acc[t]);
+    dq[t] = qdinv[I + (qd.nx + 1) * (J + (qd.ny + 1) * K)];
   }
 #pragma unroll
-  for (int v = 0; v < NV; ++v) g[v * nq + n] = acc[v];
-  if (cs.r) cheb_start_at<NV>(cs, nq, n, qdinv[n], acc);
+  for (int t = 0; t < kKT; ++t) {
+    const int K = blockIdx.z * kKT + t;
+    if (K > qd.nz) break;
+    const int n = I + (qd.nx + 1) * (J + (qd.ny + 1) * K);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      acc[t][v] = dq[t] != 0.0f ? acc[t][v] : 0.0f;
+      g[v * nq + n] = acc[t][v];
+    }
+    if (cs.r) cheb_start_at<NV>(cs, nq, n, dq[t], acc[t]);
+  }
 }
 
 // z += C G phi for the dofs of component c (grid n0 x n1 x n2, open along c);
@@ -529,31 +555,48 @@ __global__ void k_g(HexDev h, AuxTab tab, const float* __restrict__ phi, const u
                     const int* __restrict__ done) {
   if (done && *done) return;
   const int mx = h.nx * P, my = h.ny * P, mz = h.nz * P;
-  const int n0 = mx + (c != 0), n1 = my + (c != 1);
-  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  const int n0 = mx + (c != 0), n1 = my + (c != 1), n2 = mz + (c != 2);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
   if (i >= n0) return;
-  const int gd = (int)h.off[c] + i + n0 * (j + n1 * k);
-  if (ess[gd]) return;
   const int nq = (mx + 1) * (my + 1) * (mz + 1);
-  const int o = c == 0 ? i : (c == 1 ? j : k);
-  const int e = o / P, a = o - e * P;
   const int stride = c == 0 ? 1 : (c == 1 ? (mx + 1) : (mx + 1) * (my + 1));
-  int t[3] = {i, j, k};
-  t[c] = e * P;
-  const int n_base = t[0] + (mx + 1) * (t[1] + (my + 1) * t[2]);
-  float v[NV];
-  for (int s = 0; s < NV; ++s) v[s] = 0.0f;
+  // loads of all kKT dofs first (phi gathers, masks, the z values), then the updates
+  float v[kKT][NV];
+  T za[kKT], zb[kKT];
+  bool on[kKT];
 #pragma unroll
-  for (int q = 0; q <= P; ++q) {
-    const float w = tab.D[a][q];
+  for (int t = 0; t < kKT; ++t) {
+    const int k = blockIdx.z * kKT + t;
+    on[t] = k < n2;
+    const int kk = on[t] ? k : n2 - 1;
+    const int gd = (int)h.off[c] + i + n0 * (j + n1 * kk);
+    const int o = c == 0 ? i : (c == 1 ? j : kk);
+    const int e = o / P, a = o - e * P;
+    int tq[3] = {i, j, kk};
+    tq[c] = e * P;
+    const int n_base = tq[0] + (mx + 1) * (tq[1] + (my + 1) * tq[2]);
+    for (int s2 = 0; s2 < NV; ++s2) v[t][s2] = 0.0f;
 #pragma unroll
-    for (int s = 0; s < NV; ++s) v[s] += w * phi[s * nq + n_base + q * stride];
+    for (int q = 0; q <= P; ++q) {
+      const float w = tab.D[a][q];
+#pragma unroll
+      for (int s2 = 0; s2 < NV; ++s2) v[t][s2] += w * phi[s2 * nq + n_base + q * stride];
+    }
+    on[t] = on[t] && !ess[gd];
+    za[t] = z0[gd];
+    if (NV > 1) zb[t] = z1[gd];
   }
-  if (NV == 1) {
-    z0[gd] += (T)(c00 * v[0]);
-  } else {
-    z0[gd] += (T)(c00 * v[0] + c01 * v[NV - 1]);
-    z1[gd] += (T)(c10 * v[0] + c11 * v[NV - 1]);
+#pragma unroll
+  for (int t = 0; t < kKT; ++t) {
+    if (!on[t]) continue;
+    const int k = blockIdx.z * kKT + t;
+    const int gd = (int)h.off[c] + i + n0 * (j + n1 * k);
+    if (NV == 1) {
+      z0[gd] = za[t] + (T)(c00 * v[t][0]);
+    } else {
+      z0[gd] = za[t] + (T)(c00 * v[t][0] + c01 * v[t][NV - 1]);
+      z1[gd] = zb[t] + (T)(c10 * v[t][0] + c11 * v[t][NV - 1]);
+    }
   }
 }
 
@@ -569,37 +612,53 @@ template <int NV, int P>
 __global__ void k_rq(Dims vd, AuxTab tab, const float* __restrict__ g, const float* __restrict__ dinv1,
                      float* __restrict__ b1, ChebStart cs, const int* __restrict__ done) {
   if (done && *done) return;
-  NODE_IJK(vd, i, j, k, n);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i > vd.nx) return;
   const int mx = vd.nx * P, my = vd.ny * P, mz = vd.nz * P;
   const int nq = (mx + 1) * (my + 1) * (mz + 1), n1 = (int)vd.nodes();
-  float acc[NV];
-  for (int v = 0; v < NV; ++v) acc[v] = 0.0f;
-  if (dinv1[n] != 0.0f) {
+  // 1-D taps with out-of-grid entries clamped and weighted 0 (no branches)
+  int ix[2 * P + 1];
+  float wx[2 * P + 1];
+#pragma unroll
+  for (int d = -P; d <= P; ++d) {
+    const int Iq = i * P + d;
+    const bool in = Iq >= 0 && Iq <= mx;
+    ix[d + P] = min(max(Iq, 0), mx);
+    wx[d + P] = in ? wq1d(Iq, i, P, tab) : 0.0f;
+  }
+#pragma unroll
+  for (int t = 0; t < kKT; ++t) {
+    const int k = blockIdx.z * kKT + t;
+    if (k > vd.nz) break;
+    const int n = i + (vd.nx + 1) * (j + (vd.ny + 1) * k);
+    float acc[NV];
+    for (int v = 0; v < NV; ++v) acc[v] = 0.0f;
 #pragma unroll
     for (int dz = -P; dz <= P; ++dz) {
       const int Kq = k * P + dz;
-      if (Kq < 0 || Kq > mz) continue;
-      const float wz = wq1d(Kq, k, P, tab);
+      const float wz = (Kq >= 0 && Kq <= mz) ? wq1d(Kq, k, P, tab) : 0.0f;
+      const int Kc = min(max(Kq, 0), mz);
 #pragma unroll
       for (int dy = -P; dy <= P; ++dy) {
         const int Jq = j * P + dy;
-        if (Jq < 0 || Jq > my) continue;
-        const float wy = wq1d(Jq, j, P, tab) * wz;
-        const int row = (mx + 1) * (Jq + (my + 1) * Kq);
+        const float wy = (Jq >= 0 && Jq <= my) ? wq1d(Jq, j, P, tab) * wz : 0.0f;
+        const int row = (mx + 1) * (min(max(Jq, 0), my) + (my + 1) * Kc);
 #pragma unroll
-        for (int dx = -P; dx <= P; ++dx) {
-          const int Iq = i * P + dx;
-          if (Iq < 0 || Iq > mx) continue;
-          const float w = wq1d(Iq, i, P, tab) * wy;
+        for (int dx = 0; dx <= 2 * P; ++dx) {
+          const float w = wx[dx] * wy;
 #pragma unroll
-          for (int v = 0; v < NV; ++v) acc[v] += w * g[v * nq + row + Iq];
+          for (int v = 0; v < NV; ++v) acc[v] += w * g[v * nq + row + ix[dx]];
         }
       }
     }
-  }
+    const float d1 = dinv1[n];
 #pragma unroll
-  for (int v = 0; v < NV; ++v) b1[v * n1 + n] = acc[v];
-  cheb_start_at<NV>(cs, n1, n, dinv1[n], acc);
+    for (int v = 0; v < NV; ++v) {
+      acc[v] = d1 != 0.0f ? acc[v] : 0.0f;
+      b1[v * n1 + n] = acc[v];
+    }
+    cheb_start_at<NV>(cs, n1, n, d1, acc);
+  }
 }
 
 // phi = D_L^-1 g + P0 x1 on the Gauss-Lobatto grid (zero at fixed nodes)
@@ -608,30 +667,40 @@ __global__ void k_pq(Dims vd, AuxTab tab, const float* __restrict__ g, const flo
                      const float* __restrict__ x1, float* __restrict__ phi, const int* __restrict__ done) {
   if (done && *done) return;
   const Dims qd{vd.nx * P, vd.ny * P, vd.nz * P};
-  NODE_IJK(qd, I, J, K, n);
+  const int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y;
+  if (I > qd.nx) return;
   const int nq = (int)qd.nodes(), n1 = (int)vd.nodes();
-  const float dq = qdinv[n];
-  if (dq == 0.0f) {
-#pragma unroll
-    for (int v = 0; v < NV; ++v) phi[v * nq + n] = 0.0f;
-    return;
-  }
-  const int ex = min(I / P, vd.nx - 1), ey = min(J / P, vd.ny - 1), ez = min(K / P, vd.nz - 1);
-  const float xi = tab.gll[I - ex * P], yi = tab.gll[J - ey * P], zi = tab.gll[K - ez * P];
-  float acc[NV];
-#pragma unroll
-  for (int v = 0; v < NV; ++v) acc[v] = dq * g[v * nq + n];
   const int sx = vd.nx + 1, sxy = (vd.nx + 1) * (vd.ny + 1);
-  const int v0 = ex + sx * ey + sxy * ez;
+  const int ex = min(I / P, vd.nx - 1), ey = min(J / P, vd.ny - 1);
+  const float xi = tab.gll[I - ex * P], yi = tab.gll[J - ey * P];
+  float acc[kKT][NV], dq[kKT];
 #pragma unroll
-  for (int a = 0; a < 8; ++a) {
-    const float w = ((a & 1) ? xi : 1.0f - xi) * (((a >> 1) & 1) ? yi : 1.0f - yi) * (((a >> 2) & 1) ? zi : 1.0f - zi);
-    const int vn = v0 + (a & 1) + sx * ((a >> 1) & 1) + sxy * ((a >> 2) & 1);
+  for (int t = 0; t < kKT; ++t) {  // loads of all planes first
+    const int K = min((int)blockIdx.z * kKT + t, qd.nz);
+    const int n = I + (qd.nx + 1) * (J + (qd.ny + 1) * K);
+    const int ez = min(K / P, vd.nz - 1);
+    const float zi = tab.gll[K - ez * P];
+    dq[t] = qdinv[n];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) acc[v] += w * x1[v * n1 + vn];
+    for (int v = 0; v < NV; ++v) acc[t][v] = dq[t] * g[v * nq + n];
+    const int v0 = ex + sx * ey + sxy * ez;
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+      const float w = ((a & 1) ? xi : 1.0f - xi) * (((a >> 1) & 1) ? yi : 1.0f - yi) *
+                      (((a >> 2) & 1) ? zi : 1.0f - zi);
+      const int vn = v0 + (a & 1) + sx * ((a >> 1) & 1) + sxy * ((a >> 2) & 1);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) acc[t][v] += w * x1[v * n1 + vn];
+    }
   }
 #pragma unroll
-  for (int v = 0; v < NV; ++v) phi[v * nq + n] = acc[v];
+  for (int t = 0; t < kKT; ++t) {
+    const int K = blockIdx.z * kKT + t;
+    if (K > qd.nz) break;
+    const int n = I + (qd.nx + 1) * (J + (qd.ny + 1) * K);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) phi[v * nq + n] = dq[t] != 0.0f ? acc[t][v] : 0.0f;
+  }
 }
 
 // diag of L = G^T M_sigma G on the Gauss-Lobatto grid (order p > 1)
@@ -943,8 +1012,14 @@ static ChebStart start_of(AuxLevel& L) {
 }
 
 template <int NV>
+static bool vcycle_coop(const hcop* h, AuxMG* M, int l0, const int* done, cudaStream_t s);
+static int coop_from_level();
+
+template <int NV>
 static void vcycle(const hcop* h, AuxMG* M, int l, const int* done, cudaStream_t s) {
   AuxLevel& L = M->lev[l];
+  // from the configured level down, the rest of the cycle as one cooperative launch
+  if (l == coop_from_level() && vcycle_coop<NV>(h, M, l, done, s)) return;
   if (l == M->nlev - 1) {
     smooth<NV>(h, L, kAuxCoarseDegree, true, done, s);
     return;
@@ -973,7 +1048,7 @@ static void vcycle(const hcop* h, AuxMG* M, int l, const int* done, cudaStream_t
 // at a grid barrier between steps.
 constexpr int kVThreads = 512;
 constexpr int kMaxVSteps = 64;
-constexpr unsigned kBarSpins = 1u << 22;  // ~0.3 s of polling before a wait gives up
+constexpr unsigned kBarSpins = 1u << 23;  // >= ~1 s of polling (L2 round trips) before a wait gives up
 enum : int { kOpFused = 0, kOpResid = 1, kOpRestrict = 2, kOpProlong = 3, kOpAdd = 4 };
 
 struct VStep {
@@ -1015,7 +1090,6 @@ __device__ __forceinline__ bool coop_sync(CoopBar* bar) {
           atomicExch(&bar->err, 1);
           break;
         }
-        __nanosleep(40);
       }
     }
     __threadfence();
@@ -1099,22 +1173,32 @@ static void vcycle_steps(const AuxMG* M, int l, std::vector<VStep>& out) {
   smooth_steps(M, l, kAuxDegree, false, out);
 }
 
-// HC_AUX_VCYCLE=kernels in the environment selects the per-step kernels (read
-// at every application, so one handle can run both forms)
-static bool coop_wanted() {
+// Level from which the V-cycle runs as one cooperative launch, from
+// HC_AUX_VCYCLE (read at every application, so one handle can run every form):
+// default "kernels" -> none (-1): one launch per step, replayed from a CUDA
+// graph; "coop" -> all levels (0); "hybrid" -> level 1 down (the finest level's
+// steps stay separate kernels).  Measured on 48^3 and 64^3 p = 2 grids, the
+// per-step kernels are the fastest form (64^3: 259 us per preconditioner
+// application against 286 us hybrid and 308 us cooperative): a grid barrier
+// costs more than the dependency between two graph nodes, and the cooperative
+// form's level vectors must bypass L1 (its blocks read what others wrote in
+// the same launch), which the 27-point stencils otherwise reuse.
+static int coop_from_level() {
   const char* env = std::getenv("HC_AUX_VCYCLE");
-  return !(env && std::strcmp(env, "kernels") == 0);
+  if (env && std::strcmp(env, "coop") == 0) return 0;
+  if (env && std::strcmp(env, "hybrid") == 0) return 1;
+  return -1;
 }
 
 // false: not available (no cooperative support, too many steps); the caller
 // issues the per-step kernels
 template <int NV>
-static bool vcycle_coop(const hcop* h, AuxMG* M, const int* done, cudaStream_t s, cudaError_t* err) {
+static bool vcycle_coop(const hcop* h, AuxMG* M, int l0, const int* done, cudaStream_t s) {
   (void)h;
   const int blocks = NV == 1 ? M->coop_blocks : M->coop_blocks2;
-  if (!M->bar || blocks <= 0 || !coop_wanted()) return false;
+  if (!M->bar || blocks <= 0 || l0 < 0 || l0 >= M->nlev) return false;
   std::vector<VStep> steps;
-  vcycle_steps(M, 0, steps);
+  vcycle_steps(M, l0, steps);
   if ((int)steps.size() > kMaxVSteps) return false;
   VCycleArgs a{};
   a.nlev = M->nlev;
@@ -1135,7 +1219,8 @@ static bool vcycle_coop(const hcop* h, AuxMG* M, const int* done, cudaStream_t s
   at[0].val.cooperative = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  *err = cudaLaunchKernelEx(&cfg, k_vcycle<NV>, a, done);
+  // a failed launch is also the thread's last error, which the caller reads
+  (void)cudaLaunchKernelEx(&cfg, k_vcycle<NV>, a, done);
   return true;
 }
 
@@ -1160,8 +1245,10 @@ static void coop_setup(hcop* h, AuxMG* M) {
     return;
   }
   if (cudaMemsetAsync(M->bar, 0, sizeof(CoopBar), h->stream) != cudaSuccess) return;
-  M->coop_blocks = sms * std::min(b1, 2);
-  M->coop_blocks2 = sms * std::min(b2, 2);
+  // one block per SM: the coarse levels have few nodes, and every block is
+  // one arrival at each grid barrier
+  M->coop_blocks = sms;
+  M->coop_blocks2 = sms;
 }
 
 // z += C G V G^T r   (NV = 1: real r, coefficient c00; NV = 2: planar complex,
@@ -1174,20 +1261,19 @@ static void aux_apply_p(const hcop* h, AuxMG* M, const T* r0, const T* r1, T* z0
   const int mx = h->nx * P, my = h->ny * P, mz = h->nz * P;
   float* g = P > 1 ? M->g : L0.b;
   const float* qd = P > 1 ? M->qdinv : L0.dinv;
-  const NodeGrid gq = node_grid(mx, my, mz), g1 = node_grid(L0.d.nx, L0.d.ny, L0.d.nz);
+  const NodeGrid gq = node_grid_kt(mx, my, mz), g1 = node_grid_kt(L0.d.nx, L0.d.ny, L0.d.nz);
   const ChebStart none{nullptr, nullptr, nullptr, 0.0f};
   k_gt<T, NV, P><<<gq.grid, gq.block, 0, s>>>(hd, M->tab, r0, r1, qd, g, P > 1 ? none : start_of(L0), done);
   if (P > 1) k_rq<NV, P><<<g1.grid, g1.block, 0, s>>>(L0.d, M->tab, g, L0.dinv, L0.b, start_of(L0), done);
-  cudaError_t ce = cudaSuccess;  // a failed launch is also the thread's last error, read by the caller
-  if (!vcycle_coop<NV>(h, M, done, s, &ce)) vcycle<NV>(h, M, 0, done, s);
-  (void)ce;
+  vcycle<NV>(h, M, 0, done, s);
   const float* phi = L0.x;  // order 1: phi is the finest Q1 level's x
   if (P > 1) {
     k_pq<NV, P><<<gq.grid, gq.block, 0, s>>>(L0.d, M->tab, g, M->qdinv, L0.x, M->phi, done);
     phi = M->phi;
   }
   // z += C G phi, one launch per Nedelec component (grid open along c)
-  const NodeGrid c0 = node_grid(mx - 1, my, mz), c1 = node_grid(mx, my - 1, mz), c2 = node_grid(mx, my, mz - 1);
+  const NodeGrid c0 = node_grid_kt(mx - 1, my, mz), c1 = node_grid_kt(mx, my - 1, mz),
+                 c2 = node_grid_kt(mx, my, mz - 1);
   k_g<T, NV, P, 0><<<c0.grid, c0.block, 0, s>>>(hd, M->tab, phi, h->ess, z0, z1, coef[0], coef[1], coef[2], coef[3],
                                                 done);
   k_g<T, NV, P, 1><<<c1.grid, c1.block, 0, s>>>(hd, M->tab, phi, h->ess, z0, z1, coef[0], coef[1], coef[2], coef[3],
@@ -1226,7 +1312,7 @@ cudaError_t auxmg_apply(const hcop* h, const T* r0, const T* r1, T* z0, T* z1, c
     return cudaGetLastError();
   }
   const void* key[5] = {r0, r1, z0, z1, done};
-  const int coop = coop_wanted() ? 1 : 0;
+  const int coop = coop_from_level() + 1;
   for (AuxGraph& g : M->graphs) {
     if (g.exec && g.nv == NV && g.tsize == (int)sizeof(T) && g.coop == coop &&
         std::memcmp(g.key, key, sizeof(key)) == 0 && std::memcmp(g.coef, coef, sizeof(g.coef)) == 0)

@@ -942,21 +942,32 @@ static hc_status polish64(hcop* h, const hc_solve_params* prm, const SolveCfg& i
     c64.lmax = h->lmax64;
   }
   // aim below the tolerance: the polish stops on its recursive residual,
-  // the status is judged on the true residual below
+  // the status is judged on the true residual.  Where the two drift apart
+  // (operators at the FP64 floor), a restart from the current x -- whose
+  // set-up recomputes b - J x -- is one FP64 refinement step: up to three
+  // rounds, while each at least halves the true residual.
   c64.rtol = 0.5 * prm->rtol;
   c64.atol = 0.5 * prm->atol;
-  c64.maxit = prm->maxit - *iters;
-  int it = 0, ap = 0;
-  const hc_status pst = pcg_run<double>(h, c64, b, x, wk64, &it, &ap);
-  *iters += it;
-  *applies += ap + 1;
-  ++*outer;
-  if (pst == HC_ECUDA || pst == HC_ENOMEM) return pst;
-  st = resid64(h, b, x, r64, rn2, bn2);
-  if (st != HC_OK) return st;
-  if (!std::isfinite(std::sqrt(*rn2))) return HC_BREAKDOWN;
-  if (pst == HC_BREAKDOWN) return pst;
-  return std::sqrt(*rn2) <= tol ? HC_OK : HC_NOT_CONVERGED;
+  double rn_prev = std::sqrt(*rn2);
+  for (int round = 0; round < 3; ++round) {
+    c64.maxit = prm->maxit - *iters;
+    if (c64.maxit < 1) return HC_NOT_CONVERGED;
+    int it = 0, ap = 0;
+    const hc_status pst = pcg_run<double>(h, c64, b, x, wk64, &it, &ap);
+    *iters += it;
+    *applies += ap + 1;
+    ++*outer;
+    if (pst == HC_ECUDA || pst == HC_ENOMEM) return pst;
+    st = resid64(h, b, x, r64, rn2, bn2);
+    if (st != HC_OK) return st;
+    const double rn = std::sqrt(*rn2);
+    if (!std::isfinite(rn)) return HC_BREAKDOWN;
+    if (pst == HC_BREAKDOWN) return pst;
+    if (rn <= tol) return HC_OK;
+    if (rn > 0.5 * rn_prev) break;
+    rn_prev = rn;
+  }
+  return HC_NOT_CONVERGED;
 }
 
 static void fill_info(hc_solve_info* info, hc_status result, int iters, int outer, int applies, double rn2,

@@ -653,19 +653,35 @@ hc_status multi_solve_device(hcop* h, const hc_solve_params* prm, int R, const d
     w = mwork(h);
     r64 = (double*)w->vec;
     double* wk64 = (double*)((char*)w->vec + off);
-    int used = 0;
-    for (int k = 0; k < R; ++k) used = std::max(used, total[k]);
     // aim below the tolerance: the polish stops on its recursive residual,
-    // the status below is judged on the true one
-    st = mpcg_run<double>(h, R, 0.5 * prm->rtol, 0.5 * prm->atol, std::max(1, prm->maxit - used), B, X, wk64, h->dinv,
-                          aux);
-    if (st != HC_OK) return st;
-    for (int k = 0; k < R; ++k) {
-      total[k] += w->hS->it[k];
-      ++outer[k];
+    // the status below is judged on the true one.  A restart from X (its
+    // set-up recomputes B - J X per column) is one FP64 refinement step: up
+    // to three rounds while the worst unconverged column at least halves.
+    double worst_prev = 0.0;
+    for (int k = 0; k < R; ++k)
+      if (rn[k] > tol[k]) worst_prev = std::max(worst_prev, rn[k] / std::max(tol[k], 1e-300));
+    for (int round = 0; round < 3; ++round) {
+      int used = 0;
+      for (int k = 0; k < R; ++k) used = std::max(used, total[k]);
+      if (used >= prm->maxit) break;
+      st = mpcg_run<double>(h, R, 0.5 * prm->rtol, 0.5 * prm->atol, std::max(1, prm->maxit - used), B, X, wk64,
+                            h->dinv, aux);
+      if (st != HC_OK) return st;
+      for (int k = 0; k < R; ++k) {
+        total[k] += w->hS->it[k];
+        ++outer[k];
+      }
+      st = residual();
+      if (st != HC_OK) return st;
+      double worst = 0.0;
+      bool bad = false;
+      for (int k = 0; k < R; ++k) {
+        if (!std::isfinite(rn[k])) bad = true;
+        if (rn[k] > tol[k]) worst = std::max(worst, rn[k] / std::max(tol[k], 1e-300));
+      }
+      if (bad || worst == 0.0 || worst > 0.5 * worst_prev) break;
+      worst_prev = worst;
     }
-    st = residual();
-    if (st != HC_OK) return st;
   }
   hc_status worst = HC_OK;
   for (int k = 0; k < R; ++k) {

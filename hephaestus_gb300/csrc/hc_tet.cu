@@ -443,8 +443,6 @@ __global__ void __launch_bounds__(256, 3) tet_apply_tiles20(int64_t ne, const in
       for (int i = 0; i < 5; ++i)
 #pragma unroll
         for (int k = 0; k < 4; ++k) acc[i][k] = 0.f;
-      // K is read once per apply: streaming (evict-first) loads keep the
-      // gathered X rows and the atomically updated Y rows in L2
       const TK* Kg = K + (e * L + 5 * g) * L;
 #pragma unroll
       for (int j0 = 0; j0 < L; j0 += 4) {
@@ -452,7 +450,7 @@ __global__ void __launch_bounds__(256, 3) tet_apply_tiles20(int64_t ne, const in
 #pragma unroll
         for (int i = 0; i < 5; ++i) {
           if constexpr (sizeof(TK) == 2) {
-            const uint2 v = __ldcs(reinterpret_cast<const uint2*>(Kg + i * L + j0));
+            const uint2 v = __ldg(reinterpret_cast<const uint2*>(Kg + i * L + j0));
             const float2 fa = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v.x));
             const float2 fb = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v.y));
             kq[i][0] = fa.x;
@@ -460,7 +458,7 @@ __global__ void __launch_bounds__(256, 3) tet_apply_tiles20(int64_t ne, const in
             kq[i][2] = fb.x;
             kq[i][3] = fb.y;
           } else {
-            const float4 v = __ldcs(reinterpret_cast<const float4*>(Kg + i * L + j0));
+            const float4 v = __ldg(reinterpret_cast<const float4*>(Kg + i * L + j0));
             kq[i][0] = v.x;
             kq[i][1] = v.y;
             kq[i][2] = v.z;
@@ -612,14 +610,13 @@ __global__ void __launch_bounds__(32 * kTcW, 5) tet_apply_mma16(int64_t ne, cons
       const int row = 8 * nt + g;  // output row i = B column n
       uint32_t b0 = 0u, b1 = 0u, b2 = 0u;
       if (row < L) {
-        // B[j][i] = K_e[i][j]: pairs along j.  K is read once per apply:
-        // streaming loads (evict-first), so that it does not push the X rows
-        // that neighbouring elements gather again, nor the Y rows they add
-        // to, out of L2
-        const unsigned int* Kr = reinterpret_cast<const unsigned int*>(Ke + row * (L / 2));
-        b0 = __ldcs(Kr + tig);                   // j = 2 tig, 2 tig + 1
-        b1 = __ldcs(Kr + 4 + tig);               // j = 2 tig + 8, + 9
-        if (tig < 2) b2 = __ldcs(Kr + 8 + tig);  // j = 16 + 2 tig, + 1
+        // B[j][i] = K_e[i][j]: pairs along j.  (Streaming, evict-first loads
+        // of K were measured: +63 MB of DRAM reads per apply, no faster --
+        // a K row's sectors are shared with the next row's loads.)
+        const uint32_t* Kr = Ke + row * (L / 2);
+        b0 = __ldg(Kr + tig);                   // j = 2 tig, 2 tig + 1
+        b1 = __ldg(Kr + 4 + tig);               // j = 2 tig + 8, + 9
+        if (tig < 2) b2 = __ldg(Kr + 8 + tig);  // j = 16 + 2 tig, + 1
       }
       mma_16816(acc[nt], ah, b0, b1);
       mma_16816(acc[nt], al, b0, b1);

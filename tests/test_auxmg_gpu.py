@@ -150,9 +150,10 @@ def test_aux_cocg_converges_at_low_frequency_where_jacobi_stalls():
 
 @pytest.mark.parametrize("n, p", [(40, 2), (24, 1), (17, 3)])
 def test_cooperative_vcycle_equals_per_step_kernels(n, p, monkeypatch):
-    """The Q1 V-cycle as one cooperative launch (grid barriers between steps)
-    runs the same steps with the same per-node arithmetic as the per-step
-    kernels (HC_AUX_VCYCLE=kernels): on one handle, z = B r through
+    """The Q1 V-cycle as one cooperative launch (grid barriers between steps;
+    HC_AUX_VCYCLE=coop: all levels, =hybrid (the default): the levels below
+    the finest) runs the same steps with the same per-node arithmetic as the
+    per-step kernels (HC_AUX_VCYCLE=kernels): on one handle, z = B r through
     hc_precond_apply_device is bit-identical (no atomics on this path), on
     hierarchies of 3-4 levels and odd grid sizes; and B is D^-1 plus a
     positive semi-definite correction (r.(z - D^-1 r) >= 0 up to the
@@ -166,7 +167,7 @@ def test_cooperative_vcycle_equals_per_step_kernels(n, p, monkeypatch):
     r = torch.tensor(np.random.default_rng(3).standard_normal(op.ndof), device="cuda")
     r2 = torch.tensor(np.random.default_rng(4).standard_normal(op.ndof), device="cuda")
     zs = {}
-    for mode in ("coop", "kernels", "coop"):
+    for mode in ("coop", "kernels", "hybrid", "coop"):
         monkeypatch.setenv("HC_AUX_VCYCLE", mode)
         z, z2 = torch.empty_like(r), torch.empty_like(r)
         op.PrecondApplyDevice(r, z, "aux")
@@ -176,9 +177,11 @@ def test_cooperative_vcycle_equals_per_step_kernels(n, p, monkeypatch):
     zj = torch.empty_like(r)
     op.PrecondApplyDevice(r, zj, "jacobi")
     for k in (0, 1):
-        a, b = zs["coop"][0][k], zs["kernels"][0][k]
-        d = np.abs(a - b)
-        assert np.array_equal(a, b), (k, int(np.count_nonzero(d)), float(d.max() / np.abs(b).max()), int(np.argmax(d)))
-        assert np.array_equal(a, zs["coop"][1][k])  # replays are reproducible
+        b = zs["kernels"][0][k]
+        for mode in ("coop", "hybrid"):
+            a = zs[mode][0][k]
+            d = np.abs(a - b)
+            assert np.array_equal(a, b), (mode, k, int(np.count_nonzero(d)), float(d.max() / np.abs(b).max()))
+        assert np.array_equal(zs["coop"][0][k], zs["coop"][1][k])  # replays are reproducible
     rh, z = r.cpu().numpy(), zs["coop"][0][0]
     assert rh @ (z - zj.cpu().numpy()) >= -1e-6 * abs(rh @ z)
