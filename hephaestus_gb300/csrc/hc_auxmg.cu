@@ -29,6 +29,8 @@
 #include <string>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "hc_internal.h"
 
 namespace hc {
@@ -42,6 +44,12 @@ constexpr int kAuxDegree = 2;        // Chebyshev degree of the pre- and post-sm
 constexpr int kAuxCoarseDegree = 4;  // Chebyshev degree on the coarsest grid
 constexpr double kAuxRatio = 30.0;
 constexpr int kAuxGraphs = 8;
+// coarse-level cluster launch of the V-cycle (k_vcycle_cluster)
+constexpr int kClusterCtas = 8;
+constexpr int kClusterThreads = 1024;
+constexpr int64_t kSmallLevelNodes = 10000;
+// forms of the V-cycle (vcycle_mode)
+enum { kVKernels = 0, kVCoop = 1, kVHybrid = 2, kVCluster = 3 };
 
 static inline unsigned agrid(int64_t n, int threads = 256) {
   const int64_t b = (n + threads - 1) / threads;
@@ -92,6 +100,7 @@ struct CoopBar {
 struct AuxMG {
   int p = 1, nlev = 0;
   CoopBar* bar = nullptr;  // cooperative V-cycle state, nullptr: per-step kernels
+  bool cluster_ok = false;  // the coarse-level cluster launch fits on this device
   int coop_blocks = 0;     // co-resident blocks of the cooperative V-cycle (per NV: [NV - 1])
   int coop_blocks2 = 0;
   std::vector<AuxGraph> graphs;   // at most kAuxGraphs, oldest replaced first
@@ -1013,13 +1022,19 @@ static ChebStart start_of(AuxLevel& L) {
 
 template <int NV>
 static bool vcycle_coop(const hcop* h, AuxMG* M, int l0, const int* done, cudaStream_t s);
+template <int NV>
+static bool vcycle_cluster(const hcop* h, AuxMG* M, int lr, int l0, const int* done, cudaStream_t s);
 static int coop_from_level();
+static int vcycle_mode();
 
 template <int NV>
 static void vcycle(const hcop* h, AuxMG* M, int l, const int* done, cudaStream_t s) {
   AuxLevel& L = M->lev[l];
   // from the configured level down, the rest of the cycle as one cooperative launch
   if (l == coop_from_level() && vcycle_coop<NV>(h, M, l, done, s)) return;
+  const bool cl = vcycle_mode() == kVCluster;
+  // a V-cycle whose finest level is small: all of it in one cluster launch
+  if (cl && l == 0 && L.d.nodes() <= kSmallLevelNodes && vcycle_cluster<NV>(h, M, -1, 0, done, s)) return;
   if (l == M->nlev - 1) {
     smooth<NV>(h, L, kAuxCoarseDegree, true, done, s);
     return;
@@ -1029,8 +1044,11 @@ static void vcycle(const hcop* h, AuxMG* M, int l, const int* done, cudaStream_t
   // r = b - L x (masked), restricted
   const NodeGrid gl = node_grid(L.d.nx, L.d.ny, L.d.nz), gc = node_grid(C.d.nx, C.d.ny, C.d.nz);
   k_cheb_resid<NV><<<gl.grid, gl.block, 0, s>>>(L.d, L.St, L.dinv, L.b, L.x, L.r, L.dv, 1.0f, done);
-  k_restrict<NV><<<gc.grid, gc.block, 0, s>>>(L.d, C.d, L.r, C.dinv, C.b, start_of(C), done);
-  vcycle<NV>(h, M, l + 1, done, s);
+  // the coarse levels below a large one: restriction and their cycle in one cluster launch
+  if (!(cl && C.d.nodes() <= kSmallLevelNodes && vcycle_cluster<NV>(h, M, l, l + 1, done, s))) {
+    k_restrict<NV><<<gc.grid, gc.block, 0, s>>>(L.d, C.d, L.r, C.dinv, C.b, start_of(C), done);
+    vcycle<NV>(h, M, l + 1, done, s);
+  }
   k_prolong_add<NV><<<gl.grid, gl.block, 0, s>>>(L.d, C.d, C.x, L.dinv, L.x, done);
   smooth<NV>(h, L, kAuxDegree, false, done, s);
 }
@@ -1098,6 +1116,44 @@ __device__ __forceinline__ bool coop_sync(CoopBar* bar) {
   return *(volatile int*)&bar->err == 0;
 }
 
+// One step of the V-cycle step list over the level's nodes, thread gt of gs.
+template <int NV>
+__device__ __forceinline__ void run_step(const VCycleArgs& a, const VStep& st, int64_t gt, int64_t gs) {
+  const VLevelDev& L = a.lev[st.lev];
+  if (st.op == kOpRestrict) {
+    const VLevelDev& C = a.lev[st.lev + 1];
+    const ChebStart cs{C.r, C.dv, C.x, C.start_inv_theta};
+    const int nx1 = C.d.nx + 1, ny1 = C.d.ny + 1, nn = (int)C.d.nodes();
+    for (int64_t q = gt; q < nn; q += gs) {
+      const int n = (int)q, i = n % nx1, t = n / nx1, j = t % ny1, k = t / ny1;
+      restrict_at<NV, true>(L.d, C.d, L.r, C.dinv, C.b, cs, n, i, j, k);
+    }
+    return;
+  }
+  const int nx1 = L.d.nx + 1, ny1 = L.d.ny + 1, nn = (int)L.d.nodes();
+  const float* din = st.swap ? L.t : L.dv;
+  float* dout = st.swap ? L.dv : L.t;
+  for (int64_t q = gt; q < nn; q += gs) {
+    const int n = (int)q, i = n % nx1, t = n / nx1, j = t % ny1, k = t / ny1;
+    switch (st.op) {
+      case kOpFused:
+        cheb_fused_at<NV, true>(L.d, L.St, L.dinv, din, dout, L.r, L.x, st.c1, st.c2, st.add_in, n, i, j, k);
+        break;
+      case kOpResid: cheb_resid_at<NV, true>(L.d, L.St, L.dinv, L.b, L.x, L.r, L.dv, st.c1, n, i, j, k); break;
+      case kOpProlong: {
+        const VLevelDev& C = a.lev[st.lev + 1];
+        prolong_add_at<NV, true>(L.d, C.d, C.x, L.dinv, L.x, n, i, j, k);
+        break;
+      }
+      default:
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+          L.x[v * nn + n] = __fadd_rn(vld<true>(L.x + v * nn + n), vld<true>(L.dv + v * nn + n));
+        break;
+    }
+  }
+}
+
 template <int NV>
 __global__ void __launch_bounds__(kVThreads) k_vcycle(const __grid_constant__ VCycleArgs a,
                                                       const int* __restrict__ done) {
@@ -1105,40 +1161,7 @@ __global__ void __launch_bounds__(kVThreads) k_vcycle(const __grid_constant__ VC
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gs = (int64_t)gridDim.x * blockDim.x;
   bool ok = *(volatile int*)&a.bar->err == 0;
   for (int s = 0; s < a.nsteps && ok; ++s) {
-    const VStep& st = a.step[s];
-    const VLevelDev& L = a.lev[st.lev];
-    if (st.op == kOpRestrict) {
-      const VLevelDev& C = a.lev[st.lev + 1];
-      const ChebStart cs{C.r, C.dv, C.x, C.start_inv_theta};
-      const int nx1 = C.d.nx + 1, ny1 = C.d.ny + 1, nn = (int)C.d.nodes();
-      for (int64_t q = gt; q < nn; q += gs) {
-        const int n = (int)q, i = n % nx1, t = n / nx1, j = t % ny1, k = t / ny1;
-        restrict_at<NV, true>(L.d, C.d, L.r, C.dinv, C.b, cs, n, i, j, k);
-      }
-    } else {
-      const int nx1 = L.d.nx + 1, ny1 = L.d.ny + 1, nn = (int)L.d.nodes();
-      const float* din = st.swap ? L.t : L.dv;
-      float* dout = st.swap ? L.dv : L.t;
-      for (int64_t q = gt; q < nn; q += gs) {
-        const int n = (int)q, i = n % nx1, t = n / nx1, j = t % ny1, k = t / ny1;
-        switch (st.op) {
-          case kOpFused:
-            cheb_fused_at<NV, true>(L.d, L.St, L.dinv, din, dout, L.r, L.x, st.c1, st.c2, st.add_in, n, i, j, k);
-            break;
-          case kOpResid: cheb_resid_at<NV, true>(L.d, L.St, L.dinv, L.b, L.x, L.r, L.dv, st.c1, n, i, j, k); break;
-          case kOpProlong: {
-            const VLevelDev& C = a.lev[st.lev + 1];
-            prolong_add_at<NV, true>(L.d, C.d, C.x, L.dinv, L.x, n, i, j, k);
-            break;
-          }
-          default:
-#pragma unroll
-            for (int v = 0; v < NV; ++v)
-              L.x[v * nn + n] = __fadd_rn(vld<true>(L.x + v * nn + n), vld<true>(L.dv + v * nn + n));
-            break;
-        }
-      }
-    }
+    run_step<NV>(a, a.step[s], gt, gs);
     if (s + 1 < a.nsteps) ok = coop_sync(a.bar);
   }
   if (!ok && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1146,6 +1169,28 @@ __global__ void __launch_bounds__(kVThreads) k_vcycle(const __grid_constant__ VC
     // reductions turn into HC_BREAKDOWN
     const int nn = (int)a.lev[0].d.nodes();
     for (int v = 0; v < NV; ++v) a.lev[0].x[v * nn] = __int_as_float(0x7fc00000);
+  }
+}
+
+// The coarse levels (<= kSmallLevelNodes nodes) of the V-cycle in one launch
+// of one thread-block cluster: kClusterCtas CTAs of kClusterThreads threads
+// walk the step list and meet at the cluster's hardware barrier between steps
+// (barrier.cluster arrive/wait: release/acquire at cluster scope; every
+// thread reaches every barrier, the loops over nodes sit between them).  On
+// grids of a few thousand nodes a step is one or two L2 round trips, far
+// below the launch and drain of a separate kernel.
+
+template <int NV>
+__global__ void __launch_bounds__(kClusterThreads, 1) k_vcycle_cluster(const __grid_constant__ VCycleArgs a,
+                                                                       const int* __restrict__ done) {
+  if (done && *done) return;  // the flag is the same for every thread: all leave before any barrier
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  const int64_t gt = (int64_t)cl.block_rank() * blockDim.x + threadIdx.x;
+  const int64_t gs = (int64_t)kClusterCtas * blockDim.x;
+  for (int s = 0; s < a.nsteps; ++s) {
+    run_step<NV>(a, a.step[s], gt, gs);
+    if (s + 1 < a.nsteps) cl.sync();
   }
 }
 
@@ -1173,21 +1218,29 @@ static void vcycle_steps(const AuxMG* M, int l, std::vector<VStep>& out) {
   smooth_steps(M, l, kAuxDegree, false, out);
 }
 
-// Level from which the V-cycle runs as one cooperative launch, from
-// HC_AUX_VCYCLE (read at every application, so one handle can run every form):
-// default "kernels" -> none (-1): one launch per step, replayed from a CUDA
-// graph; "coop" -> all levels (0); "hybrid" -> level 1 down (the finest level's
-// steps stay separate kernels).  Measured on 48^3 and 64^3 p = 2 grids, the
-// per-step kernels are the fastest form (64^3: 259 us per preconditioner
-// application against 286 us hybrid and 308 us cooperative): a grid barrier
-// costs more than the dependency between two graph nodes, and the cooperative
-// form's level vectors must bypass L1 (its blocks read what others wrote in
-// the same launch), which the 27-point stencils otherwise reuse.
-static int coop_from_level() {
+// Form of the Q1 V-cycle, from HC_AUX_VCYCLE (read at every application, so one
+// handle can run every form; all forms are bit-identical):
+//   "kernels" (default): one launch per step, replayed from a CUDA graph;
+//   "cluster": per-step kernels on the large levels, the coarse levels
+//              (<= kSmallLevelNodes nodes) in one thread-block-cluster launch;
+//   "coop":    every level in one cooperative launch (grid barriers);
+//   "hybrid":  the levels below the finest in one cooperative launch.
+// Measured per preconditioner application at 64^3 / 48^3 p = 2: kernels 258 /
+// 158 us, cluster 262 / 163 us, hybrid 275 / 184 us, coop 297 / 204 us.  Inside
+// a graph, consecutive small kernels overlap their launch and drain, so a
+// coarse-level step costs about as much as a cluster barrier plus the L2
+// round trips of the single-launch forms (whose level vectors must bypass L1:
+// their blocks read what other blocks wrote in the same launch).
+static int vcycle_mode() {
   const char* env = std::getenv("HC_AUX_VCYCLE");
-  if (env && std::strcmp(env, "coop") == 0) return 0;
-  if (env && std::strcmp(env, "hybrid") == 0) return 1;
-  return -1;
+  if (env && std::strcmp(env, "cluster") == 0) return kVCluster;
+  if (env && std::strcmp(env, "coop") == 0) return kVCoop;
+  if (env && std::strcmp(env, "hybrid") == 0) return kVHybrid;
+  return kVKernels;
+}
+static int coop_from_level() {
+  const int m = vcycle_mode();
+  return m == kVCoop ? 0 : (m == kVHybrid ? 1 : -1);
 }
 
 // false: not available (no cooperative support, too many steps); the caller
@@ -1224,10 +1277,64 @@ static bool vcycle_coop(const hcop* h, AuxMG* M, int l0, const int* done, cudaSt
   return true;
 }
 
+// Restriction lr -> lr + 1 (lr >= 0) and the whole cycle from level l0 down, in
+// one cluster launch; false if clusters are unavailable or the list is too long.
+template <int NV>
+static bool vcycle_cluster(const hcop* h, AuxMG* M, int lr, int l0, const int* done, cudaStream_t s) {
+  (void)h;
+  if (!M->cluster_ok || l0 < 0 || l0 >= M->nlev) return false;
+  std::vector<VStep> steps;
+  if (lr >= 0) steps.push_back(VStep{kOpRestrict, lr, 0, 0, 0.0f, 0.0f});
+  vcycle_steps(M, l0, steps);
+  if ((int)steps.size() > kMaxVSteps) return false;
+  VCycleArgs a{};
+  a.nlev = M->nlev;
+  a.nsteps = (int)steps.size();
+  a.bar = M->bar;
+  for (int l = 0; l < M->nlev; ++l) {
+    const AuxLevel& L = M->lev[l];
+    a.lev[l] = VLevelDev{L.d, L.St, L.dinv, L.x, L.b, L.r, L.dv, L.t, cheb_coef(L.lmax, 1).inv_theta};
+  }
+  for (int k = 0; k < a.nsteps; ++k) a.step[k] = steps[k];
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(kClusterCtas);
+  cfg.blockDim = dim3(kClusterThreads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = kClusterCtas;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  // a failed launch is also the thread's last error, which the caller reads
+  (void)cudaLaunchKernelEx(&cfg, k_vcycle_cluster<NV>, a, done);
+  return true;
+}
+
 // Blocks of the cooperative V-cycle: co-resident by construction (occupancy
 // x SMs, at most 2 per SM); 0 when the device cannot launch cooperatively.
 static void coop_setup(hcop* h, AuxMG* M) {
   M->coop_blocks = M->coop_blocks2 = 0;
+  // thread-block clusters of kClusterCtas: at least one must fit for each NV
+  {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(kClusterCtas);
+    cfg.blockDim = dim3(kClusterThreads);
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = kClusterCtas;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int c1 = 0, c2 = 0;
+    const bool ok = cudaOccupancyMaxActiveClusters(&c1, k_vcycle_cluster<1>, &cfg) == cudaSuccess &&
+                    cudaOccupancyMaxActiveClusters(&c2, k_vcycle_cluster<2>, &cfg) == cudaSuccess;
+    if (!ok) cudaGetLastError();
+    M->cluster_ok = ok && c1 > 0 && c2 > 0;
+  }
   int dev = 0, coop = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return;
   if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return;
@@ -1312,7 +1419,7 @@ cudaError_t auxmg_apply(const hcop* h, const T* r0, const T* r1, T* z0, T* z1, c
     return cudaGetLastError();
   }
   const void* key[5] = {r0, r1, z0, z1, done};
-  const int coop = coop_from_level() + 1;
+  const int coop = vcycle_mode();
   for (AuxGraph& g : M->graphs) {
     if (g.exec && g.nv == NV && g.tsize == (int)sizeof(T) && g.coop == coop &&
         std::memcmp(g.key, key, sizeof(key)) == 0 && std::memcmp(g.coef, coef, sizeof(g.coef)) == 0)

@@ -924,6 +924,7 @@ cudaError_t hex_launch_p(const HexDev& d, const T* fac, const T* x, T* y, T ms, 
       int& occ = per_sm[f][o][sizeof(T) == 8];
       if (!occ) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nt, sm);
         if (occ < 1) occ = 1;
       }

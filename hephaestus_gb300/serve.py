@@ -210,7 +210,8 @@ class GpuExecutor:
     stream (one per worker).  keep: False, True, or a predicate on the
     request -- the final A of kept requests is copied to the host (kept)."""
 
-    def __init__(self, slots, precision="mixed", precond="aux", rtol=1e-12, dt=0.01, keep=False, inner_rtol=3e-4):
+    def __init__(self, slots, precision="mixed_rr", precond="aux", rtol=1e-12, dt=0.01, keep=False,
+                 inner_rtol=None):
         import torch
 
         self.torch = torch
@@ -221,7 +222,8 @@ class GpuExecutor:
         self.dt = dt
         self.keep = keep
         self.kept = {}
-        self.inner_rtol = inner_rtol
+        # residual replacement: replace after a 10x drop; refinement: inner solves to 3e-4
+        self.inner_rtol = inner_rtol if inner_rtol is not None else (0.1 if precision == "mixed_rr" else 3e-4)
 
     @staticmethod
     def fields(req):

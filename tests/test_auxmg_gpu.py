@@ -150,10 +150,12 @@ def test_aux_cocg_converges_at_low_frequency_where_jacobi_stalls():
 
 @pytest.mark.parametrize("n, p", [(40, 2), (24, 1), (17, 3)])
 def test_cooperative_vcycle_equals_per_step_kernels(n, p, monkeypatch):
-    """The Q1 V-cycle as one cooperative launch (grid barriers between steps;
-    HC_AUX_VCYCLE=coop: all levels, =hybrid (the default): the levels below
-    the finest) runs the same steps with the same per-node arithmetic as the
-    per-step kernels (HC_AUX_VCYCLE=kernels): on one handle, z = B r through
+    """The Q1 V-cycle's launch forms -- one cooperative launch with grid
+    barriers (HC_AUX_VCYCLE=coop: all levels, =hybrid: the levels below the
+    finest), the coarse levels in one thread-block cluster (=cluster; with
+    n = 17, p = 3 the whole cycle) -- run the same steps with the same per-node
+    arithmetic as the per-step kernels (HC_AUX_VCYCLE=kernels, the default):
+    on one handle, z = B r through
     hc_precond_apply_device is bit-identical (no atomics on this path), on
     hierarchies of 3-4 levels and odd grid sizes; and B is D^-1 plus a
     positive semi-definite correction (r.(z - D^-1 r) >= 0 up to the
@@ -167,7 +169,7 @@ def test_cooperative_vcycle_equals_per_step_kernels(n, p, monkeypatch):
     r = torch.tensor(np.random.default_rng(3).standard_normal(op.ndof), device="cuda")
     r2 = torch.tensor(np.random.default_rng(4).standard_normal(op.ndof), device="cuda")
     zs = {}
-    for mode in ("coop", "kernels", "hybrid", "coop"):
+    for mode in ("coop", "kernels", "hybrid", "cluster", "coop"):
         monkeypatch.setenv("HC_AUX_VCYCLE", mode)
         z, z2 = torch.empty_like(r), torch.empty_like(r)
         op.PrecondApplyDevice(r, z, "aux")
@@ -178,7 +180,7 @@ def test_cooperative_vcycle_equals_per_step_kernels(n, p, monkeypatch):
     op.PrecondApplyDevice(r, zj, "jacobi")
     for k in (0, 1):
         b = zs["kernels"][0][k]
-        for mode in ("coop", "hybrid"):
+        for mode in ("coop", "hybrid", "cluster"):
             a = zs[mode][0][k]
             d = np.abs(a - b)
             assert np.array_equal(a, b), (mode, k, int(np.count_nonzero(d)), float(d.max() / np.abs(b).max()))

@@ -15,17 +15,18 @@ def _stream():
     return S.make_stream(10, rate=300.0, seed=11, dof_range=(1e4, 1.5e5), steps=3)
 
 
-def test_results_same_alone_and_in_the_mix():
+@pytest.mark.parametrize("precision", ["mixed", "mixed_rr"])
+def test_results_same_alone_and_in_the_mix(precision):
     import torch
 
     free, _ = torch.cuda.mem_get_info()
-    mix = S.GpuExecutor(slots=4, precision="mixed", rtol=1e-12, keep=True)
+    mix = S.GpuExecutor(slots=4, precision=precision, rtol=1e-12, keep=True)
     done, wall = S.run_stream(_stream(), mix, budget_bytes=int(0.3 * free), slots=4)
     assert all(r.result["status"] == "OK" for r in done), [r.result for r in done]
     # overlap really happened: some request started before another finished
     spans = sorted((r.start, r.finish) for r in done)
     assert any(spans[k + 1][0] < spans[k][1] for k in range(len(spans) - 1))
-    alone = S.GpuExecutor(slots=1, precision="mixed", rtol=1e-12, keep=True)
+    alone = S.GpuExecutor(slots=1, precision=precision, rtol=1e-12, keep=True)
     ref64 = S.GpuExecutor(slots=1, precision="fp64", rtol=1e-12, keep=True)
     for r in _stream():
         alone(r, 0)
@@ -39,7 +40,8 @@ def test_results_same_alone_and_in_the_mix():
         assert np.linalg.norm(a_mix - a64) / nrm <= TOL, rid
 
 
-def test_served_results_match_the_oracle():
+@pytest.mark.parametrize("precision", ["mixed", "mixed_rr"])
+def test_served_results_match_the_oracle(precision):
     """Requests served concurrently (mixed precision, rtol 1e-12) against the
     oracle's backward-Euler steps with FP64 sparse direct solves of the same
     seeded problems (small requests, so the direct solves stay quick)."""
@@ -50,7 +52,7 @@ def test_served_results_match_the_oracle():
 
     reqs = S.make_stream(4, rate=300.0, seed=13, dof_range=(1e4, 3e4), steps=3, multi_step_frac=0.5)
     free, _ = torch.cuda.mem_get_info()
-    ex = S.GpuExecutor(slots=4, precision="mixed", rtol=1e-12, keep=True)
+    ex = S.GpuExecutor(slots=4, precision=precision, rtol=1e-12, keep=True)
     done, _ = S.run_stream(reqs, ex, budget_bytes=int(0.3 * free), slots=4)
     assert all(r.result["status"] == "OK" for r in done), [r.result for r in done]
     for r in done:
