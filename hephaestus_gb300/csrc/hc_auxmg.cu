@@ -515,14 +515,25 @@ __device__ __forceinline__ void gt_at(const HexDev& h, const AuxTab& tab, const 
     // visit 1: (e0, q0) inside, else (e0 - 1, P); visit 2: (e0, 0) on a boundary
     const int ea = q0 != 0 ? e0 : max(e0 - 1, 0), qa = q0 != 0 ? q0 : P;
     const float ma = (q0 != 0 || ic > 0) ? 1.0f : 0.0f;
-    const int eb = min(e0, ne[c] - 1);
-    const float mb = (q0 == 0 && e0 < ne[c]) ? 1.0f : 0.0f;
 #pragma unroll
     for (int a2 = 0; a2 < P; ++a2) {
-      const float wa = ma * tab.D[a2][qa], wb = mb * tab.D[a2][0];
-      const int ga = b0 + (ea * P + a2) * s_c, gb = b0 + (eb * P + a2) * s_c;
+      const float wa = ma * tab.D[a2][qa];
+      const int ga = b0 + (ea * P + a2) * s_c;
 #pragma unroll
-      for (int v = 0; v < NV; ++v) acc[v] += wa * (float)rr[v][ga] + wb * (float)rr[v][gb];
+      for (int v = 0; v < NV; ++v) acc[v] += wa * (float)rr[v][ga];
+    }
+    // the second visit only on element boundaries: the same for the whole warp
+    // along y and z (J, K are block coordinates), divergent only along x
+    if (c == 0 || q0 == 0) {
+      const int eb = min(e0, ne[c] - 1);
+      const float mb = (q0 == 0 && e0 < ne[c]) ? 1.0f : 0.0f;
+#pragma unroll
+      for (int a2 = 0; a2 < P; ++a2) {
+        const float wb = mb * tab.D[a2][0];
+        const int gb = b0 + (eb * P + a2) * s_c;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) acc[v] += wb * (float)rr[v][gb];
+      }
     }
   }
 }

@@ -696,7 +696,7 @@ __device__ __forceinline__ void flush_comp(const HexDev& d, T* __restrict__ y, T
 }
 
 template <typename T, int P, bool FULL, int BX, int BY, int BZ, bool OVERWRITE>
-__global__ void __launch_bounds__(BX* BY* BZ, sizeof(T) == 4 ? 3 : 2)
+__global__ void __launch_bounds__(BX* BY* BZ, sizeof(T) == 4 ? (FULL ? 3 : 4) : 2)
     hex_apply_tiled(HexDev d, const T* __restrict__ fac, const T* __restrict__ x, T* __restrict__ y, T mscale,
                     T cscale, int masked, KrylovScalars* S, double* partials, int nbricks) {
   if (S && S->done) return;
@@ -790,14 +790,48 @@ __global__ void __launch_bounds__(BX* BY* BZ, sizeof(T) == 4 ? 3 : 2)
       T r0[RTC], r1[RTC], r2[RTC];
       curl_nd<T, P>(u0, u1, u2, r0, r1, r2);
       T y0[NDC], y1[NDC], y2[NDC];
-      if (mscale == T(0)) {
+      T g0[RTC], g1[RTC], g2[RTC];
+      T eacc = T(0);
+      if constexpr (!FULL) {
+        // axis-aligned: the blocks are diagonal, so each u_c and r_c is last
+        // used by its own mass block -- computed one component at a time they
+        // die early, which keeps the live set (and the register count) down
+        auto mass_c = [&](auto cc, const T* u, T* yv) {
+          constexpr int c = decltype(cc)::value;
+          if (mscale == T(0)) {
 #pragma unroll
-        for (int i = 0; i < NDC; ++i) y0[i] = y1[i] = y2[i] = T(0);
+            for (int i = 0; i < NDC; ++i) yv[i] = T(0);
+          } else {
+            mass_block<T, P, c, c, false>(u, yv, fm[c == 0 ? 0 : (c == 1 ? 3 : 5)]);
+          }
+          if (S) {
+#pragma unroll
+            for (int i = 0; i < NDC; ++i) eacc += u[i] * yv[i];
+          }
+        };
+        mass_c(std::integral_constant<int, 2>{}, u2, y2);
+        mass_c(std::integral_constant<int, 1>{}, u1, y1);
+        mass_c(std::integral_constant<int, 0>{}, u0, y0);
+        auto rt_c = [&](auto cc, const T* r, T* gv) {
+          constexpr int c = decltype(cc)::value;
+          rt_block<T, P, c, c, false>(r, gv, fc[c == 0 ? 0 : (c == 1 ? 3 : 5)]);
+          if (S) {
+#pragma unroll
+            for (int i = 0; i < RTC; ++i) eacc += r[i] * gv[i];
+          }
+        };
+        rt_c(std::integral_constant<int, 0>{}, r0, g0);
+        rt_c(std::integral_constant<int, 1>{}, r1, g1);
+        rt_c(std::integral_constant<int, 2>{}, r2, g2);
+        if (S) en += (double)eacc;
       } else {
-        mass_block<T, P, 0, 0, false>(u0, y0, fm[0]);
-        mass_block<T, P, 1, 1, false>(u1, y1, fm[3]);
-        mass_block<T, P, 2, 2, false>(u2, y2, fm[5]);
-        if constexpr (FULL) {
+        if (mscale == T(0)) {
+#pragma unroll
+          for (int i = 0; i < NDC; ++i) y0[i] = y1[i] = y2[i] = T(0);
+        } else {
+          mass_block<T, P, 0, 0, false>(u0, y0, fm[0]);
+          mass_block<T, P, 1, 1, false>(u1, y1, fm[3]);
+          mass_block<T, P, 2, 2, false>(u2, y2, fm[5]);
           mass_block<T, P, 0, 1>(u1, y0, fm[1]);
           mass_block<T, P, 0, 2>(u2, y0, fm[2]);
           mass_block<T, P, 1, 0>(u0, y1, fm[1]);
@@ -805,28 +839,24 @@ __global__ void __launch_bounds__(BX* BY* BZ, sizeof(T) == 4 ? 3 : 2)
           mass_block<T, P, 2, 0>(u0, y2, fm[2]);
           mass_block<T, P, 2, 1>(u1, y2, fm[4]);
         }
-      }
-      T eacc = T(0);
-      if (S) {
+        if (S) {
 #pragma unroll
-        for (int i = 0; i < NDC; ++i) eacc += u0[i] * y0[i] + u1[i] * y1[i] + u2[i] * y2[i];
-      }
-      T g0[RTC], g1[RTC], g2[RTC];
-      rt_block<T, P, 0, 0, false>(r0, g0, fc[0]);
-      rt_block<T, P, 1, 1, false>(r1, g1, fc[3]);
-      rt_block<T, P, 2, 2, false>(r2, g2, fc[5]);
-      if constexpr (FULL) {
+          for (int i = 0; i < NDC; ++i) eacc += u0[i] * y0[i] + u1[i] * y1[i] + u2[i] * y2[i];
+        }
+        rt_block<T, P, 0, 0, false>(r0, g0, fc[0]);
+        rt_block<T, P, 1, 1, false>(r1, g1, fc[3]);
+        rt_block<T, P, 2, 2, false>(r2, g2, fc[5]);
         rt_block<T, P, 0, 1>(r1, g0, fc[1]);
         rt_block<T, P, 0, 2>(r2, g0, fc[2]);
         rt_block<T, P, 1, 0>(r0, g1, fc[1]);
         rt_block<T, P, 1, 2>(r2, g1, fc[4]);
         rt_block<T, P, 2, 0>(r0, g2, fc[2]);
         rt_block<T, P, 2, 1>(r1, g2, fc[4]);
-      }
-      if (S) {
+        if (S) {
 #pragma unroll
-        for (int i = 0; i < RTC; ++i) eacc += r0[i] * g0[i] + r1[i] * g1[i] + r2[i] * g2[i];
-        en += (double)eacc;
+          for (int i = 0; i < RTC; ++i) eacc += r0[i] * g0[i] + r1[i] * g1[i] + r2[i] * g2[i];
+          en += (double)eacc;
+        }
       }
       curl_nd_t<T, P>(g0, g1, g2, y0, y1, y2);
       sscatter<T, P, BX, BY, BZ, 0>(sy, lx, ly, lz, y0);
