@@ -549,8 +549,8 @@ def run_batch(args):
     db = B.DeviceBatch(probs, dict(base, Precision="fp64"))
     setup_s = time.perf_counter() - t0
     res, sols, times = {}, {}, {}
-    for prec in ("fp64", "mixed"):
-        db.set_params(dict(base, Precision=prec))
+    for prec in ("fp64", "mixed", "mixed_rr"):
+        db.set_params(dict(base, Precision=prec, InnerTolerance=0.1 if prec == "mixed_rr" else args.inner_rtol))
         db.zero()
         db.solve()  # graph construction + warm-up
         db.zero()
@@ -560,16 +560,24 @@ def run_batch(args):
         torch.cuda.synchronize()
         times[prec] = time.perf_counter() - t0
         sols[prec] = db.solutions()
-    rel = []
-    for (ar, ai), (br, bi) in zip(sols["mixed"], sols["fp64"]):
-        d = torch.sqrt(torch.sum((ar - br) ** 2 + (ai - bi) ** 2))
-        nrm = torch.sqrt(torch.sum(br ** 2 + bi ** 2))
-        rel.append(float(d / nrm))
+    rels, goods = {}, {}
     ok = {p: sum(r["status"] == "OK" for r in res[p]) for p in res}
-    good = sum(1 for k in range(len(probs)) if res["mixed"][k]["status"] == "OK" and rel[k] <= 1e-10)
+    for m in ("mixed", "mixed_rr"):
+        rel = []
+        for (ar, ai), (br, bi) in zip(sols[m], sols["fp64"]):
+            d = torch.sqrt(torch.sum((ar - br) ** 2 + (ai - bi) ** 2))
+            nrm = torch.sqrt(torch.sum(br ** 2 + bi ** 2))
+            rel.append(float(d / nrm))
+        rels[m] = rel
+        goods[m] = sum(1 for k in range(len(probs)) if res[m][k]["status"] == "OK" and rel[k] <= 1e-10)
+    # headline: the faster mixed form, counting only solves within 1e-10 of FP64
+    best = max(("mixed", "mixed_rr"), key=lambda m: goods[m] / times[m])
+    rel, good = rels["mixed"], goods["mixed"]
     line = {
         "metric": "converged complex solves/s, batch of %d uneven eddy-current problems (mixed vs FP64)" % len(probs),
-        "value": good / times["mixed"], "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
+        "value": goods[best] / times[best], "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
+        "headline_form": {"mixed": "FP32 COCG inside FP64 refinement",
+                          "mixed_rr": "one FP32 COCG with FP64 residual replacement"}[best],
         "dtype": "f32 inner / f64 refinement", "data": "synthetic (seeded meshes, fields, frequencies)",
         "config": {"workload": "complex_batch%d: cube hex n in U{8..40}, p in {1,2,3}, omega log-U[1e1,1e5], "
                                "nu 10^U(0,3), sigma 10^U(-2,6), coil RHS" % len(probs),
@@ -580,7 +588,11 @@ def run_batch(args):
         "fp64": {"solves_per_s": ok["fp64"] / times["fp64"], "seconds": times["fp64"], "converged": ok["fp64"]},
         "mixed": {"solves_per_s": ok["mixed"] / times["mixed"], "seconds": times["mixed"], "converged": ok["mixed"],
                   "within_1e-10_of_fp64": good},
+        "mixed_rr": {"solves_per_s": ok["mixed_rr"] / times["mixed_rr"], "seconds": times["mixed_rr"],
+                     "converged": ok["mixed_rr"], "within_1e-10_of_fp64": goods["mixed_rr"],
+                     "rel_err_vs_fp64": {"max": max(rels["mixed_rr"]), "median": float(np.median(rels["mixed_rr"]))}},
         "speedup_mixed_over_fp64": (ok["mixed"] / times["mixed"]) / max(ok["fp64"] / times["fp64"], 1e-30),
+        "speedup_mixed_rr_over_fp64": (ok["mixed_rr"] / times["mixed_rr"]) / max(ok["fp64"] / times["fp64"], 1e-30),
         "mdofs_solved_per_s": {p: sum(pb.ndof for pb, r in zip(probs, res[p]) if r["status"] == "OK") / times[p] / 1e6
                                for p in res},
         "rel_err_mixed_vs_fp64": {"max": max(rel), "median": float(np.median(rel))},
@@ -589,7 +601,7 @@ def run_batch(args):
     }
     # e2e: the same batch with its right-hand sides copied from pinned host
     # memory and its solutions copied back, inside the timed region
-    db.set_params(dict(base, Precision="mixed"))
+    db.set_params(dict(base, Precision=best, InnerTolerance=0.1 if best == "mixed_rr" else args.inner_rtol))
     db.zero()
     hb = [(b[0].cpu().pin_memory(), b[1].cpu().pin_memory()) for b in db.rhs]
     hx = [(torch.empty_like(b[0]), torch.empty_like(b[1])) for b in hb]

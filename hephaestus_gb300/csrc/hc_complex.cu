@@ -790,8 +790,8 @@ static hc_status complex_params(hcop* h, const hc_solve_params* p) {
     h->err = "null solve parameters";
     return HC_EINVAL;
   }
-  if (p->precision != HC_FP64 && p->precision != HC_MIXED) {
-    h->err = "precision must be HC_FP64 or HC_MIXED";
+  if (p->precision != HC_FP64 && p->precision != HC_MIXED && p->precision != HC_MIXED_RR) {
+    h->err = "precision must be HC_FP64, HC_MIXED or HC_MIXED_RR";
     return HC_EINVAL;
   }
   if (p->precond != HC_PRECOND_JACOBI && p->precond != HC_PRECOND_AUX) {
@@ -812,6 +812,11 @@ hc_status hc_solve_complex_device(hcop_t* h, const hc_solve_params* prm, double 
   if (st == HC_OK) st = complex_params(h, prm);
   if (st != HC_OK) return st;
   hc_solve_info loc{};
+  if (prm->precision == HC_MIXED_RR) {  // residual replacement is built in the graph-driven solve
+    st = complex_graph_launch(h, prm, omega, br, bi, xr, xi, 0);
+    if (st != HC_OK) return st;
+    return complex_graph_result(h, info ? info : &loc);
+  }
   return complex_solve_device(h, prm, omega, br, bi, xr, xi, info ? info : &loc);
 }
 
@@ -829,7 +834,12 @@ hc_status hc_solve_complex(hcop_t* h, const hc_solve_params* prm, double omega, 
   hc_status sst = HC_ECUDA;
   if (e == cudaSuccess) {
     hc_solve_info loc{};
-    sst = complex_solve_device(h, prm, omega, d, d + n, d + 2 * n, d + 3 * n, info ? info : &loc);
+    if (prm->precision == HC_MIXED_RR) {
+      sst = complex_graph_launch(h, prm, omega, d, d + n, d + 2 * n, d + 3 * n, 0);
+      if (sst == HC_OK) sst = complex_graph_result(h, info ? info : &loc);
+    } else {
+      sst = complex_solve_device(h, prm, omega, d, d + n, d + 2 * n, d + 3 * n, info ? info : &loc);
+    }
   }
   if (e == cudaSuccess && sst != HC_ECUDA && sst != HC_ENOMEM)
     e = cudaMemcpyAsync(x, d + 2 * n, 2 * n * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
@@ -889,6 +899,10 @@ namespace hc {
 struct CRefine {
   double rn, bn, tol, rtol, atol, rn_prev;
   int outer, total, max_outer, maxit, status, active, trips, polish;
+  // residual replacement (HC_MIXED_RR): FP32 units of the initial residual,
+  // recursive |r|^2 at the last replacement, replacement threshold
+  double scale, rr_last, delta2;
+  int since, slow, stop;
 };
 
 __global__ void k_g_init(CScalars* S, double rtol2, double atol2, int maxit) {
@@ -1007,6 +1021,123 @@ __global__ void k_r_accum(int64_t n, CRefine* R, const CScalars* S, const float*
   }
 }
 
+// ---- residual replacement in the graph-driven COCG (HC_MIXED_RR) ----------------------
+// One FP32 COCG runs through; at the end of a batch of iterations where its
+// recursive residual fell by delta since the last replacement, met its
+// tolerance, or 8 batches passed, an IF node adds the FP32 correction to the
+// FP64 x, computes b - J x in FP64 and puts it (in units of the initial
+// residual) in place of the FP32 recursive residual; direction and r^T z are
+// kept (van der Vorst & Ye residual replacement, as in the real solver).
+__global__ void k_rr_start(CRefine* R, CScalars* S, double delta2, cudaGraphConditionalHandle hl) {
+  const double rn = sqrt(S->rr);
+  R->bn = sqrt(S->bb);
+  R->tol = fmax(R->rtol * R->bn, R->atol);
+  R->rn = rn;
+  R->rn_prev = rn;
+  R->scale = rn > 0.0 ? rn : 1.0;
+  R->rr_last = 1.0;
+  R->delta2 = delta2;
+  R->since = R->slow = R->stop = 0;
+  int go = 1;
+  if (!isfinite(rn)) {
+    R->status = HC_BREAKDOWN;
+    go = 0;
+  } else if (rn <= R->tol) {
+    R->status = HC_OK;
+    go = 0;
+  }
+  R->active = go;
+  R->stop = !go;
+  // the FP32 COCG's stopping test, relative to |r0 / scale| = 1
+  const double t = 0.5 * R->tol / R->scale;
+  S->rtol2 = t * t;
+  S->atol2 = 0.0;
+  S->maxit = R->maxit;
+  S->trips = 0;
+  S->done = go ? 0 : 1;
+  cudaGraphSetConditional(hl, (unsigned)go);
+}
+
+// end of a batch: is a replacement due?
+__global__ void k_rr_due(CRefine* R, const CScalars* S, cudaGraphConditionalHandle hif) {
+  int due = 0;
+  if (!(S->done && S->status == HC_BREAKDOWN)) {
+    ++R->since;
+    due = S->done || S->rr <= R->delta2 * R->rr_last || R->since >= 8;
+  }
+  if (due) R->since = 0;
+  cudaGraphSetConditional(hif, (unsigned)due);
+}
+
+// x += scale c, c = 0
+__global__ void k_rr_fold(int64_t n, const CRefine* R, float* cr, float* ci, double* xr, double* xi) {
+  const double s = R->scale;
+  GS_LOOP(k, n) {
+    xr[k] += s * (double)cr[k];
+    xi[k] += s * (double)ci[k];
+    cr[k] = 0.0f;
+    ci[k] = 0.0f;
+  }
+}
+
+// decision from the FP64 residual (S->rr = |b - J x|^2 from k_c_resid64)
+__global__ void k_rr_after(CRefine* R, CScalars* S) {
+  const double rn = sqrt(S->rr);
+  R->rn = rn;
+  R->total = S->it;
+  R->outer += 1;
+  if (!isfinite(rn)) {
+    R->status = HC_BREAKDOWN;
+    R->stop = 1;
+  } else if (rn <= R->tol) {
+    R->status = HC_OK;
+    R->stop = 1;
+  } else if (S->it >= S->maxit) {
+    R->status = HC_NOT_CONVERGED;
+    R->stop = 1;
+  } else {
+    R->slow = rn > 0.5 * R->rn_prev ? R->slow + 1 : 0;
+    R->rn_prev = rn;
+    if (R->slow >= 2) {  // the FP32 iteration stopped paying: finish in FP64
+      R->status = HC_NOT_CONVERGED;
+      R->polish = 1;
+      R->stop = 1;
+    }
+  }
+  if (R->stop) {
+    S->done = 1;
+    return;
+  }
+  const double rr = S->rr / (R->scale * R->scale);
+  S->rr = rr;
+  S->done = 0;
+  S->status = HC_NOT_CONVERGED;
+  R->rr_last = rr;
+}
+
+// the FP32 recursive residual := (b - J x) / scale
+__global__ void k_rr_d2f(int64_t n, const CRefine* R, const double* a, const double* b, float* af, float* bf) {
+  if (R->stop) return;
+  const double s = 1.0 / R->scale;
+  GS_LOOP(k, n) {
+    af[k] = (float)(a[k] * s);
+    bf[k] = (float)(b[k] * s);
+  }
+}
+
+// after the loop: a batch that ended on the iteration cap or a breakdown
+// without a replacement leaves its correction in c; its true residual decides
+__global__ void k_rr_final(CRefine* R, const CScalars* S) {
+  const double rn = sqrt(S->rr);
+  if (!R->stop) {
+    R->rn = rn;
+    R->total = S->it;
+    R->status = !isfinite(rn) ? HC_BREAKDOWN : (rn <= R->tol ? HC_OK : (S->status == HC_BREAKDOWN ? HC_BREAKDOWN
+                                                                                                 : HC_NOT_CONVERGED));
+    R->stop = 1;
+  }
+}
+
 struct ComplexGraph {
   cudaGraphExec_t exec = nullptr;
   cudaStream_t cap = nullptr;
@@ -1079,6 +1210,93 @@ static hc_status complex_graph_build(hcop* h, const hc_solve_params* prm, double
         }
         k_c_cond<<<1, 1, 0, s>>>(S, hl, unit);
         return cudaGetLastError();
+      });
+  } else if (prm->precision == HC_MIXED_RR) {
+    double* r64 = (double*)w->vec;
+    double* i64 = r64 + n;
+    float* rf = (float*)(i64 + n);
+    float* if_ = rf + n;
+    float* cr = if_ + n;
+    float* ci = cr + n;
+    const CocgPlan<float> plan{h, omega, aux, ci + n, S};
+    CRefine* R = G->R;
+    const double delta = prm->inner_rtol > 0 ? std::min(prm->inner_rtol, 0.5) : 0.1;
+    const int max_outer = prm->max_outer > 0 ? prm->max_outer : 50;
+    cudaGraphConditionalHandle hl = 0, hif = 0;
+    GraphChain body, rep;
+    if (e == cudaSuccess) e = chain_handle(c, &hl);
+    if (e == cudaSuccess)
+      e = chain_segment(c, G->cap, [&](cudaStream_t s) {
+        k_r_init<<<1, 1, 0, s>>>(R, prm->rtol, prm->atol, prm->maxit, max_outer);
+        cudaError_t ee = complex_apply_done<double>(h, omega, xr, xi, r64, i64, nullptr, s);
+        if (ee != cudaSuccess) return ee;
+        k_c_resid64<<<cgrid(n), kRedThreads, 0, s>>>(n, br, bi, r64, i64, S, h->partials);
+        k_rr_start<<<1, 1, 0, s>>>(R, S, delta * delta, hl);
+        // rf = r / |r|, c = 0 (scale = |r| = R->rn at the start)
+        k_r_d2f<<<cgrid(n), kRedThreads, 0, s>>>(n, R, r64, i64, rf, if_, cr, ci);
+        return plan.setup(rf, if_, nullptr, nullptr, true, &R->active, s);
+      });
+    if (e == cudaSuccess) e = chain_while(c, hl, &body);
+    if (e == cudaSuccess) e = chain_handle(body, &hif);
+    if (e == cudaSuccess)
+      e = chain_segment(body, G->cap, [&](cudaStream_t s) {
+        for (int k = 0; k < chunk; ++k) {
+          cudaError_t ee = plan.iterate(cr, ci, s);
+          if (ee != cudaSuccess) return ee;
+        }
+        k_rr_due<<<1, 1, 0, s>>>(R, S, hif);
+        return cudaGetLastError();
+      });
+    if (e == cudaSuccess) e = chain_if(body, hif, &rep);
+    if (e == cudaSuccess)
+      e = chain_segment(rep, G->cap, [&](cudaStream_t s) {
+        k_rr_fold<<<cgrid(n), kRedThreads, 0, s>>>(n, R, cr, ci, xr, xi);
+        cudaError_t ee = complex_apply_done<double>(h, omega, xr, xi, r64, i64, nullptr, s);
+        if (ee != cudaSuccess) return ee;
+        k_c_resid64<<<cgrid(n), kRedThreads, 0, s>>>(n, br, bi, r64, i64, S, h->partials);
+        k_rr_after<<<1, 1, 0, s>>>(R, S);
+        k_rr_d2f<<<cgrid(n), kRedThreads, 0, s>>>(n, R, r64, i64, plan.r(0), plan.r(1));
+        return cudaGetLastError();
+      });
+    if (e == cudaSuccess)
+      e = chain_segment(body, G->cap, [&](cudaStream_t s) {
+        k_c_cond<<<1, 1, 0, s>>>(S, hl, unit);
+        return cudaGetLastError();
+      });
+    // the correction of a loop that ended without a replacement, and the true residual
+    if (e == cudaSuccess)
+      e = chain_segment(c, G->cap, [&](cudaStream_t s) {
+        k_rr_fold<<<cgrid(n), kRedThreads, 0, s>>>(n, R, cr, ci, xr, xi);
+        cudaError_t ee = complex_apply_done<double>(h, omega, xr, xi, r64, i64, nullptr, s);
+        if (ee != cudaSuccess) return ee;
+        k_c_resid64<<<cgrid(n), kRedThreads, 0, s>>>(n, br, bi, r64, i64, S, h->partials);
+        k_rr_final<<<1, 1, 0, s>>>(R, S);
+        return cudaGetLastError();
+      });
+    // FP64 polish (runs only when the FP32 iteration stalled)
+    const CocgPlan<double> p64{h, omega, aux, (double*)((char*)w->vec + polish_offset(n)), S};
+    cudaGraphConditionalHandle hp = 0;
+    GraphChain pb;
+    if (e == cudaSuccess) e = chain_handle(c, &hp);
+    if (e == cudaSuccess)
+      e = chain_segment(c, G->cap, [&](cudaStream_t s) {
+        k_polish_init<<<1, 1, 0, s>>>(S, R, prm->rtol * prm->rtol, prm->atol * prm->atol, hp);
+        return p64.setup(br, bi, xr, xi, false, &R->polish, s, &S->done);
+      });
+    if (e == cudaSuccess) e = chain_while(c, hp, &pb);
+    if (e == cudaSuccess)
+      e = chain_segment(pb, G->cap, [&](cudaStream_t s) {
+        for (int k = 0; k < chunk; ++k) {
+          cudaError_t ee = p64.iterate(xr, xi, s);
+          if (ee != cudaSuccess) return ee;
+        }
+        k_c_cond<<<1, 1, 0, s>>>(S, hp, unit);
+        return cudaGetLastError();
+      });
+    if (e == cudaSuccess)
+      e = chain_segment(c, G->cap, [&](cudaStream_t s) {
+        k_polish_finish<<<1, 1, 0, s>>>(R, S);
+        return cudaMemcpyAsync(G->hR, R, sizeof(CRefine), cudaMemcpyDeviceToHost, s);
       });
   } else {
     double* r64 = (double*)w->vec;

@@ -1,7 +1,7 @@
 // hc_graph.h -- building device-driven solve graphs.
 //
 // A solve graph is a chain of captured segments (child-graph nodes) and
-// conditional WHILE nodes.  A WHILE body ends with a kernel that sets the
+// conditional WHILE and IF nodes.  A WHILE body ends with a kernel that sets the
 // loop condition from device state (the solver's `done` flag and a trip
 // counter with a hard bound), so a launched solve runs to completion on the
 // device without host round trips and always terminates.
@@ -46,6 +46,23 @@ inline cudaError_t chain_while(GraphChain& c, cudaGraphConditionalHandle hnd, Gr
   p.type = cudaGraphNodeTypeConditional;
   p.conditional.handle = hnd;
   p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  cudaGraphNode_t n = nullptr;
+  const cudaError_t e = cudaGraphAddNode(&n, c.graph, c.last ? &c.last : nullptr, nullptr, c.last ? 1 : 0, &p);
+  if (e != cudaSuccess) return e;
+  c.last = n;
+  body->graph = p.conditional.phGraph_out[0];
+  body->last = nullptr;
+  return cudaSuccess;
+}
+
+// Append an IF node driven by hnd (condition set by a kernel before it);
+// body receives its (empty) chain.
+inline cudaError_t chain_if(GraphChain& c, cudaGraphConditionalHandle hnd, GraphChain* body) {
+  cudaGraphNodeParams p{};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = hnd;
+  p.conditional.type = cudaGraphCondTypeIf;
   p.conditional.size = 1;
   cudaGraphNode_t n = nullptr;
   const cudaError_t e = cudaGraphAddNode(&n, c.graph, c.last ? &c.last : nullptr, nullptr, c.last ? 1 : 0, &p);

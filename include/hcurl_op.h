@@ -66,10 +66,12 @@ enum {
   HC_MIXED = 2,  /* FP32 inner PCG inside FP64 iterative refinement       */
   HC_BF16 = 3,   /* tet multi-RHS apply: BF16 element matrices, FP32
                     vectors and accumulation                               */
-  HC_MIXED_RR = 4 /* one FP32 PCG whose recursive residual is replaced by
-                    the FP64 residual b - J x (and its correction added to
-                    the FP64 x) each time it fell by inner_rtol; single
-                    right-hand-side solves (hc_solve_device)               */
+  HC_MIXED_RR = 4 /* one FP32 PCG (COCG for complex solves) whose recursive
+                    residual is replaced by the FP64 residual b - J x (and
+                    its correction added to the FP64 x) each time it fell
+                    by inner_rtol; single right-hand-side solves
+                    (hc_solve*, hc_solve_complex*: complex ones run the
+                    graph-driven solve)                                    */
 };
 
 /* HC_PRECOND_AUX: Jacobi plus the auxiliary-space gradient correction

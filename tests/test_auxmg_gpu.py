@@ -96,7 +96,7 @@ def test_aux_cuts_iterations_where_jacobi_stalls():
     assert its["jacobi"][0] != "OK" or its["jacobi"][1] > 5 * its["aux"][1], its
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_rr"])
 @pytest.mark.parametrize("p", [1, 2, 3])
 def test_aux_cocg_matches_direct(precision, p):
     import torch

@@ -78,7 +78,7 @@ def test_complex_apply_omega_zero_is_curlcurl():
 
 
 @pytest.mark.parametrize("p,omega", [(1, 1e2), (2, 1e3), (3, 1e4)])
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_rr"])
 def test_complex_solve_matches_direct(p, omega, precision):
     op, J, rng = _pair(3, p, omega, seed=10 + p)
     b = _crandn(rng, op.ndof)
@@ -139,7 +139,7 @@ def test_complex_entry_points_reject_bad_input():
     assert L.hc_mult_complex(top.h, 1.0, p(xt), p(yt)) == N.HC_ENOTSUP
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_rr"])
 @pytest.mark.parametrize("p", [1, 2, 3])
 def test_graph_solve_matches_direct_and_reuses_graph(precision, p):
     import torch
@@ -170,7 +170,7 @@ def test_graph_solve_stops_at_maxit():
     omega = 10.0
     op, J, rng = _pair(4, 2, omega, seed=41)
     b = _crandn(rng, op.ndof)
-    for precision in ("fp64", "mixed"):
+    for precision in ("fp64", "mixed", "mixed_rr"):
         s = GpuComplexCOCGSolver({"Tolerance": 1e-14, "MaxIter": 7, "Precision": precision}, op, omega)
         br = torch.tensor(b.real, device="cuda")
         bi = torch.tensor(b.imag, device="cuda")
