@@ -901,8 +901,8 @@ struct CRefine {
   int outer, total, max_outer, maxit, status, active, trips, polish;
   // residual replacement (HC_MIXED_RR): FP32 units of the initial residual,
   // recursive |r|^2 at the last replacement, replacement threshold
-  double scale, rr_last, delta2;
-  int since, slow, stop;
+  double scale, rr_last, delta2, rr_rec;
+  int since, slow, stop, flat;
 };
 
 __global__ void k_g_init(CScalars* S, double rtol2, double atol2, int maxit) {
@@ -1037,7 +1037,8 @@ __global__ void k_rr_start(CRefine* R, CScalars* S, double delta2, cudaGraphCond
   R->scale = rn > 0.0 ? rn : 1.0;
   R->rr_last = 1.0;
   R->delta2 = delta2;
-  R->since = R->slow = R->stop = 0;
+  R->since = R->slow = R->stop = R->flat = 0;
+  R->rr_rec = 1.0;
   int go = 1;
   if (!isfinite(rn)) {
     R->status = HC_BREAKDOWN;
@@ -1065,7 +1066,10 @@ __global__ void k_rr_due(CRefine* R, const CScalars* S, cudaGraphConditionalHand
     ++R->since;
     due = S->done || S->rr <= R->delta2 * R->rr_last || R->since >= 8;
   }
-  if (due) R->since = 0;
+  if (due) {
+    R->since = 0;
+    R->rr_rec = S->rr;  // the recursive residual the replacement is about to overwrite
+  }
   cudaGraphSetConditional(hif, (unsigned)due);
 }
 
@@ -1096,9 +1100,17 @@ __global__ void k_rr_after(CRefine* R, CScalars* S) {
     R->status = HC_NOT_CONVERGED;
     R->stop = 1;
   } else {
-    R->slow = rn > 0.5 * R->rn_prev ? R->slow + 1 : 0;
+    // FP32 floor: the true residual no longer halves while the recursive one
+    // runs ahead of it (10x in norm).  COCG's residual also has plateaus
+    // where both stall together: those are not a floor, but six of them in a
+    // row end the FP32 iteration too.
+    const double tr = rn / R->scale;
+    const bool drift = tr * tr > 100.0 * R->rr_rec;
+    const bool flat = rn > 0.5 * R->rn_prev;
+    R->slow = (flat && drift) ? R->slow + 1 : 0;
+    R->flat = flat ? R->flat + 1 : 0;
     R->rn_prev = rn;
-    if (R->slow >= 2) {  // the FP32 iteration stopped paying: finish in FP64
+    if (R->slow >= 2 || R->flat >= 6) {  // the FP32 iteration stopped paying: finish in FP64
       R->status = HC_NOT_CONVERGED;
       R->polish = 1;
       R->stop = 1;
