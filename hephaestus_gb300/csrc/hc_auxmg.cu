@@ -195,21 +195,18 @@ __global__ void k_stencil(Dims d, const float* __restrict__ Ke, float* __restric
   }
 }
 
-// Node-grid kernels run on a 3-D launch grid: x = position along a grid row,
-// y and z = the row's (j, k); no index decoding.
+// Node-grid kernels: a block of 256 threads covers 256 consecutive nodes of
+// one z-plane (the plane's rows flattened, i fastest), grid.y = the planes.
+// (One block per grid row left a third of the lanes idle on 65-node rows:
+// 66 nodes in 96 threads, the third warp with two active lanes.)
 struct NodeGrid {
   dim3 grid, block;
 };
-// rows of w nodes split into equal blocks of at most 256 threads (a row of
-// 129 becomes one block of 160, not 128 + 1)
-static inline int row_block(int w) {
-  const int nb = (w + 255) / 256;
-  return ((w + nb - 1) / nb + 31) / 32 * 32;
-}
+constexpr int kNodeThreads = 256;
 static inline NodeGrid node_grid(int nx, int ny, int nz) {
-  const int w = nx + 1;
-  const int bx = row_block(w);
-  return NodeGrid{dim3((unsigned)((w + bx - 1) / bx), (unsigned)(ny + 1), (unsigned)(nz + 1)), dim3((unsigned)bx)};
+  const int64_t plane = (int64_t)(nx + 1) * (ny + 1);
+  return NodeGrid{dim3((unsigned)((plane + kNodeThreads - 1) / kNodeThreads), (unsigned)(nz + 1), 1u),
+                  dim3((unsigned)kNodeThreads)};
 }
 // Transfer kernels on the large grids: KT consecutive z-planes per thread,
 // every load issued before the node's mask is applied, so that a thread keeps
@@ -219,13 +216,19 @@ static inline NodeGrid node_grid(int nx, int ny, int nz) {
 constexpr int kKT = 4;
 static inline NodeGrid node_grid_kt(int nx, int ny, int nz) {
   NodeGrid g = node_grid(nx, ny, nz);
-  g.grid.z = (unsigned)((nz + 1 + kKT - 1) / kKT);
+  g.grid.y = (unsigned)((nz + 1 + kKT - 1) / kKT);
   return g;
 }
-#define NODE_IJK(d, i, j, k, n)                                              \
-  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z; \
-  if (i > (d).nx) return;                                                   \
-  const int n = i + ((d).nx + 1) * (j + ((d).ny + 1) * k)
+// (i, j) of this thread's node in a plane of (nx + 1) x (ny + 1) nodes; threads
+// past the plane's end return
+#define PLANE_IJ(nx, ny, i, j)                                  \
+  const int t_ = blockIdx.x * blockDim.x + threadIdx.x;         \
+  if (t_ >= ((nx) + 1) * ((ny) + 1)) return;                    \
+  const int i = t_ % ((nx) + 1), j = t_ / ((nx) + 1)
+#define NODE_IJK(d, i, j, k, n)                                 \
+  PLANE_IJ((d).nx, (d).ny, i, j);                               \
+  const int k = blockIdx.y;                                     \
+  const int n = t_ + ((d).nx + 1) * ((d).ny + 1) * k
 
 // Loads of level vectors.  COH (the cooperative V-cycle, where one launch
 // writes a vector in one step and other blocks read it in a later one): L2
@@ -522,8 +525,8 @@ __device__ __forceinline__ void gt_at(const HexDev& h, const AuxTab& tab, const 
 #pragma unroll
       for (int v = 0; v < NV; ++v) acc[v] += wa * (float)rr[v][ga];
     }
-    // the second visit only on element boundaries: the same for the whole warp
-    // along y and z (J, K are block coordinates), divergent only along x
+    // the second visit only on element boundaries: along z the same for the
+    // whole warp, along y for all but the warps that straddle two rows
     if (c == 0 || q0 == 0) {
       const int eb = min(e0, ne[c] - 1);
       const float mb = (q0 == 0 && e0 < ne[c]) ? 1.0f : 0.0f;
@@ -543,19 +546,18 @@ __global__ void k_gt(HexDev h, AuxTab tab, const T* __restrict__ r0, const T* __
                      const int* __restrict__ done) {
   if (done && *done) return;
   const Dims qd{h.nx * P, h.ny * P, h.nz * P};
-  const int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y;
-  if (I > qd.nx) return;
+  PLANE_IJ(qd.nx, qd.ny, I, J);
   const int nq = (int)qd.nodes();
   float acc[kKT][NV], dq[kKT];
 #pragma unroll
   for (int t = 0; t < kKT; ++t) {  // gathers of all planes first
-    const int K = min((int)blockIdx.z * kKT + t, qd.nz);
+    const int K = min((int)blockIdx.y * kKT + t, qd.nz);
     gt_at<T, NV, P>(h, tab, r0, r1, qd.nx, qd.ny, I, J, K, acc[t]);
     dq[t] = qdinv[I + (qd.nx + 1) * (J + (qd.ny + 1) * K)];
   }
 #pragma unroll
   for (int t = 0; t < kKT; ++t) {
-    const int K = blockIdx.z * kKT + t;
+    const int K = blockIdx.y * kKT + t;
     if (K > qd.nz) break;
     const int n = I + (qd.nx + 1) * (J + (qd.ny + 1) * K);
 #pragma unroll
@@ -576,8 +578,7 @@ __global__ void k_g(HexDev h, AuxTab tab, const float* __restrict__ phi, const u
   if (done && *done) return;
   const int mx = h.nx * P, my = h.ny * P, mz = h.nz * P;
   const int n0 = mx + (c != 0), n1 = my + (c != 1), n2 = mz + (c != 2);
-  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-  if (i >= n0) return;
+  PLANE_IJ(n0 - 1, n1 - 1, i, j);
   const int nq = (mx + 1) * (my + 1) * (mz + 1);
   const int stride = c == 0 ? 1 : (c == 1 ? (mx + 1) : (mx + 1) * (my + 1));
   // loads of all kKT dofs first (phi gathers, masks, the z values), then the updates
@@ -586,7 +587,7 @@ __global__ void k_g(HexDev h, AuxTab tab, const float* __restrict__ phi, const u
   bool on[kKT];
 #pragma unroll
   for (int t = 0; t < kKT; ++t) {
-    const int k = blockIdx.z * kKT + t;
+    const int k = blockIdx.y * kKT + t;
     on[t] = k < n2;
     const int kk = on[t] ? k : n2 - 1;
     const int gd = (int)h.off[c] + i + n0 * (j + n1 * kk);
@@ -609,7 +610,7 @@ __global__ void k_g(HexDev h, AuxTab tab, const float* __restrict__ phi, const u
 #pragma unroll
   for (int t = 0; t < kKT; ++t) {
     if (!on[t]) continue;
-    const int k = blockIdx.z * kKT + t;
+    const int k = blockIdx.y * kKT + t;
     const int gd = (int)h.off[c] + i + n0 * (j + n1 * k);
     if (NV == 1) {
       z0[gd] = za[t] + (T)(c00 * v[t][0]);
@@ -632,8 +633,7 @@ template <int NV, int P>
 __global__ void k_rq(Dims vd, AuxTab tab, const float* __restrict__ g, const float* __restrict__ dinv1,
                      float* __restrict__ b1, ChebStart cs, const int* __restrict__ done) {
   if (done && *done) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-  if (i > vd.nx) return;
+  PLANE_IJ(vd.nx, vd.ny, i, j);
   const int mx = vd.nx * P, my = vd.ny * P, mz = vd.nz * P;
   const int nq = (mx + 1) * (my + 1) * (mz + 1), n1 = (int)vd.nodes();
   // 1-D taps with out-of-grid entries clamped and weighted 0 (no branches)
@@ -648,7 +648,7 @@ __global__ void k_rq(Dims vd, AuxTab tab, const float* __restrict__ g, const flo
   }
 #pragma unroll
   for (int t = 0; t < kKT; ++t) {
-    const int k = blockIdx.z * kKT + t;
+    const int k = blockIdx.y * kKT + t;
     if (k > vd.nz) break;
     const int n = i + (vd.nx + 1) * (j + (vd.ny + 1) * k);
     float acc[NV];
@@ -687,8 +687,7 @@ __global__ void k_pq(Dims vd, AuxTab tab, const float* __restrict__ g, const flo
                      const float* __restrict__ x1, float* __restrict__ phi, const int* __restrict__ done) {
   if (done && *done) return;
   const Dims qd{vd.nx * P, vd.ny * P, vd.nz * P};
-  const int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y;
-  if (I > qd.nx) return;
+  PLANE_IJ(qd.nx, qd.ny, I, J);
   const int nq = (int)qd.nodes(), n1 = (int)vd.nodes();
   const int sx = vd.nx + 1, sxy = (vd.nx + 1) * (vd.ny + 1);
   const int ex = min(I / P, vd.nx - 1), ey = min(J / P, vd.ny - 1);
@@ -696,7 +695,7 @@ __global__ void k_pq(Dims vd, AuxTab tab, const float* __restrict__ g, const flo
   float acc[kKT][NV], dq[kKT];
 #pragma unroll
   for (int t = 0; t < kKT; ++t) {  // loads of all planes first
-    const int K = min((int)blockIdx.z * kKT + t, qd.nz);
+    const int K = min((int)blockIdx.y * kKT + t, qd.nz);
     const int n = I + (qd.nx + 1) * (J + (qd.ny + 1) * K);
     const int ez = min(K / P, vd.nz - 1);
     const float zi = tab.gll[K - ez * P];
@@ -715,7 +714,7 @@ __global__ void k_pq(Dims vd, AuxTab tab, const float* __restrict__ g, const flo
   }
 #pragma unroll
   for (int t = 0; t < kKT; ++t) {
-    const int K = blockIdx.z * kKT + t;
+    const int K = blockIdx.y * kKT + t;
     if (K > qd.nz) break;
     const int n = I + (qd.nx + 1) * (J + (qd.ny + 1) * K);
 #pragma unroll
