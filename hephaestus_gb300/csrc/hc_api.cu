@@ -871,10 +871,6 @@ hc_status hc_solve_device(hcop_t* h, const hc_solve_params* prm, const double* b
   if (!info) info = &loc;
   std::memset(info, 0, sizeof(*info));
   if (prm->precond == HC_PRECOND_AUX && h->type == HC_TET) {  // one-column block PCG with the tet AMG
-    if (prm->precision == HC_MIXED_RR) {
-      h->err = "hc_solve_device: HC_MIXED_RR is not built for tet AUX solves (use HC_MIXED)";
-      return HC_ENOTSUP;
-    }
     if ((reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(x)) % 16 != 0) {
       h->err = "hc_solve_device: b and x must be 16-byte aligned for tet AUX solves";
       return HC_EINVAL;

@@ -958,7 +958,15 @@ cudaError_t hex_launch_p(const HexDev& d, const T* fac, const T* x, T* y, T ms, 
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nt, sm);
         if (occ < 1) occ = 1;
       }
-      const int grid = std::min(nbricks, occ * nsm);
+      // Persistent grid: occ CTAs per SM, or one fewer when that needs no
+      // more rounds over the bricks -- a last round that fills few slots
+      // costs as much as a full one, and one more resident CTA per SM raises
+      // the brick throughput by only about 10 % (measured at 64^3: 61.7 us
+      // with 3 CTAs per SM, 56.0 us with 4).
+      const auto rounds = [&](int per) { return (nbricks + per * nsm - 1) / (per * nsm); };
+      int per_sm_used = occ;
+      if (occ > 1 && rounds(occ - 1) * (occ - 1) * 1.1 <= rounds(occ) * occ) per_sm_used = occ - 1;
+      const int grid = std::min(nbricks, per_sm_used * nsm);
       kern<<<grid, nt, sm, s>>>(d, fac, x, y, ms, cs, masked, S, partials, nbricks);
     };
     if (d.full) {

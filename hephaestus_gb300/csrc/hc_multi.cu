@@ -12,6 +12,7 @@
 // A converged right-hand side is frozen (alpha = 0, direction zeroed) while the
 // others continue.
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -498,9 +499,18 @@ static hc_status multi_prepare(hcop* h, size_t vec_bytes) {
 }
 
 // Block PCG on J X = B (X: initial guess); wk holds r, p, q (and z with aux): 3 (4) n R of T.
+// Host callback of mpcg_run at each batch boundary (after the scalars were
+// read into hs): go on as hs says, iterate on after the callback changed the
+// iterate and the device scalars (and hs), or stop.
+enum { kMHookGoOn = 0, kMHookResumed = 1, kMHookStop = 2 };
+struct MultiHook {
+  virtual int at_batch(MScalars* hs) = 0;
+  virtual ~MultiHook() = default;
+};
+
 template <typename T>
 static hc_status mpcg_run(hcop* h, int R, double rtol, double atol, int maxit, const T* B, T* X, T* wk,
-                          const T* dinv, bool aux) {
+                          const T* dinv, bool aux, MultiHook* hook) {
   MultiWork* w = mwork(h);
   cudaStream_t s = h->stream;
   const int64_t n = h->ndof;
@@ -541,6 +551,11 @@ static hc_status mpcg_run(hcop* h, int R, double rtol, double atol, int maxit, c
     HC_CUDA_TRY(h, cudaGetLastError());
     HC_CUDA_TRY(h, cudaMemcpyAsync(hs, w->S, sizeof(MScalars), cudaMemcpyDeviceToHost, s));
     HC_CUDA_TRY(h, cudaStreamSynchronize(s));
+    if (hook) {
+      const int a = hook->at_batch(hs);
+      if (a == kMHookStop) break;
+      if (a == kMHookResumed && launched < maxit) continue;
+    }
     if (hs->all_done || launched >= maxit) break;
   }
   return HC_OK;
@@ -567,7 +582,7 @@ hc_status multi_solve_device(hcop* h, const hc_solve_params* prm, int R, const d
     hc_status st = multi_prepare(h, nk * nr * sizeof(double));
     if (st != HC_OK) return st;
     w = mwork(h);
-    st = mpcg_run<double>(h, R, prm->rtol, prm->atol, prm->maxit, B, X, (double*)w->vec, h->dinv, aux);
+    st = mpcg_run<double>(h, R, prm->rtol, prm->atol, prm->maxit, B, X, (double*)w->vec, h->dinv, aux, nullptr);
     if (st != HC_OK) return st;
     hc_status worst = HC_OK;
     for (int k = 0; k < R; ++k) {
@@ -610,7 +625,158 @@ hc_status multi_solve_device(hcop* h, const hc_solve_params* prm, int R, const d
   const int max_outer = prm->max_outer > 0 ? prm->max_outer : 50;
   std::vector<double> rn_prev(R, 0.0);
   bool stalled = false;
-  for (int step = 0;; ++step) {
+  if (prm->precision == HC_MIXED_RR) {
+    // One FP32 block PCG with FP64 residual replacement, per column: the
+    // block form of the single-column solve (van der Vorst & Ye residual
+    // replacement; direction and r.z kept across a replacement).
+    struct BlockReplace : MultiHook {
+      hcop* h;
+      MultiWork* w;
+      int R;
+      int64_t n;
+      unsigned g;
+      double *r64, *X;
+      float *rpcg, *c;
+      double delta2;
+      std::vector<double>*rn, *tol, scale, rr_last, rnp, inv;
+      std::vector<int> stop, slow, *total;
+      std::function<hc_status()> residual;
+      int since = 0, replacements = 0, maxit = 0;
+      bool any_stalled = false;
+      hc_status err = HC_OK;
+      int at_batch(MScalars* hs) override {
+        bool due = hs->all_done != 0;
+        for (int k = 0; k < R; ++k) {
+          if (stop[k]) continue;
+          if (hs->done[k] && hs->status[k] == HC_BREAKDOWN) continue;
+          if (hs->done[k] || hs->rr[k] <= delta2 * rr_last[k]) due = true;
+        }
+        if (!due && ++since < 8) return kMHookGoOn;
+        since = 0;
+        cudaStream_t s = h->stream;
+        // x += scale_k c_k, c = 0, then the FP64 residual of every column
+        for (int k = 0; k < R; ++k) inv[kMaxRhs + k] = scale[k];
+        cudaError_t e = cudaMemcpyAsync(w->col, inv.data(), 2 * kMaxRhs * sizeof(double), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) {
+          k_m_axpy<<<g, kMThreads, 0, s>>>(n, R, c, w->col + kMaxRhs, X);
+          e = cudaMemsetAsync(c, 0, (size_t)n * R * sizeof(float), s);
+        }
+        if (e != cudaSuccess) {
+          h->err = cudaGetErrorString(e);
+          err = HC_ECUDA;
+          return kMHookStop;
+        }
+        std::vector<int> it_now(R), done_now(R), st_now(R);
+        for (int k = 0; k < R; ++k) {
+          it_now[k] = hs->it[k];
+          done_now[k] = hs->done[k];
+          st_now[k] = hs->status[k];
+        }
+        err = residual();  // overwrites hs (= w->hS) with the device scalars and rr, bb
+        if (err != HC_OK) return kMHookStop;
+        ++replacements;
+        bool all = true;
+        for (int k = 0; k < R; ++k) {
+          const double r = (*rn)[k];
+          if (!stop[k]) {
+            (*total)[k] = it_now[k];
+            if (!std::isfinite(r)) {
+              stop[k] = HC_BREAKDOWN + 100;
+            } else if (r <= (*tol)[k]) {
+              stop[k] = HC_OK + 100;
+            } else if (done_now[k] && st_now[k] == HC_BREAKDOWN) {
+              stop[k] = HC_BREAKDOWN + 100;
+            } else if (it_now[k] >= maxit) {
+              stop[k] = HC_NOT_CONVERGED + 100;
+            } else {
+              slow[k] = r > 0.5 * rnp[k] ? slow[k] + 1 : 0;
+              rnp[k] = r;
+              if (slow[k] >= 2) {  // this column's FP32 floor: finish it in FP64
+                stop[k] = HC_NOT_CONVERGED + 100;
+                any_stalled = true;
+              }
+            }
+          }
+          const bool on = !stop[k];
+          inv[k] = on ? 1.0 / scale[k] : 0.0;
+          hs->rr[k] = on ? r * r / (scale[k] * scale[k]) : 0.0;
+          hs->done[k] = on ? 0 : 1;
+          hs->status[k] = on ? HC_NOT_CONVERGED : stop[k] - 100;
+          hs->it[k] = it_now[k];
+          if (on) rr_last[k] = hs->rr[k];
+          all &= !on;
+        }
+        hs->all_done = all ? 1 : 0;
+        if (all) return kMHookStop;
+        // the FP32 recursive residuals := (b - J x) / scale (zero for stopped columns)
+        e = cudaMemcpyAsync(w->col, inv.data(), 2 * kMaxRhs * sizeof(double), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) {
+          k_m_d2f<<<g, kMThreads, 0, s>>>(n, R, r64, w->col, rpcg, c);
+          e = cudaMemcpyAsync(w->S, hs, sizeof(MScalars), cudaMemcpyHostToDevice, s);
+        }
+        if (e != cudaSuccess) {
+          h->err = cudaGetErrorString(e);
+          err = HC_ECUDA;
+          return kMHookStop;
+        }
+        return kMHookResumed;
+      }
+    };
+    BlockReplace hk;
+    hk.h = h;
+    hk.w = w;
+    hk.R = R;
+    hk.n = n;
+    hk.g = g;
+    hk.r64 = r64;
+    hk.X = X;
+    hk.rpcg = wk;  // the block PCG's residual is its first work block
+    hk.c = c;
+    const double delta = prm->inner_rtol > 0 ? std::min(prm->inner_rtol, 0.5) : 0.1;
+    hk.delta2 = delta * delta;
+    hk.rn = &rn;
+    hk.tol = &tol;
+    hk.total = &total;
+    hk.residual = residual;
+    hk.maxit = prm->maxit;
+    hk.scale.assign(R, 1.0);
+    hk.rr_last.assign(R, 1.0);
+    hk.rnp = rn;
+    hk.inv.assign(2 * kMaxRhs, 0.0);
+    hk.stop.assign(R, 0);
+    hk.slow.assign(R, 0);
+    double rin = 1.0;  // the FP32 stopping test, in units of each column's |r0|
+    for (int k = 0; k < R; ++k) {
+      if (!(rn[k] > tol[k]) || !std::isfinite(rn[k])) {
+        hk.stop[k] = (std::isfinite(rn[k]) ? HC_OK : HC_BREAKDOWN) + 100;
+        hk.scale[k] = 1.0;
+        hk.inv[k] = 0.0;
+      } else {
+        hk.scale[k] = rn[k];
+        hk.inv[k] = 1.0 / rn[k];
+        rin = std::min(rin, 0.5 * tol[k] / rn[k]);
+      }
+      hk.inv[kMaxRhs + k] = hk.scale[k];
+    }
+    HC_CUDA_TRY(h, cudaMemcpyAsync(w->col, hk.inv.data(), 2 * kMaxRhs * sizeof(double), cudaMemcpyHostToDevice, s));
+    k_m_d2f<<<g, kMThreads, 0, s>>>(n, R, r64, w->col, rf, c);
+    HC_CUDA_TRY(h, cudaGetLastError());
+    st = mpcg_run<float>(h, R, rin, 0.0, prm->maxit, rf, c, wk, h->dinvf, aux, &hk);
+    if (st != HC_OK) return st;
+    if (hk.err != HC_OK) return hk.err;
+    // the correction since the last replacement (iteration cap) and the final residuals
+    for (int k = 0; k < R; ++k) hk.inv[kMaxRhs + k] = hk.scale[k];
+    HC_CUDA_TRY(h, cudaMemcpyAsync(w->col, hk.inv.data(), 2 * kMaxRhs * sizeof(double), cudaMemcpyHostToDevice, s));
+    k_m_axpy<<<g, kMThreads, 0, s>>>(n, R, c, w->col + kMaxRhs, X);
+    HC_CUDA_TRY(h, cudaGetLastError());
+    for (int k = 0; k < R; ++k)
+      if (!hk.stop[k]) total[k] = w->hS->it[k];
+    st = residual();
+    if (st != HC_OK) return st;
+    for (int k = 0; k < R; ++k) outer[k] = hk.replacements;
+    stalled = hk.any_stalled;
+  }
+  for (int step = 0; prm->precision != HC_MIXED_RR; ++step) {
     bool all = true, any_bad = false;
     for (int k = 0; k < R; ++k) {
       if (!std::isfinite(rn[k])) any_bad = true;
@@ -637,7 +803,7 @@ hc_status multi_solve_device(hcop* h, const hc_solve_params* prm, int R, const d
     HC_CUDA_TRY(h, cudaMemcpyAsync(w->col, inv.data(), 2 * kMaxRhs * sizeof(double), cudaMemcpyHostToDevice, s));
     k_m_d2f<<<g, kMThreads, 0, s>>>(n, R, r64, w->col, rf, c);
     st = mpcg_run<float>(h, R, inner, 0.0, std::min(prm->maxit - used, std::max(100, prm->maxit / 4)), rf, c, wk,
-                         h->dinvf, aux);
+                         h->dinvf, aux, nullptr);
     if (st != HC_OK) return st;
     for (int k = 0; k < R; ++k) total[k] += w->hS->it[k];
     k_m_axpy<<<g, kMThreads, 0, s>>>(n, R, c, w->col + kMaxRhs, X);
@@ -665,7 +831,7 @@ hc_status multi_solve_device(hcop* h, const hc_solve_params* prm, int R, const d
       for (int k = 0; k < R; ++k) used = std::max(used, total[k]);
       if (used >= prm->maxit) break;
       st = mpcg_run<double>(h, R, 0.5 * prm->rtol, 0.5 * prm->atol, std::max(1, prm->maxit - used), B, X, wk64,
-                            h->dinv, aux);
+                            h->dinv, aux, nullptr);
       if (st != HC_OK) return st;
       for (int k = 0; k < R; ++k) {
         total[k] += w->hS->it[k];
@@ -706,8 +872,8 @@ extern "C" hc_status hc_solve_multi_device(hcop_t* h, const hc_solve_params* prm
     h->err = "hc_solve_multi_device: nrhs must be 1, 2, 4, 8, 16 or 32";
     return HC_EINVAL;
   }
-  if (prm->precision != HC_FP64 && prm->precision != HC_MIXED) {
-    h->err = "precision must be HC_FP64 or HC_MIXED";
+  if (prm->precision != HC_FP64 && prm->precision != HC_MIXED && prm->precision != HC_MIXED_RR) {
+    h->err = "precision must be HC_FP64, HC_MIXED or HC_MIXED_RR";
     return HC_EINVAL;
   }
   if ((reinterpret_cast<uintptr_t>(B) | reinterpret_cast<uintptr_t>(X)) % 16 != 0) {

@@ -69,8 +69,8 @@ enum {
   HC_MIXED_RR = 4 /* one FP32 PCG (COCG for complex solves) whose recursive
                     residual is replaced by the FP64 residual b - J x (and
                     its correction added to the FP64 x) each time it fell
-                    by inner_rtol; single right-hand-side solves
-                    (hc_solve*, hc_solve_complex*: complex ones run the
+                    by inner_rtol (per column in block solves); real,
+                    block and complex solves (complex ones run the
                     graph-driven solve)                                    */
 };
 

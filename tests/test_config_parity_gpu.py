@@ -198,7 +198,7 @@ def _tets(n, nrhs, seed=0):
     return op, ref, np.ascontiguousarray(B)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_rr"])
 def test_tets8_16rhs_block_solve_matches_oracle_direct(precision):
     import torch
 

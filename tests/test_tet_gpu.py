@@ -121,7 +121,7 @@ def test_tet_solve_matches_oracle(prec):
     assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-9
 
 
-@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed_rr"])
 @pytest.mark.parametrize("nrhs", [1, 4, 16])
 def test_tet_multi_rhs_solve_matches_oracle(prec, nrhs):
     """Block PCG over nrhs columns = the oracle's PCG column by column.  The

@@ -70,7 +70,7 @@ def test_gradient_is_curl_free(p):
 
 
 @pytest.mark.parametrize("p", [1, 2])
-@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed_rr"])
 def test_aux_block_solve_matches_oracle(p, prec):
     import torch
 
