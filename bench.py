@@ -952,7 +952,10 @@ def tet_solves(args, op, nrhs):
     # residual near 1e-14: the ladder goes that far (FP64 PCG's true residual
     # stalls above it; the refinement of the mixed solver does not)
     ladder = [t for t in RTOL_LADDER + (2e-14, 1e-14) if t <= args.tet_rtol] or [args.tet_rtol]
-    for prec in ("fp64", "mixed", "mixed_rr"):
+    # (residual replacement -- "mixed_rr" -- is left out here: on this operator
+    # the FP32 block PCG without restarts needs ~2,000 iterations, 6x slower
+    # than refinement; the hex line times it)
+    for prec in ("fp64", "mixed"):
         def once(tol):
             X.zero_()
             return solver(prec, tol).MultMultiDevice(B, X)
@@ -1072,9 +1075,6 @@ def tet_solves(args, op, nrhs):
     out["mixed_within_fp64_reproducibility"] = bool(out["mixed"]["rel_err_vs_fp64_truth_max"] <=
                                                     max(XERR_BAR, 2.0 * floor))
     out["speedup_credited"] = bool(out["fp64"]["meets_1e-10"] and out["mixed"]["meets_1e-10"])
-    out["speedup_mixed_rr_over_fp64"] = out["mixed_rr"]["solves_per_s"] / out["fp64"]["solves_per_s"]
-    out["mixed_rr_as_accurate_as_fp64"] = bool(out["mixed_rr"]["rel_err_vs_fp64_truth_max"] <=
-                                               max(out["fp64"]["rel_err_vs_fp64_truth_max"], XERR_BAR))
     out["speedup_mixed_over_fp64_refined"] = out["mixed"]["solves_per_s"] / out["fp64_refined"]["solves_per_s"]
     out["speedup_over_fp64_refined_credited"] = bool(out["fp64_refined"]["meets_1e-10"] and
                                                      out["mixed"]["meets_1e-10"])
