@@ -17,7 +17,7 @@ HC_OK, HC_EINVAL, HC_ENOMEM, HC_ECUDA, HC_NOT_CONVERGED, HC_BREAKDOWN, HC_TIMEOU
 STATUS_NAMES = ["OK", "EINVAL", "ENOMEM", "ECUDA", "NOT_CONVERGED", "BREAKDOWN", "TIMEOUT", "ENOTSUP"]
 HC_HEX, HC_TET = 0, 1
 HC_FP64, HC_FP32, HC_MIXED, HC_BF16, HC_MIXED_RR = 0, 1, 2, 3, 4
-HC_PRECOND_NONE, HC_PRECOND_JACOBI, HC_PRECOND_CHEBYSHEV, HC_PRECOND_AUX = 0, 1, 2, 3
+HC_PRECOND_NONE, HC_PRECOND_JACOBI, HC_PRECOND_CHEBYSHEV, HC_PRECOND_AUX, HC_PRECOND_AUX_MULT = 0, 1, 2, 3, 4
 HC_FIELD_ELEM, HC_FIELD_QUAD = 0, 1
 
 

@@ -819,13 +819,17 @@ static hc_status check_params(hcop* h, const hc_solve_params* p) {
     h->err = "precision must be HC_FP64, HC_MIXED or HC_MIXED_RR";
     return HC_EINVAL;
   }
-  if (p->precond < HC_PRECOND_NONE || p->precond > HC_PRECOND_AUX) {
+  if (p->precond < HC_PRECOND_NONE || p->precond > HC_PRECOND_AUX_MULT) {
     h->err = "unknown preconditioner";
     return HC_EINVAL;
   }
   if (p->precond == HC_PRECOND_CHEBYSHEV && p->cheb_degree < 1) {
     h->err = "cheb_degree must be >= 1";
     return HC_EINVAL;
+  }
+  if (p->precond == HC_PRECOND_AUX_MULT && h->type != HC_HEX) {
+    h->err = "HC_PRECOND_AUX_MULT is built for hex handles";
+    return HC_ENOTSUP;
   }
   if (!(p->rtol >= 0.0) || !(p->atol >= 0.0) || p->maxit < 1) {
     h->err = "rtol, atol must be >= 0 and maxit >= 1";
@@ -877,7 +881,7 @@ hc_status hc_solve_device(hcop_t* h, const hc_solve_params* prm, const double* b
     }
     return multi_solve_device(h, prm, 1, b, x, info);
   }
-  if (prm->precond == HC_PRECOND_AUX) {
+  if (prm->precond == HC_PRECOND_AUX || prm->precond == HC_PRECOND_AUX_MULT) {
     st = auxmg_setup(h);
     if (st != HC_OK) return st;
   }
@@ -885,13 +889,13 @@ hc_status hc_solve_device(hcop_t* h, const hc_solve_params* prm, const double* b
   if (prm->precision == HC_MIXED_RR) return mixed_rr_device(h, prm, b, x, info);
   SolveCfg cfg;
   cfg.precond = prm->precond;
-  cfg.cheb_degree = prm->cheb_degree;
+  cfg.cheb_degree = prm->cheb_degree > 0 ? prm->cheb_degree : 2;
   cfg.cheb_ratio = prm->cheb_ratio > 0 ? prm->cheb_ratio : 30.0;
   cfg.rtol = prm->rtol;
   cfg.atol = prm->atol;
   cfg.maxit = prm->maxit;
   cfg.lmax = prm->cheb_lmax;
-  if (cfg.precond == HC_PRECOND_CHEBYSHEV && cfg.lmax <= 0) {
+  if ((cfg.precond == HC_PRECOND_CHEBYSHEV || cfg.precond == HC_PRECOND_AUX_MULT) && cfg.lmax <= 0) {
     if (h->lmax64 <= 0) {
       double lm = 0;
       st = lanczos_device<double>(h, 20, &lm);

@@ -265,6 +265,11 @@ struct OpJ {
   cudaError_t apply(const T* x, T* y, KrylovScalars* S, double* partials, cudaStream_t s,
                     bool y_zero_free = true) const;
 };
+// Weight c of the gradient-space correction in HC_PRECOND_AUX_MULT.  The
+// correction V only approximates (G^T J G)^-1 (an additive two-level V-cycle
+// that can overshoot up to twice); damping it keeps the multiplicative cycle
+// a contraction.
+constexpr float kAuxMultWeight = 0.5f;
 struct SolveCfg {
   int precond;
   int cheb_degree;

@@ -497,6 +497,29 @@ __global__ void k_chebk(int64_t n, const T* __restrict__ r, const T* __restrict_
   }
 }
 
+// Multiplicative auxiliary-space preconditioner (HC_PRECOND_AUX_MULT):
+// t = r - J z after the pre-smoothing
+template <typename T>
+__global__ void k_amul_t(int64_t n, const T* __restrict__ r, const T* __restrict__ w, T* __restrict__ t,
+                         const KrylovScalars* S) {
+  if (S->done) return;
+  GS_LOOP(i, n) t[i] = r[i] - w[i];
+}
+// first post-smoothing step from z != 0 (w = J z): d = D^-1 (r - w) / theta
+template <typename T>
+__global__ void k_cheb0r(int64_t n, const T* __restrict__ r, const T* __restrict__ dinv, T* __restrict__ z,
+                         T* __restrict__ dk, T* __restrict__ w, const uint8_t* __restrict__ ess, T inv_theta,
+                         int init_next, const KrylovScalars* S) {
+  if (S->done) return;
+  GS_LOOP(i, n) {
+    const T d = dinv[i] * (r[i] - w[i]) * inv_theta;
+    dk[i] = d;
+    const T zi = z[i] + d;
+    z[i] = zi;
+    if (init_next) w[i] = ess[i] ? zi : T(0);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Lanczos kernels on D^-1/2 J D^-1/2
 // ---------------------------------------------------------------------------
@@ -768,10 +791,11 @@ static hc_status pcg_run(hcop* h, const SolveCfg& cfg, const T* b, T* x, T* wk, 
   const bool jac = cfg.precond == HC_PRECOND_JACOBI || cfg.precond == HC_PRECOND_NONE;
   const bool none = cfg.precond == HC_PRECOND_NONE;
   const bool aux = cfg.precond == HC_PRECOND_AUX;
-  // z = C(r) for the Chebyshev preconditioner
+  const bool amult = cfg.precond == HC_PRECOND_AUX_MULT;
+  // z = C(r) for the Chebyshev preconditioner (and the smoother of AUX_MULT)
   double theta = 0, delta = 0, sigma1 = 0;
   std::vector<double> c1s, c2s;
-  if (cfg.precond == HC_PRECOND_CHEBYSHEV) {
+  if (cfg.precond == HC_PRECOND_CHEBYSHEV || amult) {
     const double lmin = cfg.lmax / cfg.cheb_ratio;
     theta = 0.5 * (cfg.lmax + lmin);
     delta = 0.5 * (cfg.lmax - lmin);
@@ -784,17 +808,40 @@ static hc_status pcg_run(hcop* h, const SolveCfg& cfg, const T* b, T* x, T* wk, 
       rho = rn;
     }
   }
-  auto cheb = [&]() -> cudaError_t {
-    k_cheb0<T><<<g, kRedThreads, 0, s>>>(n, r, dinv, z, dk, w, h->ess, (T)(1.0 / theta), S);
+  // Chebyshev steps 1.. of z toward J z = r; w = (I - P) z on entry.  The
+  // last step leaves w = (I - P) z too when init_last (the next apply's start).
+  auto cheb_steps = [&](bool init_last) -> cudaError_t {
     for (int k = 1; k < cfg.cheb_degree; ++k) {
       cudaError_t e = op.apply(z, w, nullptr, nullptr, s);
       if (e != cudaSuccess) return e;
       ++napply;
-      const int init_next = (k + 1 < cfg.cheb_degree) ? 1 : 0;
+      const int init_next = (k + 1 < cfg.cheb_degree || init_last) ? 1 : 0;
       k_chebk<T><<<g, kRedThreads, 0, s>>>(n, r, dinv, z, dk, w, h->ess, (T)c1s[k - 1], (T)c2s[k - 1],
                                            init_next, S);
     }
     return cudaGetLastError();
+  };
+  auto cheb = [&](bool init_last) -> cudaError_t {
+    k_cheb0<T><<<g, kRedThreads, 0, s>>>(n, r, dinv, z, dk, w, h->ess, (T)(1.0 / theta), S);
+    return cheb_steps(init_last);
+  };
+  // AUX_MULT: z = S r; z += c G V G^T (r - J z); z += S (r - J z) with S the
+  // Chebyshev-Jacobi polynomial: a symmetric multiplicative (smoother,
+  // gradient-space correction, smoother) cycle, as AMS cycles are.
+  auto aux_mult = [&]() -> cudaError_t {
+    cudaError_t e = cheb(true);
+    if (e != cudaSuccess) return e;
+    if ((e = op.apply(z, w, nullptr, nullptr, s)) != cudaSuccess) return e;
+    ++napply;
+    k_amul_t<T><<<g, kRedThreads, 0, s>>>(n, r, w, dk, S);
+    const float coef[4] = {kAuxMultWeight, 0.0f, 0.0f, 0.0f};
+    if ((e = auxmg_apply<T, 1>(h, dk, nullptr, z, nullptr, coef, &S->done, s)) != cudaSuccess) return e;
+    if ((e = init_masked<T>(n, h->ess, z, w, s)) != cudaSuccess) return e;
+    if ((e = op.apply(z, w, nullptr, nullptr, s)) != cudaSuccess) return e;
+    ++napply;
+    k_cheb0r<T><<<g, kRedThreads, 0, s>>>(n, r, dinv, z, dk, w, h->ess, (T)(1.0 / theta),
+                                          cfg.cheb_degree > 1 ? 1 : 0, S);
+    return cheb_steps(false);
   };
   // z = B r for the non-Jacobi preconditioners
   auto precond = [&](bool z_ready) -> cudaError_t {
@@ -803,7 +850,8 @@ static hc_status pcg_run(hcop* h, const SolveCfg& cfg, const T* b, T* x, T* wk, 
       const float coef[4] = {1.0f, 0.0f, 0.0f, 0.0f};
       return auxmg_apply<T, 1>(h, r, nullptr, z, nullptr, coef, &S->done, s);
     }
-    return cheb();
+    if (amult) return aux_mult();
+    return cheb(false);
   };
 
   // r = b - J x
@@ -902,7 +950,7 @@ static hc_status inner_cfg(hcop* h, const hc_solve_params* prm, double rtol, flo
   in->rtol = rtol;
   in->atol = 0.0;
   in->lmax = prm->cheb_lmax;
-  if (in->precond == HC_PRECOND_CHEBYSHEV && in->lmax <= 0) {
+  if ((in->precond == HC_PRECOND_CHEBYSHEV || in->precond == HC_PRECOND_AUX_MULT) && in->lmax <= 0) {
     if (h->lmax32 <= 0) {
       double lm = 0;
       const hc_status st = lanczos_device<float>(h, 20, &lm, wk);
@@ -932,7 +980,7 @@ static hc_status polish64(hcop* h, const hc_solve_params* prm, const SolveCfg& i
   c64.cheb_degree = in.cheb_degree;
   c64.cheb_ratio = in.cheb_ratio;
   c64.lmax = prm->cheb_lmax;
-  if (c64.precond == HC_PRECOND_CHEBYSHEV && c64.lmax <= 0) {
+  if ((c64.precond == HC_PRECOND_CHEBYSHEV || c64.precond == HC_PRECOND_AUX_MULT) && c64.lmax <= 0) {
     if (h->lmax64 <= 0) {
       double lm = 0;
       st = lanczos_device<double>(h, 20, &lm, wk64);

@@ -437,7 +437,7 @@ class HCurlOperator:
 
 
 _PRECOND = {"none": N.HC_PRECOND_NONE, "jacobi": N.HC_PRECOND_JACOBI, "chebyshev": N.HC_PRECOND_CHEBYSHEV,
-            "aux": N.HC_PRECOND_AUX}
+            "aux": N.HC_PRECOND_AUX, "aux_mult": N.HC_PRECOND_AUX_MULT}
 _PREC = {"fp64": N.HC_FP64, "mixed": N.HC_MIXED, "mixed_rr": N.HC_MIXED_RR}
 
 

@@ -77,8 +77,14 @@ enum {
 /* HC_PRECOND_AUX: Jacobi plus the auxiliary-space gradient correction
  * G V G^T (V one multigrid V-cycle for G^T M_sigma G on the H1 nodes), the
  * gradient part of the AMS preconditioner the reference uses
- * (hcurl_formulation.cpp:69-79).  Structured hex grids with sigma.        */
-enum { HC_PRECOND_NONE = 0, HC_PRECOND_JACOBI = 1, HC_PRECOND_CHEBYSHEV = 2, HC_PRECOND_AUX = 3 };
+ * (hcurl_formulation.cpp:69-79).  Structured hex grids with sigma.
+ * HC_PRECOND_AUX_MULT (hex handles, real solves): the same correction in a
+ * symmetric multiplicative cycle, z = S r; z += c G V G^T (r - J z);
+ * z += S (r - J z), S the Chebyshev-Jacobi polynomial of degree cheb_degree
+ * (<= 0 -> 2) on [lmax/cheb_ratio, lmax], c = 1/2: 2 cheb_degree operator
+ * applications per iteration, several times fewer iterations.           */
+enum { HC_PRECOND_NONE = 0, HC_PRECOND_JACOBI = 1, HC_PRECOND_CHEBYSHEV = 2, HC_PRECOND_AUX = 3,
+       HC_PRECOND_AUX_MULT = 4 };
 
 typedef struct {
   int32_t elem_type;        /* HC_HEX (structured grid) or HC_TET                 */
@@ -108,7 +114,8 @@ typedef struct {
 typedef struct {
   int32_t precision;        /* HC_FP64 | HC_FP32 | HC_MIXED                        */
   int32_t precond;          /* HC_PRECOND_*                                        */
-  int32_t cheb_degree;      /* polynomial degree (>= 1) for HC_PRECOND_CHEBYSHEV   */
+  int32_t cheb_degree;      /* polynomial degree (>= 1) for HC_PRECOND_CHEBYSHEV,
+                               smoother degree of HC_PRECOND_AUX_MULT (<= 0 -> 2) */
   double cheb_ratio;        /* interval [lmax/ratio, lmax]; <= 0 -> 30              */
   double cheb_lmax;         /* upper eigenvalue bound of D^-1 J; <= 0 -> estimate  */
   double rtol, atol;        /* stop when ||b - J x|| <= max(rtol ||b||, atol)      */
