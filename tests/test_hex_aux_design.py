@@ -1,0 +1,192 @@
+"""CPU check of the design of the hex auxiliary-space preconditioners on the
+oracle's matrices (8^3 hexes, Nedelec p = 2, the benchmark's coefficient
+draws nu = 10^U(0,3), sigma = 10^U(-2,6), dt = 0.01, coil load).
+
+The reference preconditions with HypreAMS (hcurl_formulation.cpp:69-79):
+smoothing plus corrections in the gradient space (G: H1 -> ND) and in the
+vector-potential space (Pi: (H1)^3 -> ND).  The library builds the gradient
+part (HC_PRECOND_AUX, additive; HC_PRECOND_AUX_MULT, multiplicative with
+Chebyshev-Jacobi smoothing).  This test records, with exact auxiliary solves
+where stated, why:
+
+* G and Pi are exact: curl G phi = 0, and Pi of a constant field is curl-free;
+* with the exact (G^T J G)^-1, adding the Pi correction with an exact
+  (Pi^T J Pi)^-1 on the order-p Gauss-Lobatto nodes cuts the iterations
+  about threefold -- but the cheap forms of it a GPU cycle could afford
+  (Pi through the Q1 vertex fields with an exact Galerkin solve; the diagonal
+  of Pi^T J Pi plus that Q1 correction) gain little: the order-p part of
+  Pi^T J Pi needs a solver as costly as the outer iteration;
+* the multiplicative cycle smoother - c G V G^T - smoother with the library's
+  structure of V (Jacobi on the Gauss-Lobatto nodes plus a Q1 correction,
+  here with an exact Q1 solve) and c = 1/2 cuts the iterations of the
+  additive form about threefold.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from hephaestus_gb300 import meshes
+from tests import hexref as H
+from tests import oracle_ref as R
+
+sp = pytest.importorskip("scipy.sparse")
+spl = pytest.importorskip("scipy.sparse.linalg")
+
+N, P, DT = 8, 2, 0.01
+
+
+@pytest.fixture(scope="module")
+def setup():
+    rng = np.random.default_rng(0)
+    ne = N ** 3
+    nu, sigma = meshes.loguniform(ne, 1.0, 1e3, rng), meshes.loguniform(ne, 1e-2, 1e6, rng)
+    ref = oracle.Problem.hex(N, N, N, P)
+    ref.set_coef(DT * nu, sigma)
+    ref.assemble()
+    mask = ref.hex_ess_mask(0x3F)
+    ref.set_ess(mask)
+    J = R.eliminated(ref).tocsr()
+    b = ref.load_coil(q=P + 2)
+    b[mask != 0] = 0.0
+    m = N * P
+    gc, go = H.gll_nodes(P + 1), H.gl_nodes(P)
+
+    def per_element(T):
+        A = sp.lil_matrix((m, m + 1))
+        for e in range(N):
+            A[e * P:(e + 1) * P, e * P:e * P + P + 1] = T
+        return A.tocsr()
+
+    I1 = sp.identity(m + 1, format="csr")
+
+    def along(T, c):  # T along direction c of an (m+1)^3 node field, [k, j, i] order
+        return [sp.kron(I1, sp.kron(I1, T)), sp.kron(I1, sp.kron(T, I1)), sp.kron(T, sp.kron(I1, I1))][c]
+
+    Dm = per_element(H.lagrange_deriv_matrix(gc, go))
+    Em = per_element(H.lagrange_values(gc, go))
+    G = sp.vstack([along(Dm, c) for c in range(3)]).tocsr()
+    nq = (m + 1) ** 3
+    h = 1.0 / N
+    Pi = sp.hstack([sp.vstack([along(Em, c) * h if c == d else sp.csr_matrix((along(Em, c).shape[0], nq))
+                               for c in range(3)]) for d in range(3)]).tocsr()
+    free = sp.diags((mask == 0).astype(float))
+    idx = np.indices((m + 1,) * 3).reshape(3, -1)
+    bnd = np.any((idx == 0) | (idx == m), axis=0)
+    # trilinear interpolation from the (N+1)^3 vertices to the Gauss-Lobatto nodes
+    w = np.zeros((m + 1, N + 1))
+    for e in range(N):
+        for a in range(P + 1):
+            w[e * P + a, e], w[e * P + a, e + 1] = 1 - gc[a], gc[a]
+    w = sp.csr_matrix(w)
+    P0 = sp.kron(w, sp.kron(w, w)).tocsr()
+    vidx = np.indices((N + 1,) * 3).reshape(3, -1)
+    vbnd = np.any((vidx == 0) | (vidx == N), axis=0)
+    return dict(ref=ref, J=J, b=b, G=free @ G, Pi=free @ Pi, Graw=G, Piraw=Pi, bnd=bnd, P0=P0, vbnd=vbnd)
+
+
+def _solver(A, fixed):
+    keep = np.where(~fixed)[0]
+    lu = spl.splu(A[keep][:, keep].tocsc())
+
+    def solve(r):
+        z = np.zeros(A.shape[0])
+        z[keep] = lu.solve(r[keep])
+        return z
+    return solve
+
+
+def _pcg(J, b, M, rtol=1e-10, maxit=1000):
+    x = np.zeros_like(b)
+    r = b.copy()
+    z = M(r)
+    d = z.copy()
+    rz = r @ z
+    nb = np.linalg.norm(b)
+    for it in range(1, maxit + 1):
+        q = J @ d
+        a = rz / (d @ q)
+        x += a * d
+        r -= a * q
+        if np.linalg.norm(r) <= rtol * nb:
+            return it
+        z = M(r)
+        rz2 = r @ z
+        d = z + rz2 / rz * d
+        rz = rz2
+    return maxit
+
+
+def _cheb(J, dinv, lmax, r, x, deg=2, ratio=30.0):
+    """Chebyshev-Jacobi iteration on J x = r from x (Saad, Alg. 12.1)."""
+    lo = lmax / ratio
+    th, de = 0.5 * (lmax + lo), 0.5 * (lmax - lo)
+    rho = de / th
+    d = dinv * (r - J @ x) / th
+    x = x + d
+    for _ in range(1, deg):
+        rho2 = 1.0 / (2.0 * th / de - rho)
+        d = rho2 * rho * d + 2.0 * rho2 / de * (dinv * (r - J @ x))
+        x = x + d
+        rho = rho2
+    return x
+
+
+def test_gradient_and_pi_are_exact(setup):
+    s = setup
+    rng = np.random.default_rng(1)
+    phi = rng.standard_normal(s["Graw"].shape[1])
+    g = s["Graw"] @ phi
+    assert np.linalg.norm(s["ref"].apply_curlcurl(g)) <= 1e-12 * np.linalg.norm(s["ref"].apply(g))
+    nq = s["Graw"].shape[1]
+    for d in range(3):
+        c = np.zeros(3 * nq)
+        c[d * nq:(d + 1) * nq] = 1.0
+        v = s["Piraw"] @ c
+        assert np.linalg.norm(s["ref"].apply_curlcurl(v)) <= 1e-12 * np.linalg.norm(s["ref"].apply(v))
+
+
+def test_pi_part_pays_only_with_an_order_p_solve(setup):
+    s = setup
+    J, b, G, Pi = s["J"], s["b"], s["G"], s["Pi"]
+    dinv = 1.0 / J.diagonal()
+    sG = _solver((G.T @ J @ G).tocsr(), s["bnd"])
+    AP = (Pi.T @ J @ Pi).tocsr()
+    fixed3 = np.concatenate([s["bnd"]] * 3)
+    sP = _solver(AP, fixed3)
+    P03 = sp.block_diag([s["P0"]] * 3).tocsr()
+    Pi1 = Pi @ P03
+    sP1 = _solver((Pi1.T @ J @ Pi1).tocsr(), np.concatenate([s["vbnd"]] * 3))
+    dP = AP.diagonal()
+    dPinv = np.where(fixed3 | (dP == 0), 0.0, 1.0 / np.where(dP == 0, 1.0, dP))
+
+    base = _pcg(J, b, lambda r: dinv * r + G @ sG(G.T @ r))
+    exact = _pcg(J, b, lambda r: dinv * r + G @ sG(G.T @ r) + Pi @ sP(Pi.T @ r))
+    q1 = _pcg(J, b, lambda r: dinv * r + G @ sG(G.T @ r) + Pi1 @ sP1(Pi1.T @ r))
+    diag_q1 = _pcg(J, b, lambda r: dinv * r + G @ sG(G.T @ r) + Pi @ (dPinv * (Pi.T @ r)) + Pi1 @ sP1(Pi1.T @ r))
+    assert exact * 2.5 < base, (base, exact)
+    assert q1 > 0.8 * base and diag_q1 > 0.8 * base, (base, q1, diag_q1)
+
+
+def test_multiplicative_cycle_cuts_iterations(setup):
+    s = setup
+    J, b, G = s["J"], s["b"], s["G"]
+    dinv = 1.0 / J.diagonal()
+    AG = (G.T @ J @ G).tocsr()
+    dG = AG.diagonal()
+    dGinv = np.where(s["bnd"] | (dG == 0), 0.0, 1.0 / np.where(dG == 0, 1.0, dG))
+    P0 = s["P0"]
+    s1 = _solver((P0.T @ AG @ P0).tocsr(), s["vbnd"])
+
+    def V(y):  # the library's structure: Gauss-Lobatto Jacobi + Q1 correction
+        return dGinv * y + P0 @ s1(P0.T @ y)
+
+    lmax = 1.1 * abs(spl.eigs(sp.diags(dinv) @ J, k=1, which="LM", return_eigenvectors=False)[0])
+
+    def mult(r):
+        z = _cheb(J, dinv, lmax, r, np.zeros_like(r))
+        z = z + 0.5 * (G @ V(G.T @ (r - J @ z)))
+        return _cheb(J, dinv, lmax, r, z)
+
+    additive = _pcg(J, b, lambda r: dinv * r + G @ V(G.T @ r))
+    multiplicative = _pcg(J, b, mult)
+    assert multiplicative * 2.5 < additive, (additive, multiplicative)
