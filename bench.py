@@ -1112,6 +1112,8 @@ def run_profile_case(argv):
       fp64     y = J x in FP64, 3 times
       solve    one mixed-precision PCG solve of the coil load (auxiliary-space
                preconditioner), capped at 8 inner iterations and 1 refinement step
+      solvemult one FP32 PCG with FP64 residual replacement and the multiplicative
+               auxiliary-space cycle (HC_PRECOND_AUX_MULT), capped at 8 iterations
       precond  z = B r with the auxiliary-space preconditioner (FP64 r, z), 4 times
       complex  y = (C + i omega M) x in FP32 (fused complex kernel), 5 times
       tets     16-RHS FP32 apply on the tet mesh, 3 times
@@ -1158,13 +1160,15 @@ def run_profile_case(argv):
     nu = meshes.loguniform(n ** 3, 1, 1e3, rng)
     sg = meshes.loguniform(n ** 3, 1e-2, 1e6, rng)
     op = HCurlOperator(n, n, n, p, nu, sg, dt=0.01)
-    if mode == "solve":
+    if mode in ("solve", "solvemult"):
         from hephaestus_gb300 import GpuHCurlPCGSolver
 
         b = torch.tensor(np.where(op.ess_mask() != 0, 0.0, op.LoadCoil()), device="cuda")
         x = torch.zeros_like(b)
-        s = GpuHCurlPCGSolver({"Tolerance": 1e-10, "MaxIter": 8, "MaxOuter": 1, "Precision": "mixed",
-                               "Preconditioner": "aux"}, op)
+        prm = {"Tolerance": 1e-10, "MaxIter": 8, "MaxOuter": 1, "Precision": "mixed", "Preconditioner": "aux"}
+        if mode == "solvemult":  # one FP32 PCG (residual replacement) with the multiplicative cycle
+            prm.update(Precision="mixed_rr", Preconditioner="aux_mult")
+        s = GpuHCurlPCGSolver(prm, op)
         s.MultDevice(b, x)
     elif mode == "precond":
         r = torch.randn(op.ndof, dtype=torch.float64, device="cuda")
