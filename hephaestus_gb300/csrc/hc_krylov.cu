@@ -469,55 +469,120 @@ __global__ void k_jz(int64_t n, const T* __restrict__ r, const T* __restrict__ d
 }
 
 // Chebyshev iteration (Saad, Iterative Methods for Sparse Linear Systems,
-// Alg. 12.1) on D^-1 J z = D^-1 r, zero start, fixed degree: a fixed SPD
-// polynomial preconditioner when lmax bounds the spectrum of D^-1 J.
+// Alg. 12.1) on D^-1 J z = D^-1 r with a fixed degree: a fixed SPD
+// polynomial preconditioner when lmax bounds the spectrum of D^-1 J (and the
+// smoother of HC_PRECOND_AUX_MULT).  One step:
+//     d = c1 d_prev + c2 D^-1 (r - w),  z += d     (w = J z on entry)
+// flags: kCbZ0   z = 0 on entry (first step: r - w = r, z = d, w unread)
+//        kCbDkZ  d_prev = z (the step after a first step from z = 0)
+//        kCbDk   d_prev = dk (read)            kCbStoreDk  dk = d
+//        kCbInitW w = (I - P) z afterwards (the next operator apply's start)
+// VEC: 16-byte loads and stores (every vector 16-byte aligned, ess aligned
+// to the chunk width), with a scalar tail.
+enum { kCbZ0 = 1, kCbDkZ = 2, kCbDk = 4, kCbStoreDk = 8, kCbInitW = 16 };
 template <typename T>
-__global__ void k_cheb0(int64_t n, const T* __restrict__ r, const T* __restrict__ dinv, T* __restrict__ z,
-                        T* __restrict__ dk, T* __restrict__ w, const uint8_t* __restrict__ ess, T inv_theta,
-                        const KrylovScalars* S) {
-  if (S->done) return;
-  GS_LOOP(i, n) {
-    const T zi = r[i] * dinv[i] * inv_theta;
-    z[i] = zi;
-    dk[i] = zi;
-    w[i] = ess[i] ? zi : T(0);
-  }
+__device__ __forceinline__ void cheb_elem(T& zi, T& wi, T& di, T ri, T dvi, T dki, bool e, T c1, T c2, int f) {
+  const T res = (f & kCbZ0) ? ri : ri - wi;
+  const T prev = (f & kCbDkZ) ? zi : ((f & kCbDk) ? dki : T(0));
+  di = c1 * prev + c2 * dvi * res;
+  zi = (f & kCbZ0) ? di : zi + di;
+  if (f & kCbInitW) wi = e ? zi : T(0);
 }
-template <typename T>
-__global__ void k_chebk(int64_t n, const T* __restrict__ r, const T* __restrict__ dinv, T* __restrict__ z,
-                        T* __restrict__ dk, T* __restrict__ w, const uint8_t* __restrict__ ess, T c1, T c2,
-                        int init_next, const KrylovScalars* S) {
+template <typename T, bool VEC>
+__global__ void __launch_bounds__(kRedThreads)
+    k_cheb_step(int64_t n, const T* __restrict__ r, const T* __restrict__ dinv, T* __restrict__ z,
+                T* __restrict__ dk, T* __restrict__ w, const uint8_t* __restrict__ ess, T c1, T c2, int f,
+                const KrylovScalars* S) {
   if (S->done) return;
-  GS_LOOP(i, n) {
-    const T d = c1 * dk[i] + c2 * dinv[i] * (r[i] - w[i]);
-    dk[i] = d;
-    const T zi = z[i] + d;
+  constexpr int W = Chunk16<T>::W;
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, st = (int64_t)gridDim.x * blockDim.x;
+  const int64_t nc = VEC ? n / W : 0;
+  if (VEC) {
+#pragma unroll 2
+    for (int64_t c = t0; c < nc; c += st) {
+      Chunk16<T> rv, dv, zv, wv, kv, ov;
+      rv.load(r, c);
+      dv.load(dinv, c);
+      if (!(f & kCbZ0)) {
+        zv.load(z, c);
+        wv.load(w, c);
+      }
+      if (f & kCbDk) kv.load(dk, c);
+      uint8_t m[W];
+      if constexpr (W == 4) {
+        const uchar4 e4 = reinterpret_cast<const uchar4*>(ess)[c];
+        m[0] = e4.x, m[1] = e4.y, m[2] = e4.z, m[3] = e4.w;
+      } else {
+        const uchar2 e2 = reinterpret_cast<const uchar2*>(ess)[c];
+        m[0] = e2.x, m[1] = e2.y;
+      }
+#pragma unroll
+      for (int q = 0; q < W; ++q)
+        cheb_elem<T>(zv.v[q], wv.v[q], ov.v[q], rv.v[q], dv.v[q], kv.v[q], m[q] != 0, c1, c2, f);
+      zv.store(z, c);
+      if (f & kCbStoreDk) ov.store(dk, c);
+      if (f & kCbInitW) wv.store(w, c);
+    }
+  }
+  for (int64_t i = nc * W + t0; i < n; i += st) {
+    T zi = (f & kCbZ0) ? T(0) : z[i], wi = (f & kCbZ0) ? T(0) : w[i], di;
+    cheb_elem<T>(zi, wi, di, r[i], dinv[i], (f & kCbDk) ? dk[i] : T(0), ess[i] != 0, c1, c2, f);
     z[i] = zi;
-    if (init_next) w[i] = ess[i] ? zi : T(0);
+    if (f & kCbStoreDk) dk[i] = di;
+    if (f & kCbInitW) w[i] = wi;
   }
 }
 
-// Multiplicative auxiliary-space preconditioner (HC_PRECOND_AUX_MULT):
-// t = r - J z after the pre-smoothing
-template <typename T>
-__global__ void k_amul_t(int64_t n, const T* __restrict__ r, const T* __restrict__ w, T* __restrict__ t,
-                         const KrylovScalars* S) {
+// HC_PRECOND_AUX_MULT: t = r - w (w = J z after the pre-smoothing)
+template <typename T, bool VEC>
+__global__ void __launch_bounds__(kRedThreads)
+    k_amul_t(int64_t n, const T* __restrict__ r, const T* __restrict__ w, T* __restrict__ t,
+             const KrylovScalars* S) {
   if (S->done) return;
-  GS_LOOP(i, n) t[i] = r[i] - w[i];
-}
-// first post-smoothing step from z != 0 (w = J z): d = D^-1 (r - w) / theta
-template <typename T>
-__global__ void k_cheb0r(int64_t n, const T* __restrict__ r, const T* __restrict__ dinv, T* __restrict__ z,
-                         T* __restrict__ dk, T* __restrict__ w, const uint8_t* __restrict__ ess, T inv_theta,
-                         int init_next, const KrylovScalars* S) {
-  if (S->done) return;
-  GS_LOOP(i, n) {
-    const T d = dinv[i] * (r[i] - w[i]) * inv_theta;
-    dk[i] = d;
-    const T zi = z[i] + d;
-    z[i] = zi;
-    if (init_next) w[i] = ess[i] ? zi : T(0);
+  constexpr int W = Chunk16<T>::W;
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, st = (int64_t)gridDim.x * blockDim.x;
+  const int64_t nc = VEC ? n / W : 0;
+  if (VEC) {
+#pragma unroll 2
+    for (int64_t c = t0; c < nc; c += st) {
+      Chunk16<T> rv, wv;
+      rv.load(r, c);
+      wv.load(w, c);
+#pragma unroll
+      for (int q = 0; q < W; ++q) rv.v[q] -= wv.v[q];
+      rv.store(t, c);
+    }
   }
+  for (int64_t i = nc * W + t0; i < n; i += st) t[i] = r[i] - w[i];
+}
+// w = (I - P) z (the start of an operator apply)
+template <typename T, bool VEC>
+__global__ void __launch_bounds__(kRedThreads)
+    k_init_w(int64_t n, const T* __restrict__ z, T* __restrict__ w, const uint8_t* __restrict__ ess,
+             const KrylovScalars* S) {
+  if (S->done) return;
+  constexpr int W = Chunk16<T>::W;
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, st = (int64_t)gridDim.x * blockDim.x;
+  const int64_t nc = VEC ? n / W : 0;
+  if (VEC) {
+#pragma unroll 2
+    for (int64_t c = t0; c < nc; c += st) {
+      Chunk16<T> zv;
+      zv.load(z, c);
+      uint8_t m[W];
+      if constexpr (W == 4) {
+        const uchar4 e4 = reinterpret_cast<const uchar4*>(ess)[c];
+        m[0] = e4.x, m[1] = e4.y, m[2] = e4.z, m[3] = e4.w;
+      } else {
+        const uchar2 e2 = reinterpret_cast<const uchar2*>(ess)[c];
+        m[0] = e2.x, m[1] = e2.y;
+      }
+#pragma unroll
+      for (int q = 0; q < W; ++q) zv.v[q] = m[q] ? zv.v[q] : T(0);
+      zv.store(w, c);
+    }
+  }
+  for (int64_t i = nc * W + t0; i < n; i += st) w[i] = ess[i] ? z[i] : T(0);
 }
 
 // ---------------------------------------------------------------------------
@@ -808,40 +873,59 @@ static hc_status pcg_run(hcop* h, const SolveCfg& cfg, const T* b, T* x, T* wk, 
       rho = rn;
     }
   }
-  // Chebyshev steps 1.. of z toward J z = r; w = (I - P) z on entry.  The
-  // last step leaves w = (I - P) z too when init_last (the next apply's start).
-  auto cheb_steps = [&](bool init_last) -> cudaError_t {
-    for (int k = 1; k < cfg.cheb_degree; ++k) {
-      cudaError_t e = op.apply(z, w, nullptr, nullptr, s);
-      if (e != cudaSuccess) return e;
-      ++napply;
-      const int init_next = (k + 1 < cfg.cheb_degree || init_last) ? 1 : 0;
-      k_chebk<T><<<g, kRedThreads, 0, s>>>(n, r, dinv, z, dk, w, h->ess, (T)c1s[k - 1], (T)c2s[k - 1],
-                                           init_next, S);
+  // Chebyshev smoothing of z toward J z = r (cfg.cheb_degree steps).  from0:
+  // z = 0 on entry; else w = J z on entry.  init_last: leave w = (I - P) z for
+  // the caller's next apply.  dk is stored only where a later step reads it.
+  const bool vec = al16(r) && al16(z) && al16(dk) && al16(w) && al16(dinv) &&
+                   (reinterpret_cast<uintptr_t>(h->ess) % (16 / sizeof(T))) == 0;
+  const unsigned gw = vgrid((n + Chunk16<T>::W - 1) / Chunk16<T>::W);
+  auto cheb_launch = [&](T c1, T c2, int f) {
+    if (vec)
+      k_cheb_step<T, true><<<gw, kRedThreads, 0, s>>>(n, r, dinv, z, dk, w, h->ess, c1, c2, f, S);
+    else
+      k_cheb_step<T, false><<<g, kRedThreads, 0, s>>>(n, r, dinv, z, dk, w, h->ess, c1, c2, f, S);
+  };
+  auto smooth = [&](bool from0, bool init_last) -> cudaError_t {
+    const int deg = cfg.cheb_degree;
+    for (int j = 0; j < deg; ++j) {
+      if (j > 0) {
+        cudaError_t e = op.apply(z, w, nullptr, nullptr, s);
+        if (e != cudaSuccess) return e;
+        ++napply;
+      }
+      int f = 0;
+      if (j == 0 && from0) f |= kCbZ0;
+      if (j == 1) f |= from0 ? kCbDkZ : kCbDk;
+      if (j >= 2) f |= kCbDk;
+      if (j + 1 < deg && (j >= 1 || !from0)) f |= kCbStoreDk;
+      if (j + 1 < deg || init_last) f |= kCbInitW;
+      const T c1 = j == 0 ? T(0) : (T)c1s[j - 1];
+      const T c2 = j == 0 ? (T)(1.0 / theta) : (T)c2s[j - 1];
+      cheb_launch(c1, c2, f);
     }
     return cudaGetLastError();
-  };
-  auto cheb = [&](bool init_last) -> cudaError_t {
-    k_cheb0<T><<<g, kRedThreads, 0, s>>>(n, r, dinv, z, dk, w, h->ess, (T)(1.0 / theta), S);
-    return cheb_steps(init_last);
   };
   // AUX_MULT: z = S r; z += c G V G^T (r - J z); z += S (r - J z) with S the
   // Chebyshev-Jacobi polynomial: a symmetric multiplicative (smoother,
   // gradient-space correction, smoother) cycle, as AMS cycles are.
   auto aux_mult = [&]() -> cudaError_t {
-    cudaError_t e = cheb(true);
+    cudaError_t e = smooth(true, true);
     if (e != cudaSuccess) return e;
     if ((e = op.apply(z, w, nullptr, nullptr, s)) != cudaSuccess) return e;
     ++napply;
-    k_amul_t<T><<<g, kRedThreads, 0, s>>>(n, r, w, dk, S);
+    if (vec)
+      k_amul_t<T, true><<<gw, kRedThreads, 0, s>>>(n, r, w, dk, S);
+    else
+      k_amul_t<T, false><<<g, kRedThreads, 0, s>>>(n, r, w, dk, S);
     const float coef[4] = {kAuxMultWeight, 0.0f, 0.0f, 0.0f};
     if ((e = auxmg_apply<T, 1>(h, dk, nullptr, z, nullptr, coef, &S->done, s)) != cudaSuccess) return e;
-    if ((e = init_masked<T>(n, h->ess, z, w, s)) != cudaSuccess) return e;
+    if (vec)
+      k_init_w<T, true><<<gw, kRedThreads, 0, s>>>(n, z, w, h->ess, S);
+    else
+      k_init_w<T, false><<<g, kRedThreads, 0, s>>>(n, z, w, h->ess, S);
     if ((e = op.apply(z, w, nullptr, nullptr, s)) != cudaSuccess) return e;
     ++napply;
-    k_cheb0r<T><<<g, kRedThreads, 0, s>>>(n, r, dinv, z, dk, w, h->ess, (T)(1.0 / theta),
-                                          cfg.cheb_degree > 1 ? 1 : 0, S);
-    return cheb_steps(false);
+    return smooth(false, false);
   };
   // z = B r for the non-Jacobi preconditioners
   auto precond = [&](bool z_ready) -> cudaError_t {
@@ -851,7 +935,7 @@ static hc_status pcg_run(hcop* h, const SolveCfg& cfg, const T* b, T* x, T* wk, 
       return auxmg_apply<T, 1>(h, r, nullptr, z, nullptr, coef, &S->done, s);
     }
     if (amult) return aux_mult();
-    return cheb(false);
+    return smooth(true, false);
   };
 
   // r = b - J x
