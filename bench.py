@@ -741,7 +741,8 @@ def run_serve(args):
         st = SV.latency_stats(done)
         kept[key] = ex.kept
         out[key] = {"requests": len(done), "steps": steps, "wall_s": wall, "solves_per_s": steps / wall,
-                    "ok": sum(r.result["status"] == "OK" for r in done), "precision": prec, **st}
+                    "ok": sum(r.result["status"] == "OK" for r in done), "precision": prec,
+                    "preconditioner": ex.precond, **st}
     diffs = [float(np.linalg.norm(kept["mixed"][k] - kept["fp64"][k]) / max(np.linalg.norm(kept["fp64"][k]), 1e-300))
              for k in kept["fp64"] if k in kept["mixed"]]
     # dominant kernel: the FP32 masked apply on a mid-size request (40^3 hexes, p = 2)
