@@ -209,19 +209,19 @@ class GpuExecutor:
     then takes its time steps with device-resident A, b, dA on a dedicated
     stream (one per worker).  keep: False, True, or a predicate on the
     request -- the final A of kept requests is copied to the host (kept).
-    precond None: the multiplicative auxiliary-space cycle ("aux_mult") for
-    the FP32 solves with residual replacement, the additive one ("aux")
-    otherwise -- the faster form of each precision (in FP64 the cycle's extra
-    operator applications cost more than its iterations save)."""
+    The default preconditioner is the additive auxiliary-space form: with the
+    multiplicative cycle ("aux_mult") FP32 solves with residual replacement to
+    rtol 1e-12 on small requests spend hundreds of iterations between
+    replacements near the FP32 floor."""
 
-    def __init__(self, slots, precision="mixed_rr", precond=None, rtol=1e-12, dt=0.01, keep=False,
+    def __init__(self, slots, precision="mixed_rr", precond="aux", rtol=1e-12, dt=0.01, keep=False,
                  inner_rtol=None):
         import torch
 
         self.torch = torch
         self.streams = [torch.cuda.Stream() for _ in range(slots)]
         self.precision = precision
-        self.precond = precond if precond is not None else ("aux_mult" if precision == "mixed_rr" else "aux")
+        self.precond = precond
         self.rtol = rtol
         self.dt = dt
         self.keep = keep
