@@ -82,7 +82,9 @@ enum {
  * symmetric multiplicative cycle, z = S r; z += c G V G^T (r - J z);
  * z += S (r - J z), S the Chebyshev-Jacobi polynomial of degree cheb_degree
  * (<= 0 -> 2) on [lmax/cheb_ratio, lmax], c = 1/2: 2 cheb_degree operator
- * applications per iteration, several times fewer iterations.           */
+ * applications per iteration, several times fewer iterations.  With
+ * HC_MIXED_RR it suits tolerances down to about 1e-10; tighter ones reach
+ * the FP32 floor of high-contrast fields and fall back to FP64 polishing. */
 enum { HC_PRECOND_NONE = 0, HC_PRECOND_JACOBI = 1, HC_PRECOND_CHEBYSHEV = 2, HC_PRECOND_AUX = 3,
        HC_PRECOND_AUX_MULT = 4 };
 
