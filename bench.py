@@ -559,8 +559,17 @@ def run_batch(args):
     base = {"Tolerance": args.solve_rtol, "AbsTolerance": 0.0, "MaxIter": 20000, "Preconditioner": "aux",
             "InnerTolerance": args.inner_rtol}
     t0 = time.perf_counter()
-    db = B.DeviceBatch(probs, dict(base, Precision="fp64"))
+    db = B.DeviceBatch(probs, dict(base, Precision="fp64"), autotune=not args.no_autotune)
     setup_s = time.perf_counter() - t0
+    tuned = None
+    if db.tuning:
+        tu = db.tuning
+        tuned = {"problems": len(tu), "shape_8x8x2": sum(t["shape"] == 1 for t in tu),
+                 "per_sm_set": sum(t["per_sm"] > 0 for t in tu),
+                 "complex_apply_us_default": float(sum(t["us_default"] for t in tu)),
+                 "complex_apply_us_tuned": float(sum(t["us"] for t in tu)),
+                 "how": "hc_autotune: FP32 complex apply timed per problem over brick shapes 16x4x2 / 8x8x2 "
+                        "and 0-4 CTAs per SM (setup, untimed)"}
     res, sols, times = {}, {}, {}
     for prec in ("fp64", "mixed", "mixed_rr"):
         db.set_params(dict(base, Precision=prec, InnerTolerance=0.1 if prec == "mixed_rr" else args.inner_rtol))
@@ -610,7 +619,7 @@ def run_batch(args):
                                for p in res},
         "rel_err_mixed_vs_fp64": {"max": max(rel), "median": float(np.median(rel))},
         "iterations": {p: [r["iterations"] for r in res[p]] for p in res},
-        "setup_seconds": setup_s,
+        "setup_seconds": setup_s, "launch_tuning": tuned,
     }
     # e2e: the same batch with its right-hand sides copied from pinned host
     # memory and its solutions copied back, inside the timed region
@@ -1210,6 +1219,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="batch: keep the default launch configuration")
     ap.add_argument("--no-tets", action="store_true", help="skip the tets block solves reported beside the hex line")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--cpu-step-seconds", type=float, default=1.0)

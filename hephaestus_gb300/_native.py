@@ -109,6 +109,10 @@ _SIGS = {
                                   C.POINTER(SolveInfo)]),
     "hc_lanczos_lmax": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "hc_precond_apply_device": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    "hc_set_launch": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "hc_get_launch": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "hc_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                              C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "hc_mult_multi_device": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     "hc_elem_type": (C.c_int32, [C.c_void_p]),
     "hc_tet_element_matrix": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),

@@ -46,13 +46,16 @@ def make_batch(count=64, seed=0, n_range=(8, 40), orders=(1, 2, 3), omega_range=
 
 
 class DeviceBatch:
-    """Resident operators, right-hand sides and solutions of a problem list."""
+    """Resident operators, right-hand sides and solutions of a problem list.
+    autotune: time the launch configurations of each order-1/2 problem's FP32
+    complex apply once (hc_autotune) before anything is solved."""
 
-    def __init__(self, problems, params):
+    def __init__(self, problems, params, autotune=False):
         import torch
 
         self.problems = problems
         self.ops, self.solvers, self.rhs, self.sols, self.streams = [], [], [], [], []
+        self.tuning = []
         for pb in problems:
             rng = np.random.default_rng(pb.seed)
             ne = pb.n ** 3
@@ -63,6 +66,8 @@ class DeviceBatch:
             b = torch.zeros(op.ndof, dtype=torch.float64, device="cuda")
             op.LoadCoilDevice(b, I0=float(rng.uniform(0.5, 2.0)))
             b.mul_(torch.tensor(op.ess_mask() == 0, device="cuda"))
+            if autotune and pb.p <= 2:
+                self.tuning.append(dict(op.Autotune("complex"), n=pb.n, p=pb.p))
             self.ops.append(op)
             self.streams.append(st)
             self.solvers.append(GpuComplexCOCGSolver(dict(params), op, pb.omega))

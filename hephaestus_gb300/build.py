@@ -13,8 +13,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libhcurl_gb300.so")
-SOURCES = ["hc_api.cu", "hc_hex.cu", "hc_hex_p1.cu", "hc_hex_p2.cu", "hc_hex_p3.cu", "hc_krylov.cu", "hc_post.cu", "hc_tet.cu", "hc_noalloc.cu",
-           "hc_complex.cu", "hc_auxmg.cu", "hc_multi.cu", "hc_tetaux.cu", "hc_fields.cu", "hc_dofmap.cu"]
+SOURCES = ["hc_api.cu", "hc_hex.cu", "hc_hex_p1.cu", "hc_hex_p2.cu", "hc_hex_p3.cu", "hc_hex_p1s.cu", "hc_hex_p2s.cu", "hc_krylov.cu", "hc_post.cu", "hc_tet.cu", "hc_noalloc.cu",
+           "hc_complex.cu", "hc_auxmg.cu", "hc_multi.cu", "hc_tetaux.cu", "hc_fields.cu", "hc_dofmap.cu", "hc_tune.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "--extended-lambda",
          "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]

@@ -294,7 +294,7 @@ void hc_destroy(hcop_t* h) {
   for (void* p : {(void*)h->nu, (void*)h->fac, (void*)h->facf, (void*)h->ess, (void*)h->diag, (void*)h->dinv, (void*)h->dinvf,
                   (void*)h->sdinv, (void*)h->sdinvf, (void*)h->scal, (void*)h->partials, h->work, (void*)h->xbuf,
                   (void*)h->ybuf, (void*)h->verts, (void*)h->tet_edofs, (void*)h->tet_sv, (void*)h->tetK64, (void*)h->tetK32,
-                  h->tetK16, (void*)h->tab})
+                  h->tetK16, (void*)h->tab, (void*)h->tab1})
     dfree(h, p);
   pinned_put(h->hscal);
   delete h;
@@ -451,14 +451,16 @@ hc_status hc_create(const hc_problem_desc* desc, hcop_t** out) {
       !alloc((void**)&h->dinvf, N * 4) || !alloc((void**)&h->sdinv, N * 8) || !alloc((void**)&h->sdinvf, N * 4) ||
       !alloc((void**)&h->xbuf, N * 8) || !alloc((void**)&h->ybuf, N * 8) || !alloc((void**)&h->nu, ne * 8))
     return fail_create(h, "hc_create: device allocation failed", HC_ENOMEM);
-  {
+  for (int shape = 0; shape < (p <= 2 ? 2 : 1); ++shape) {
     std::vector<int> tab;
-    hex_tile_table(p, nx, ny, tab);
-    if (dmalloc(h, (void**)&h->tab, tab.size() * sizeof(int)) != cudaSuccess)
+    hex_tile_table(p, shape, nx, ny, tab);
+    int** dst = shape ? &h->tab1 : &h->tab;
+    if (dmalloc(h, (void**)dst, tab.size() * sizeof(int)) != cudaSuccess)
       return fail_create(h, "hc_create: device allocation failed", HC_ENOMEM);
-    cudaMemcpyAsync(h->tab, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream);
+    cudaMemcpyAsync(*dst, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream);
     // pageable sources: each copy is staged before the call returns
   }
+  tune_lookup(h);  // a stored launch configuration for this problem, if any
   if (dmalloc(h, (void**)&h->verts, nv * 3 * sizeof(double)) != cudaSuccess)
     return fail_create(h, "hc_create: device allocation failed", HC_ENOMEM);
   cudaStream_t cs = h->stream;

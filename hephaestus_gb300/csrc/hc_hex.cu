@@ -10,13 +10,16 @@ namespace hc {
 cudaError_t upload_tables_p1(const void* td, const void* tf);
 cudaError_t upload_tables_p2(const void* td, const void* tf);
 cudaError_t upload_tables_p3(const void* td, const void* tf);
+cudaError_t upload_tables_p1s(const void* td, const void* tf);
+cudaError_t upload_tables_p2s(const void* td, const void* tf);
 cudaError_t upload_tables_post(const void* td, const void* tf);
 
 // upper bound on the blocks of any apply launch (sizes the reduction partials)
 int hex_apply_blocks(const HexDev& d) {
   const int legacy = (int)((d.ne + 127) / 128);
   const int b1 = brick_blocks<1>(d), b2 = brick_blocks<2>(d), b3 = brick_blocks<3>(d);
-  return std::max(std::max(legacy, b1), std::max(b2, b3));
+  const int s1 = brick_blocks<1, 1>(d), s2 = brick_blocks<2, 1>(d);
+  return std::max(std::max(std::max(legacy, b1), std::max(b2, b3)), std::max(s1, s2));
 }
 
 // instantiated in hc_hex_p{1,2,3}.cu
@@ -162,9 +165,9 @@ cudaError_t hex_diag_scaled(const HexDev& d, double* diag, double ms, double cs,
 
 cudaError_t hex_diag(const HexDev& d, double* diag, cudaStream_t s) { return hex_diag_scaled(d, diag, 1.0, 1.0, s); }
 
-void hex_tile_table(int p, int nx, int ny, std::vector<int>& tab) {
-  if (p == 1) build_tile_table<1>(nx, ny, tab);
-  else if (p == 2) build_tile_table<2>(nx, ny, tab);
+void hex_tile_table(int p, int shape, int nx, int ny, std::vector<int>& tab) {
+  if (p == 1) shape ? build_tile_table<1, 1>(nx, ny, tab) : build_tile_table<1, 0>(nx, ny, tab);
+  else if (p == 2) shape ? build_tile_table<2, 1>(nx, ny, tab) : build_tile_table<2, 0>(nx, ny, tab);
   else tab.assign(1, 0);
 }
 
@@ -183,6 +186,8 @@ cudaError_t upload_tables() {
   if (e == cudaSuccess) e = upload_tables_p1(td, tf);
   if (e == cudaSuccess) e = upload_tables_p2(td, tf);
   if (e == cudaSuccess) e = upload_tables_p3(td, tf);
+  if (e == cudaSuccess) e = upload_tables_p1s(td, tf);
+  if (e == cudaSuccess) e = upload_tables_p2s(td, tf);
   if (e == cudaSuccess) e = upload_tables_post(td, tf);
   return e;
 }

@@ -187,38 +187,49 @@ __global__ void __launch_bounds__(BX* BY* BZ, 2)
 }
 
 // y_r/y_i must hold (I-P) x_r / (I-P) x_i (masked) or zero (unmasked) on entry.
+template <typename T, int P, int S>
+cudaError_t hex_launch_cplx_ps(const HexDev& d, const T* fac, const T* xr, const T* xi, T* yr, T* yi, T omega,
+                               T cs, bool masked, const int* done, cudaStream_t s) {
+  using B = BrickShapeS<P, S>;
+  using TL = BrickTile<P, B::BX, B::BY, B::BZ>;
+  constexpr int nt = B::BX * B::BY * B::BZ;
+  const size_t sm = (6 * TL::total + 2 * (d.full ? 12 : 6) * nt) * sizeof(T);
+  const int nbricks = brick_blocks<P, S>(d);
+  static int occ_cache[2][2] = {{0, 0}, {0, 0}};
+  const int nsm = device_sms();
+  auto go = [&](auto kern, int f) {
+    int& occ = occ_cache[f][sizeof(T) == 8];
+    if (!occ) {
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nt, sm);
+      if (occ < 1) occ = 1;
+    }
+    const int per = d.per_sm > 0 ? std::min(d.per_sm, occ) : occ;
+    const int grid = std::min(nbricks, per * nsm);
+    kern<<<grid, nt, sm, s>>>(d, fac, xr, xi, yr, yi, omega, cs, masked, done, nbricks);
+  };
+  if (d.full) go(hex_apply_tiled_cplx<T, P, true, B::BX, B::BY, B::BZ>, 1);
+  else go(hex_apply_tiled_cplx<T, P, false, B::BX, B::BY, B::BZ>, 0);
+  return cudaGetLastError();
+}
+#define HC_EXTERN_CPLX_PS(T, P, S)                                                                             \
+  extern template cudaError_t hex_launch_cplx_ps<T, P, S>(const HexDev&, const T*, const T*, const T*, T*, T*, \
+                                                          T, T, bool, const int*, cudaStream_t);
+HC_EXTERN_CPLX_PS(double, 1, 1)
+HC_EXTERN_CPLX_PS(double, 2, 1)
+HC_EXTERN_CPLX_PS(float, 1, 1)
+HC_EXTERN_CPLX_PS(float, 2, 1)
+#undef HC_EXTERN_CPLX_PS
+
 template <typename T, int P>
 cudaError_t hex_launch_cplx_p(const HexDev& d, const T* fac, const T* xr, const T* xi, T* yr, T* yi, T omega,
                               T cs, bool masked, const int* done, cudaStream_t s) {
   if constexpr (P <= 2) {
-    using B = BrickShape<P>;
-    using TL = BrickTile<P, B::BX, B::BY, B::BZ>;
-    constexpr int nt = B::BX * B::BY * B::BZ;
-    const size_t sm = (6 * TL::total + 2 * (d.full ? 12 : 6) * nt) * sizeof(T);
-    const int nbricks = brick_blocks<P>(d);
-    static int occ_cache[2][2] = {{0, 0}, {0, 0}};
-    static int nsm = 0;
-    if (!nsm) {
-      int dev = 0;
-      cudaGetDevice(&dev);
-      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    }
-    auto go = [&](auto kern, int f) {
-      int& occ = occ_cache[f][sizeof(T) == 8];
-      if (!occ) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nt, sm);
-        if (occ < 1) occ = 1;
-      }
-      const int grid = std::min(nbricks, occ * nsm);
-      kern<<<grid, nt, sm, s>>>(d, fac, xr, xi, yr, yi, omega, cs, masked, done, nbricks);
-    };
-    if (d.full) go(hex_apply_tiled_cplx<T, P, true, B::BX, B::BY, B::BZ>, 1);
-    else go(hex_apply_tiled_cplx<T, P, false, B::BX, B::BY, B::BZ>, 0);
+    if (d.shape == 1) return hex_launch_cplx_ps<T, P, 1>(d, fac, xr, xi, yr, yi, omega, cs, masked, done, s);
+    return hex_launch_cplx_ps<T, P, 0>(d, fac, xr, xi, yr, yi, omega, cs, masked, done, s);
   } else {
     return cudaErrorInvalidValue;  // orders 1-2 only
   }
-  return cudaGetLastError();
 }
 
 }  // namespace hc

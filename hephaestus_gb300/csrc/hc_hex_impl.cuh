@@ -892,26 +892,30 @@ __global__ void __launch_bounds__(BX* BY* BZ, sizeof(T) == 4 ? (FULL ? 3 : 4) : 
   }
 }
 
+// Brick shapes of the tiled kernels (orders 1-2): shape 0 = 16 x 4 x 2
+// elements, shape 1 = 8 x 8 x 2 (fewer idle threads where nx is far from a
+// multiple of 16); order 3 runs the per-element kernel.  hc_autotune times
+// both per problem.
+template <int P, int S>
+struct BrickShapeS {
+  static constexpr int BX = 16, BY = 4, BZ = 2;
+};
 template <int P>
-struct BrickShape;
-template <>
-struct BrickShape<1> {
-  static constexpr int BX = 16, BY = 4, BZ = 2;
+struct BrickShapeS<P, 1> {
+  static constexpr int BX = 8, BY = 8, BZ = 2;
 };
 template <>
-struct BrickShape<2> {
-  static constexpr int BX = 16, BY = 4, BZ = 2;
-};
-template <>
-struct BrickShape<3> {
+struct BrickShapeS<3, 0> {
   static constexpr int BX = 4, BY = 4, BZ = 4;
 };
+template <int P>
+using BrickShape = BrickShapeS<P, 0>;
 
 // Host: per tile entry the dof offset relative to the brick's base (bit 31 set
 // when the entry lies on a brick face, i.e. is shared with a neighbour brick).
-template <int P>
+template <int P, int S = 0>
 inline void build_tile_table(int nx, int ny, std::vector<int>& tab) {
-  using B = BrickShape<P>;
+  using B = BrickShapeS<P, S>;
   using TL = BrickTile<P, B::BX, B::BY, B::BZ>;
   tab.assign(TL::total, 0);
   for (int c = 0; c < 3; ++c) {
@@ -927,56 +931,82 @@ inline void build_tile_table(int nx, int ny, std::vector<int>& tab) {
   }
 }
 
-template <int P>
+template <int P, int S = 0>
 __host__ __device__ inline int brick_blocks(const HexDev& d) {
-  using B = BrickShape<P>;
+  using B = BrickShapeS<P, S>;
   return ((d.nx + B::BX - 1) / B::BX) * ((d.ny + B::BY - 1) / B::BY) * ((d.nz + B::BZ - 1) / B::BZ);
 }
+
+// CTAs per SM of a persistent brick launch: the caller's (hc_autotune) when
+// set, capped by the occupancy; else occ, or one fewer when that needs no
+// more rounds over the bricks -- a last round that fills few slots costs as
+// much as a full one, and one more resident CTA per SM raises the brick
+// throughput by only about 10 % (measured at 64^3: 61.7 us with 3 CTAs per
+// SM, 56.0 us with 4).
+inline int bricks_per_sm(int occ, int nbricks, int nsm, int want) {
+  if (want > 0) return std::min(want, occ);
+  const auto rounds = [&](int per) { return (nbricks + per * nsm - 1) / (per * nsm); };
+  if (occ > 1 && rounds(occ - 1) * (occ - 1) * 1.1 <= rounds(occ) * occ) return occ - 1;
+  return occ;
+}
+
+inline int device_sms() {
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  }
+  return nsm;
+}
+
+// The tiled launch for one brick shape (instantiated per order and shape in
+// hc_hex_p{1,2}.cu and hc_hex_p{1,2}s.cu).
+template <typename T, int P, int S>
+cudaError_t hex_launch_ps(const HexDev& d, const T* fac, const T* x, T* y, T ms, T cs, bool masked,
+                          KrylovScalars* S_, double* partials, cudaStream_t s, bool y_zero_free) {
+  using B = BrickShapeS<P, S>;
+  using TL = BrickTile<P, B::BX, B::BY, B::BZ>;
+  constexpr int nt = B::BX * B::BY * B::BZ;
+  const size_t sm = (3 * TL::total + 2 * (d.full ? 12 : 6) * nt) * sizeof(T);
+  const int nbricks = brick_blocks<P, S>(d);
+  static int per_sm[2][2][2] = {{{0, 0}, {0, 0}}, {{0, 0}, {0, 0}}};
+  const int nsm = device_sms();
+  auto go = [&](auto kern, int f, int o) {
+    int& occ = per_sm[f][o][sizeof(T) == 8];
+    if (!occ) {
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nt, sm);
+      if (occ < 1) occ = 1;
+    }
+    const int grid = std::min(nbricks, bricks_per_sm(occ, nbricks, nsm, d.per_sm) * nsm);
+    kern<<<grid, nt, sm, s>>>(d, fac, x, y, ms, cs, masked, S_, partials, nbricks);
+  };
+  if (d.full) {
+    if (y_zero_free) go(hex_apply_tiled<T, P, true, B::BX, B::BY, B::BZ, true>, 1, 1);
+    else go(hex_apply_tiled<T, P, true, B::BX, B::BY, B::BZ, false>, 1, 0);
+  } else {
+    if (y_zero_free) go(hex_apply_tiled<T, P, false, B::BX, B::BY, B::BZ, true>, 0, 1);
+    else go(hex_apply_tiled<T, P, false, B::BX, B::BY, B::BZ, false>, 0, 0);
+  }
+  return cudaGetLastError();
+}
+#define HC_EXTERN_LAUNCH_PS(T, P, S)                                                                   \
+  extern template cudaError_t hex_launch_ps<T, P, S>(const HexDev&, const T*, const T*, T*, T, T, bool, \
+                                                     KrylovScalars*, double*, cudaStream_t, bool);
+HC_EXTERN_LAUNCH_PS(double, 1, 1)
+HC_EXTERN_LAUNCH_PS(double, 2, 1)
+HC_EXTERN_LAUNCH_PS(float, 1, 1)
+HC_EXTERN_LAUNCH_PS(float, 2, 1)
+#undef HC_EXTERN_LAUNCH_PS
 
 template <typename T, int P>
 cudaError_t hex_launch_p(const HexDev& d, const T* fac, const T* x, T* y, T ms, T cs, bool masked,
                          KrylovScalars* S, double* partials, cudaStream_t s, bool y_zero_free) {
   if constexpr (P <= 2) {
-    using B = BrickShape<P>;
-    using TL = BrickTile<P, B::BX, B::BY, B::BZ>;
-    constexpr int nthr = B::BX * B::BY * B::BZ;
-    const size_t sm = (3 * TL::total + 2 * (d.full ? 12 : 6) * nthr) * sizeof(T);
-    const int nbricks = brick_blocks<P>(d);
-    constexpr int nt = B::BX * B::BY * B::BZ;
-    static int per_sm[2][2][2] = {{{0, 0}, {0, 0}}, {{0, 0}, {0, 0}}};
-    static int nsm = 0;
-    if (!nsm) {
-      int dev = 0;
-      cudaGetDevice(&dev);
-      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    }
-    auto go = [&](auto kern, int f, int o) {
-      int& occ = per_sm[f][o][sizeof(T) == 8];
-      if (!occ) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nt, sm);
-        if (occ < 1) occ = 1;
-      }
-      // Persistent grid: occ CTAs per SM, or one fewer when that needs no
-      // more rounds over the bricks -- a last round that fills few slots
-      // costs as much as a full one, and one more resident CTA per SM raises
-      // the brick throughput by only about 10 % (measured at 64^3: 61.7 us
-      // with 3 CTAs per SM, 56.0 us with 4).
-      const auto rounds = [&](int per) { return (nbricks + per * nsm - 1) / (per * nsm); };
-      int per_sm_used = occ;
-      if (occ > 1 && rounds(occ - 1) * (occ - 1) * 1.1 <= rounds(occ) * occ) per_sm_used = occ - 1;
-      const int grid = std::min(nbricks, per_sm_used * nsm);
-      kern<<<grid, nt, sm, s>>>(d, fac, x, y, ms, cs, masked, S, partials, nbricks);
-    };
-    if (d.full) {
-      if (y_zero_free) go(hex_apply_tiled<T, P, true, B::BX, B::BY, B::BZ, true>, 1, 1);
-      else go(hex_apply_tiled<T, P, true, B::BX, B::BY, B::BZ, false>, 1, 0);
-    } else {
-      if (y_zero_free) go(hex_apply_tiled<T, P, false, B::BX, B::BY, B::BZ, true>, 0, 1);
-      else go(hex_apply_tiled<T, P, false, B::BX, B::BY, B::BZ, false>, 0, 0);
-    }
-    return cudaGetLastError();
+    if (d.shape == 1) return hex_launch_ps<T, P, 1>(d, fac, x, y, ms, cs, masked, S, partials, s, y_zero_free);
+    return hex_launch_ps<T, P, 0>(d, fac, x, y, ms, cs, masked, S, partials, s, y_zero_free);
   } else {
     const int blocks = (int)((d.ne + 127) / 128);
     if (d.full)

@@ -58,7 +58,10 @@ struct HexDev {
   int ess_bits;       // face attribute bits (implicit mask)
   const uint8_t* ess; // explicit device mask or nullptr
   const double* fac;  // FP64 factors (diagonal, FP64 apply)
-  const int* tab;     // brick tile table (relative dof offsets, bit 31 = brick face)
+  const int* tab;     // brick tile table of the active brick shape (relative dof
+                      // offsets, bit 31 = brick face)
+  int shape;          // brick shape of the tiled kernels (orders 1-2): 0 = 16x4x2, 1 = 8x8x2
+  int per_sm;         // CTAs per SM of the tiled kernels, 0 = the launcher's choice
 };
 
 }  // namespace hc
@@ -103,7 +106,9 @@ struct hcop {
   double* tetK64 = nullptr;            // ne * L * L element matrices (FP64)
   float* tetK32 = nullptr;             // FP32 copy
   void* tetK16 = nullptr;              // BF16 copy (made on first use)
-  int* tab = nullptr;                  // brick tile table of the apply kernel
+  int* tab = nullptr;                  // brick tile table of the apply kernel (shape 0)
+  int* tab1 = nullptr;                 // the same for brick shape 1 (orders 1-2)
+  int shape = 0, per_sm = 0;           // launch configuration of the tiled kernels (hc_autotune)
   void* cwork = nullptr;               // complex (frequency-domain) work space, hc_complex.cu
   void* aux = nullptr;                 // auxiliary-space preconditioner, hc_auxmg.cu
   void* mwork = nullptr;               // multi-RHS block PCG work space, hc_multi.cu
@@ -127,7 +132,9 @@ struct hcop {
     d.ess_bits = ess_bits;
     d.ess = explicit_mask ? ess : nullptr;
     d.fac = fac;
-    d.tab = tab;
+    d.shape = (shape == 1 && tab1) ? 1 : 0;
+    d.tab = d.shape ? tab1 : tab;
+    d.per_sm = per_sm;
     return d;
   }
 };
@@ -160,8 +167,10 @@ cudaError_t hex_apply(const HexDev& d, const T* fac, const T* x, T* y, double ms
 cudaError_t hex_diag(const HexDev& d, double* diag, cudaStream_t s);
 // diag += mscale * diag(M) + cscale * diag(dt C) (the two parts of hex_diag, scaled)
 cudaError_t hex_diag_scaled(const HexDev& d, double* diag, double mscale, double cscale, cudaStream_t s);
-// tile table of the brick kernel for order p on an nx x ny grid (host)
-void hex_tile_table(int p, int nx, int ny, std::vector<int>& tab);
+// a launch configuration stored by hc_autotune for this handle's problem, if any (hc_tune.cu)
+void tune_lookup(hcop* h);
+// tile table of the brick kernel for order p and brick shape `shape` on an nx x ny grid (host)
+void hex_tile_table(int p, int shape, int nx, int ny, std::vector<int>& tab);
 
 // ---- hc_post.cu ----
 void hex_rt_layout(const HexDev& d, int64_t* off1, int64_t* off2, int64_t* n);

@@ -430,6 +430,26 @@ class HCurlOperator:
                                                 _dev_ptr(z, "float64")), self.h)
         return z
 
+    def SetLaunch(self, shape=0, per_sm=0):
+        """Brick shape (0: 16x4x2, 1: 8x8x2 elements) and CTAs per SM (0: the
+        launcher's choice) of the tiled hex kernels (hc_set_launch)."""
+        N.check(N.lib().hc_set_launch(self.h, int(shape), int(per_sm)), self.h)
+
+    def GetLaunch(self):
+        sh, per = C.c_int32(0), C.c_int32(0)
+        N.check(N.lib().hc_get_launch(self.h, C.byref(sh), C.byref(per)), self.h)
+        return {"shape": sh.value, "per_sm": per.value}
+
+    def Autotune(self, kind="real"):
+        """Time the FP32 apply (kind 'real' or 'complex') over brick shapes and
+        CTAs per SM, keep the fastest (hc_autotune); returns the choice with
+        the mean launch times of it and of the default configuration."""
+        sh, per = C.c_int32(0), C.c_int32(0)
+        best, dflt = C.c_double(0), C.c_double(0)
+        N.check(N.lib().hc_autotune(self.h, {"real": 0, "complex": 1}[kind], C.byref(sh), C.byref(per),
+                                    C.byref(best), C.byref(dflt)), self.h)
+        return {"shape": sh.value, "per_sm": per.value, "us": best.value, "us_default": dflt.value}
+
     def LanczosLmax(self, steps=20):
         v = C.c_double(0)
         N.check(N.lib().hc_lanczos_lmax(self.h, steps, C.byref(v)), self.h)

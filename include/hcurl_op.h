@@ -172,6 +172,25 @@ hc_status hc_add_weak_curlcurl_device(hcop_t* h, const double* x, double* y, dou
 /* Diagonal of J (HypreDiagScale's diagonal, hephaestus_solvers.hpp:34-57).  */
 hc_status hc_diag(hcop_t* h, double* d);
 
+/* Launch configuration of the tiled hex kernels (orders 1-2): brick shape
+ * 0 = 16x4x2 elements per CTA, 1 = 8x8x2; per_sm = CTAs per SM of the
+ * persistent grid (0 = the launcher's choice, larger values are capped by
+ * the occupancy).  Results do not depend on it beyond rounding order.     */
+hc_status hc_set_launch(hcop_t* h, int32_t shape, int32_t per_sm);
+hc_status hc_get_launch(const hcop_t* h, int32_t* shape, int32_t* per_sm);
+/* Autotuner: times the FP32 apply (kind 0: the masked real apply of the
+ * inner PCG iterations; 1: the fused complex apply of COCG) for each brick
+ * shape and per_sm in 0..4 with CUDA events on the handle's stream (two
+ * warm-up and five timed launches each) and keeps the fastest for this
+ * handle.  The choice is also kept in a process-wide table keyed by (order,
+ * grid, axis-aligned or not) and, when the environment variable
+ * HC_TUNE_FILE names a file, appended to it; hc_create applies a stored
+ * entry for its key.  Outputs (may be NULL): the chosen shape and per_sm,
+ * the mean launch time of the choice and of the default (0, 0) in us.
+ * HC_ENOTSUP for tet handles and hex order 3 (no tiled kernel).           */
+hc_status hc_autotune(hcop_t* h, int32_t kind, int32_t* shape, int32_t* per_sm, double* us_best,
+                      double* us_default);
+
 /* Device-pointer forms, enqueued on the handle's stream.                   */
 hc_status hc_mult_device(hcop_t* h, const double* x, double* y);
 hc_status hc_mult_device_f32(hcop_t* h, const float* x, float* y);
