@@ -559,7 +559,7 @@ def run_batch(args):
     base = {"Tolerance": args.solve_rtol, "AbsTolerance": 0.0, "MaxIter": 20000, "Preconditioner": "aux",
             "InnerTolerance": args.inner_rtol}
     t0 = time.perf_counter()
-    db = B.DeviceBatch(probs, dict(base, Precision="fp64"), autotune=not args.no_autotune)
+    db = B.DeviceBatch(probs, dict(base, Precision="fp64"), autotune=args.autotune)
     setup_s = time.perf_counter() - t0
     tuned = None
     if db.tuning:
@@ -1219,7 +1219,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-autotune", action="store_true", help="batch: keep the default launch configuration")
+    ap.add_argument("--autotune", action="store_true",
+                    help="batch: tune each problem's launch configuration at set-up (hc_autotune)")
     ap.add_argument("--no-tets", action="store_true", help="skip the tets block solves reported beside the hex line")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--cpu-step-seconds", type=float, default=1.0)
