@@ -347,8 +347,6 @@ __global__ void __launch_bounds__(128) hex_apply_kernel(HexDev d, const T* __res
         fc[kd[q]] = cscale * __ldg(fac + (int64_t)(6 + kd[q]) * d.ne + e);
       }
     }
-    T r0[RTC], r1[RTC], r2[RTC];
-    curl_nd<T, P>(u0, u1, u2, r0, r1, r2);
     T y0[NDC], y1[NDC], y2[NDC];
 #pragma unroll
     for (int i = 0; i < NDC; ++i) y0[i] = y1[i] = y2[i] = T(0);
@@ -370,26 +368,32 @@ __global__ void __launch_bounds__(128) hex_apply_kernel(HexDev d, const T* __res
 #pragma unroll
       for (int i = 0; i < NDC; ++i) eacc += u0[i] * y0[i] + u1[i] * y1[i] + u2[i] * y2[i];
     }
-    T g0[RTC], g1[RTC], g2[RTC];
+    // the curl-curl part (skipped when cscale = 0: the mass-only launches of
+    // the order-3 complex apply)
+    if (cscale != T(0)) {
+      T r0[RTC], r1[RTC], r2[RTC];
+      curl_nd<T, P>(u0, u1, u2, r0, r1, r2);
+      T g0[RTC], g1[RTC], g2[RTC];
 #pragma unroll
-    for (int i = 0; i < RTC; ++i) g0[i] = g1[i] = g2[i] = T(0);
-    rt_block<T, P, 0, 0>(r0, g0, fc[0]);
-    rt_block<T, P, 1, 1>(r1, g1, fc[3]);
-    rt_block<T, P, 2, 2>(r2, g2, fc[5]);
-    if constexpr (FULL) {
-      rt_block<T, P, 0, 1>(r1, g0, fc[1]);
-      rt_block<T, P, 0, 2>(r2, g0, fc[2]);
-      rt_block<T, P, 1, 0>(r0, g1, fc[1]);
-      rt_block<T, P, 1, 2>(r2, g1, fc[4]);
-      rt_block<T, P, 2, 0>(r0, g2, fc[2]);
-      rt_block<T, P, 2, 1>(r1, g2, fc[4]);
-    }
-    if (want_energy) {
+      for (int i = 0; i < RTC; ++i) g0[i] = g1[i] = g2[i] = T(0);
+      rt_block<T, P, 0, 0>(r0, g0, fc[0]);
+      rt_block<T, P, 1, 1>(r1, g1, fc[3]);
+      rt_block<T, P, 2, 2>(r2, g2, fc[5]);
+      if constexpr (FULL) {
+        rt_block<T, P, 0, 1>(r1, g0, fc[1]);
+        rt_block<T, P, 0, 2>(r2, g0, fc[2]);
+        rt_block<T, P, 1, 0>(r0, g1, fc[1]);
+        rt_block<T, P, 1, 2>(r2, g1, fc[4]);
+        rt_block<T, P, 2, 0>(r0, g2, fc[2]);
+        rt_block<T, P, 2, 1>(r1, g2, fc[4]);
+      }
+      if (want_energy) {
 #pragma unroll
-      for (int i = 0; i < RTC; ++i) eacc += r0[i] * g0[i] + r1[i] * g1[i] + r2[i] * g2[i];
-      en = (double)eacc;
+        for (int i = 0; i < RTC; ++i) eacc += r0[i] * g0[i] + r1[i] * g1[i] + r2[i] * g2[i];
+      }
+      curl_nd_t<T, P>(g0, g1, g2, y0, y1, y2);
     }
-    curl_nd_t<T, P>(g0, g1, g2, y0, y1, y2);
+    if (want_energy) en = (double)eacc;
     scatter<T, P, 0>(d, y, ex, ey, ez, mk, y0);
     scatter<T, P, 1>(d, y, ex, ey, ez, mk, y1);
     scatter<T, P, 2>(d, y, ex, ey, ez, mk, y2);
