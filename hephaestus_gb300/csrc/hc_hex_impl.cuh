@@ -348,13 +348,53 @@ __global__ void __launch_bounds__(128) hex_apply_kernel(HexDev d, const T* __res
       }
     }
     T y0[NDC], y1[NDC], y2[NDC];
+    T eacc = T(0);
+    const bool curl = cscale != T(0);  // 0: the mass-only launches of the order-3 complex apply
+    if constexpr (!FULL) {
+      // axis-aligned: the blocks are diagonal; the curl is taken first, then
+      // each u_c dies with its own mass block and each r_c with its own
+      // curl-curl block, which keeps the live set small (the order-3
+      // element carries 144 dofs)
+      T r0[RTC], r1[RTC], r2[RTC];
+      if (curl) curl_nd<T, P>(u0, u1, u2, r0, r1, r2);
+      auto mass_c = [&](auto cc, const T* u, T* yv) {
+        constexpr int c = decltype(cc)::value;
+        if (mscale == T(0)) {
 #pragma unroll
-    for (int i = 0; i < NDC; ++i) y0[i] = y1[i] = y2[i] = T(0);
-    if (mscale != T(0)) {
-      mass_block<T, P, 0, 0>(u0, y0, fm[0]);
-      mass_block<T, P, 1, 1>(u1, y1, fm[3]);
-      mass_block<T, P, 2, 2>(u2, y2, fm[5]);
-      if constexpr (FULL) {
+          for (int i = 0; i < NDC; ++i) yv[i] = T(0);
+        } else {
+          mass_block<T, P, c, c, false>(u, yv, fm[c == 0 ? 0 : (c == 1 ? 3 : 5)]);
+        }
+        if (want_energy) {
+#pragma unroll
+          for (int i = 0; i < NDC; ++i) eacc += u[i] * yv[i];
+        }
+      };
+      mass_c(std::integral_constant<int, 2>{}, u2, y2);
+      mass_c(std::integral_constant<int, 1>{}, u1, y1);
+      mass_c(std::integral_constant<int, 0>{}, u0, y0);
+      if (curl) {
+        T g0[RTC], g1[RTC], g2[RTC];
+        auto rt_c = [&](auto cc, const T* r, T* gv) {
+          constexpr int c = decltype(cc)::value;
+          rt_block<T, P, c, c, false>(r, gv, fc[c == 0 ? 0 : (c == 1 ? 3 : 5)]);
+          if (want_energy) {
+#pragma unroll
+            for (int i = 0; i < RTC; ++i) eacc += r[i] * gv[i];
+          }
+        };
+        rt_c(std::integral_constant<int, 0>{}, r0, g0);
+        rt_c(std::integral_constant<int, 1>{}, r1, g1);
+        rt_c(std::integral_constant<int, 2>{}, r2, g2);
+        curl_nd_t<T, P>(g0, g1, g2, y0, y1, y2);
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < NDC; ++i) y0[i] = y1[i] = y2[i] = T(0);
+      if (mscale != T(0)) {
+        mass_block<T, P, 0, 0>(u0, y0, fm[0]);
+        mass_block<T, P, 1, 1>(u1, y1, fm[3]);
+        mass_block<T, P, 2, 2>(u2, y2, fm[5]);
         mass_block<T, P, 0, 1>(u1, y0, fm[1]);
         mass_block<T, P, 0, 2>(u2, y0, fm[2]);
         mass_block<T, P, 1, 0>(u0, y1, fm[1]);
@@ -362,36 +402,31 @@ __global__ void __launch_bounds__(128) hex_apply_kernel(HexDev d, const T* __res
         mass_block<T, P, 2, 0>(u0, y2, fm[2]);
         mass_block<T, P, 2, 1>(u1, y2, fm[4]);
       }
-    }
-    T eacc = T(0);
-    if (want_energy) {
+      if (want_energy) {
 #pragma unroll
-      for (int i = 0; i < NDC; ++i) eacc += u0[i] * y0[i] + u1[i] * y1[i] + u2[i] * y2[i];
-    }
-    // the curl-curl part (skipped when cscale = 0: the mass-only launches of
-    // the order-3 complex apply)
-    if (cscale != T(0)) {
-      T r0[RTC], r1[RTC], r2[RTC];
-      curl_nd<T, P>(u0, u1, u2, r0, r1, r2);
-      T g0[RTC], g1[RTC], g2[RTC];
+        for (int i = 0; i < NDC; ++i) eacc += u0[i] * y0[i] + u1[i] * y1[i] + u2[i] * y2[i];
+      }
+      if (curl) {
+        T r0[RTC], r1[RTC], r2[RTC];
+        curl_nd<T, P>(u0, u1, u2, r0, r1, r2);
+        T g0[RTC], g1[RTC], g2[RTC];
 #pragma unroll
-      for (int i = 0; i < RTC; ++i) g0[i] = g1[i] = g2[i] = T(0);
-      rt_block<T, P, 0, 0>(r0, g0, fc[0]);
-      rt_block<T, P, 1, 1>(r1, g1, fc[3]);
-      rt_block<T, P, 2, 2>(r2, g2, fc[5]);
-      if constexpr (FULL) {
+        for (int i = 0; i < RTC; ++i) g0[i] = g1[i] = g2[i] = T(0);
+        rt_block<T, P, 0, 0>(r0, g0, fc[0]);
+        rt_block<T, P, 1, 1>(r1, g1, fc[3]);
+        rt_block<T, P, 2, 2>(r2, g2, fc[5]);
         rt_block<T, P, 0, 1>(r1, g0, fc[1]);
         rt_block<T, P, 0, 2>(r2, g0, fc[2]);
         rt_block<T, P, 1, 0>(r0, g1, fc[1]);
         rt_block<T, P, 1, 2>(r2, g1, fc[4]);
         rt_block<T, P, 2, 0>(r0, g2, fc[2]);
         rt_block<T, P, 2, 1>(r1, g2, fc[4]);
-      }
-      if (want_energy) {
+        if (want_energy) {
 #pragma unroll
-        for (int i = 0; i < RTC; ++i) eacc += r0[i] * g0[i] + r1[i] * g1[i] + r2[i] * g2[i];
+          for (int i = 0; i < RTC; ++i) eacc += r0[i] * g0[i] + r1[i] * g1[i] + r2[i] * g2[i];
+        }
+        curl_nd_t<T, P>(g0, g1, g2, y0, y1, y2);
       }
-      curl_nd_t<T, P>(g0, g1, g2, y0, y1, y2);
     }
     if (want_energy) en = (double)eacc;
     scatter<T, P, 0>(d, y, ex, ey, ez, mk, y0);
