@@ -80,8 +80,13 @@ cudaError_t complex_apply_done(hcop* h, double omega, const T* xr, const T* xi, 
     case 1: return hex_launch_cplx_p<T, 1>(d, fac, xr, xi, yr, yi, om, cs, true, done, s);
     case 2: return hex_launch_cplx_p<T, 2>(d, fac, xr, xi, yr, yi, om, cs, true, done, s);
     case 3: {
-      // order 3: four launches of the real kernel (no fused variant)
       (void)done;
+      if (!d.full) {  // one two-input launch per output
+        e = hex_launch_pair<T, 3>(d, fac, xr, xi, yr, -om, cs, s);
+        if (e == cudaSuccess) e = hex_launch_pair<T, 3>(d, fac, xi, xr, yi, om, cs, s);
+        return e;
+      }
+      // general parallelepipeds: four launches of the real kernel
       e = hex_apply<T>(d, fac, xr, yr, 0.0, (double)cs, true, nullptr, nullptr, s, false);
       if (e == cudaSuccess && om != T(0)) e = hex_apply<T>(d, fac, xi, yr, -omega, 0.0, true, nullptr, nullptr, s, false);
       if (e == cudaSuccess) e = hex_apply<T>(d, fac, xi, yi, 0.0, (double)cs, true, nullptr, nullptr, s, false);

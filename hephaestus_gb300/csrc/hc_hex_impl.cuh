@@ -450,6 +450,82 @@ __global__ void __launch_bounds__(128) hex_apply_kernel(HexDev d, const T* __res
   }
 }
 
+// y += cscale C xc + mscale M xm on axis-aligned grids, thread per element,
+// essential rows and columns masked: one launch per output of the order-3
+// complex apply (y_r = C x_r - w M x_i, y_i = C x_i + w M x_r) instead of two.
+// The curl-curl part runs first (its inputs die before the mass inputs are
+// gathered), then the mass input one component at a time.
+template <typename T, int P>
+__global__ void __launch_bounds__(128) hex_apply_pair_kernel(HexDev d, const T* __restrict__ fac,
+                                                             const T* __restrict__ xc, const T* __restrict__ xm,
+                                                             T* __restrict__ y, T mscale, T cscale) {
+  constexpr int C = P + 1, O = P;
+  constexpr int NDC = O * C * C;
+  constexpr int RTC = C * O * O;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.ne) return;
+  const int ex = (int)(e % d.nx);
+  const int ey = (int)((e / d.nx) % d.ny);
+  const int ez = (int)(e / ((int64_t)d.nx * d.ny));
+  constexpr int kd[3] = {0, 3, 5};
+  T fm[3], fc[3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    fm[q] = mscale * __ldg(fac + (int64_t)kd[q] * d.ne + e);
+    fc[q] = cscale * __ldg(fac + (int64_t)(6 + kd[q]) * d.ne + e);
+  }
+  T y0[NDC], y1[NDC], y2[NDC];
+#pragma unroll
+  for (int i = 0; i < NDC; ++i) y0[i] = y1[i] = y2[i] = T(0);
+  {
+    T r0[RTC], r1[RTC], r2[RTC];
+    {
+      T u0[NDC], u1[NDC], u2[NDC];
+      gather<T, P, 0>(d, xc, ex, ey, ez, true, u0);
+      gather<T, P, 1>(d, xc, ex, ey, ez, true, u1);
+      gather<T, P, 2>(d, xc, ex, ey, ez, true, u2);
+      curl_nd<T, P>(u0, u1, u2, r0, r1, r2);
+    }
+    T g0[RTC], g1[RTC], g2[RTC];
+    rt_block<T, P, 0, 0, false>(r0, g0, fc[0]);
+    rt_block<T, P, 1, 1, false>(r1, g1, fc[1]);
+    rt_block<T, P, 2, 2, false>(r2, g2, fc[2]);
+    curl_nd_t<T, P>(g0, g1, g2, y0, y1, y2);
+  }
+  {
+    T v[NDC];
+    gather<T, P, 0>(d, xm, ex, ey, ez, true, v);
+    mass_block<T, P, 0, 0>(v, y0, fm[0]);
+  }
+  {
+    T v[NDC];
+    gather<T, P, 1>(d, xm, ex, ey, ez, true, v);
+    mass_block<T, P, 1, 1>(v, y1, fm[1]);
+  }
+  {
+    T v[NDC];
+    gather<T, P, 2>(d, xm, ex, ey, ez, true, v);
+    mass_block<T, P, 2, 2>(v, y2, fm[2]);
+  }
+  scatter<T, P, 0>(d, y, ex, ey, ez, true, y0);
+  scatter<T, P, 1>(d, y, ex, ey, ez, true, y1);
+  scatter<T, P, 2>(d, y, ex, ey, ez, true, y2);
+}
+
+template <typename T, int P>
+cudaError_t hex_launch_pair(const HexDev& d, const T* fac, const T* xc, const T* xm, T* y, T ms, T cs,
+                            cudaStream_t s) {
+  if (d.full) return cudaErrorInvalidValue;  // axis-aligned grids only
+  const int blocks = (int)((d.ne + 127) / 128);
+  hex_apply_pair_kernel<T, P><<<blocks, 128, 0, s>>>(d, fac, xc, xm, y, ms, cs);
+  return cudaGetLastError();
+}
+// instantiated in hc_hex_p3.cu
+extern template cudaError_t hex_launch_pair<double, 3>(const HexDev&, const double*, const double*, const double*,
+                                                       double*, double, double, cudaStream_t);
+extern template cudaError_t hex_launch_pair<float, 3>(const HexDev&, const float*, const float*, const float*,
+                                                      float*, float, float, cudaStream_t);
+
 // ---------------------------------------------------------------------------
 // Brick-tiled apply: one CTA per brick of BX x BY x BZ elements, one thread per
 // element.  The brick's dofs (both closed boundary planes included) are

@@ -220,6 +220,10 @@ cudaError_t dot_alpha(int64_t n, const T* p, const T* q, KrylovScalars* S, doubl
 template <typename T, int P>
 cudaError_t hex_launch_cplx_p(const HexDev& d, const T* fac, const T* xr, const T* xi, T* yr, T* yi, T omega,
                               T cs, bool masked, const int* done, cudaStream_t s);
+// y += cs C xc + ms M xm (masked, axis-aligned grids; order 3, hc_hex_p3.cu)
+template <typename T, int P>
+cudaError_t hex_launch_pair(const HexDev& d, const T* fac, const T* xc, const T* xm, T* y, T ms, T cs,
+                            cudaStream_t s);
 // ---- hc_auxmg.cu ----
 // gradient-space (auxiliary) preconditioner: setup once per handle (FP32)
 hc_status auxmg_setup(hcop* h);
