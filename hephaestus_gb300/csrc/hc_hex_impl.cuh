@@ -307,7 +307,7 @@ __device__ __forceinline__ int symk(int a, int b) {
 }
 
 template <typename T, int P, bool FULL>
-__global__ void __launch_bounds__(128) hex_apply_kernel(HexDev d, const T* __restrict__ fac,
+__global__ void __launch_bounds__(128, 1) hex_apply_kernel(HexDev d, const T* __restrict__ fac,
                                                         const T* __restrict__ x, T* __restrict__ y,
                                                         T mscale, T cscale, int masked,
                                                         KrylovScalars* S, double* partials) {
@@ -456,7 +456,7 @@ __global__ void __launch_bounds__(128) hex_apply_kernel(HexDev d, const T* __res
 // The curl-curl part runs first (its inputs die before the mass inputs are
 // gathered), then the mass input one component at a time.
 template <typename T, int P>
-__global__ void __launch_bounds__(128) hex_apply_pair_kernel(HexDev d, const T* __restrict__ fac,
+__global__ void __launch_bounds__(128, 1) hex_apply_pair_kernel(HexDev d, const T* __restrict__ fac,
                                                              const T* __restrict__ xc, const T* __restrict__ xm,
                                                              T* __restrict__ y, T mscale, T cscale) {
   constexpr int C = P + 1, O = P;
