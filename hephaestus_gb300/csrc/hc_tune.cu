@@ -5,30 +5,24 @@
 // table and, when the environment variable HC_TUNE_FILE names a file, in that
 // file (one line per problem: p full nx ny nz shape per_sm us kind), so later
 // processes start tuned: hc_create applies a stored entry for its key.
-#include <array>
 #include <cstdio>
 #include <cstdlib>
 #include <map>
 #include <mutex>
-#include <vector>
 
 #include "hc_internal.h"
+#include "hc_tune_table.h"
 
 namespace hc {
 namespace {
 
-using Key = std::array<int, 5>;  // p, full, nx, ny, nz
-struct Entry {
-  int shape = 0, per_sm = 0;
-};
-
 std::mutex g_mu;
-std::map<Key, Entry> g_table;
+std::map<TuneKey, TuneEntry> g_table;
 bool g_loaded = false;
 
-Key key_of(const hcop* h) { return Key{h->p, h->full ? 1 : 0, h->nx, h->ny, h->nz}; }
+TuneKey key_of(const hcop* h) { return TuneKey{h->p, h->full ? 1 : 0, h->nx, h->ny, h->nz}; }
 
-// entries of HC_TUNE_FILE (once per process; later lines win)
+// entries of HC_TUNE_FILE (once per process)
 void load_locked() {
   if (g_loaded) return;
   g_loaded = true;
@@ -36,25 +30,14 @@ void load_locked() {
   if (!path || !*path) return;
   FILE* f = std::fopen(path, "r");
   if (!f) return;
-  int p, full, nx, ny, nz, shape, per;
-  double us;
-  int kind;
-  while (std::fscanf(f, "%d %d %d %d %d %d %d %lf %d", &p, &full, &nx, &ny, &nz, &shape, &per, &us, &kind) == 9) {
-    if (shape < 0 || shape > 1 || per < 0 || per > 64) continue;
-    g_table[Key{p, full, nx, ny, nz}] = Entry{shape, per};
-  }
+  tune_read(f, g_table);
   std::fclose(f);
 }
 
-void store_locked(const hcop* h, const Entry& e, double us, int kind) {
+void store_locked(const hcop* h, const TuneEntry& e, double us, int kind) {
   g_table[key_of(h)] = e;
   const char* path = std::getenv("HC_TUNE_FILE");
-  if (!path || !*path) return;
-  FILE* f = std::fopen(path, "a");
-  if (!f) return;
-  std::fprintf(f, "%d %d %d %d %d %d %d %.3f %d\n", h->p, h->full ? 1 : 0, h->nx, h->ny, h->nz, e.shape,
-               e.per_sm, us, kind);
-  std::fclose(f);
+  if (path && *path) tune_append(path, key_of(h), e, us, kind);
 }
 
 }  // namespace
@@ -128,7 +111,7 @@ hc_status hc_autotune(hcop_t* h, int32_t kind, int32_t* shape, int32_t* per_sm, 
   const int old_shape = h->shape, old_per = h->per_sm;
   const int reps = 5;
   double best = 1e300, def = 0.0;
-  Entry pick{0, 0};
+  TuneEntry pick{0, 0};
   cudaError_t err = cudaSuccess;
   for (int sh = 0; sh < 2 && err == cudaSuccess; ++sh) {
     for (int per = 0; per <= 4 && err == cudaSuccess; ++per) {
@@ -145,7 +128,7 @@ hc_status hc_autotune(hcop_t* h, int32_t kind, int32_t* shape, int32_t* per_sm, 
       if (sh == 0 && per == 0) def = us;
       if (us < best) {
         best = us;
-        pick = Entry{sh, per};
+        pick = TuneEntry{sh, per};
       }
     }
   }
