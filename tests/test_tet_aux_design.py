@@ -119,3 +119,45 @@ def test_p2_gradient_correction_is_what_order_2_needs(local_tables):
     aux_p1 = _pcg(K, b, lambda r: r / d + G1 @ lu1.solve(G1.T @ r))
     assert aux_p2 < 0.35 * jac, (aux_p2, jac)
     assert aux_p1 > 0.8 * jac, (aux_p1, jac)
+
+
+def test_multiplicative_cycle_on_tets(local_tables):
+    """The symmetric multiplicative cycle (Chebyshev-Jacobi(2) smoothing around
+    the exact P2 gradient correction) cuts the additive form's iterations about
+    threefold on tets too.  It is not built for the 16-column block solve: each
+    iteration would add four block applies (0.49 ms each on tets48) and four
+    Chebyshev steps over 273 MB blocks, about 2.6x the iteration's cost."""
+    v, t, ref, ess, nu = _problem(5)
+    K0 = ref.csr().tocsr()
+    P = sp.diags((~ess).astype(float))
+    K = (P @ K0 @ P + sp.diags(ess.astype(float))).tocsr()
+    dinv = 1.0 / K.diagonal()
+    b = ref.load_coil(I0=1.0, q=4)
+    b[ess] = 0.0
+    G, nv = _global_gradient(v, t, ref, local_tables)
+    fixed = np.asarray(abs(G[ess]).sum(axis=0)).ravel() > 0
+    Gf = P @ G[:, np.where(~fixed)[0]]
+    lu = spl.splu((Gf.T @ K @ Gf).tocsc())
+    lmax = 1.1 * abs(spl.eigs(sp.diags(dinv) @ K, k=1, which="LM", return_eigenvectors=False)[0])
+
+    def cheb(r, x, deg=2, ratio=30.0):
+        lo = lmax / ratio
+        th, de = 0.5 * (lmax + lo), 0.5 * (lmax - lo)
+        rho = de / th
+        d = dinv * (r - K @ x) / th
+        x = x + d
+        for _ in range(1, deg):
+            rho2 = 1.0 / (2.0 * th / de - rho)
+            d = rho2 * rho * d + 2.0 * rho2 / de * (dinv * (r - K @ x))
+            x = x + d
+            rho = rho2
+        return x
+
+    def mult(r):
+        z = cheb(r, np.zeros_like(r))
+        z = z + Gf @ lu.solve(Gf.T @ (r - K @ z))
+        return cheb(r, z)
+
+    additive = _pcg(K, b, lambda r: dinv * r + Gf @ lu.solve(Gf.T @ r))
+    multiplicative = _pcg(K, b, mult)
+    assert multiplicative * 2.5 < additive, (additive, multiplicative)
